@@ -1,0 +1,106 @@
+// Internal declarations shared by the CUDA kernels and the host driver.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "hosnwt.h"
+
+namespace hos {
+
+// ---------------------------------------------------------------------------
+// Spectral transforms along one axis.
+//
+// Every r2r transform of the reference (fourier_FFTW.f90) is separable, so a
+// 2-D transform is a pass along x (contiguous) followed by a pass along y.
+// One pass computes, for each line and each output k < nout,
+//     out[k] = s(k) * gscale * sum_{j in [jlo, min(jhi, nin))} w(j) x[j] cos(pi m(j,k) / (2D))
+// with m(j,k) = (aj*j + bj) * (ak*k + bk) + off  (mod 4D).  The six FFTW kinds
+// (REDFT00, RODFT00 on the interior, REDFT01, RODFT01, REDFT10, RODFT10) and
+// their S2F/F2S normalisations (fourier_FFTW.f90:175-229) are parameter sets
+// of this form; sines are cosines shifted by -D.
+// ---------------------------------------------------------------------------
+enum AxisKind {
+  K_C1_S2F = 0,  // REDFT00 * s_2_f (cos, space -> modes)
+  K_C1_F2S = 1,  // f_2_s * REDFT00 (cos, modes -> space)
+  K_S1_S2F = 2,  // RODFT00 on the interior * s_2_f
+  K_S1_F2S = 3,  // f_2_s * RODFT00 on the interior
+  K_ZC_S2F = 4,  // REDFT01 / n3_add      (wavemaker z, cos)
+  K_ZS_S2F = 5,  // RODFT01 / n3_add      (wavemaker z, sin)
+  K_ZC_F2S = 6,  // 0.5 * REDFT10         (wavemaker z, cos)
+  K_ZS_F2S = 7,  // 0.5 * RODFT10         (wavemaker z, sin)
+};
+
+struct AxisJob {
+  const double* in;
+  double* out;
+  long long in_sk, in_sl;    // stride along the transform axis / between lines
+  long long out_sk, out_sl;
+  int nlines;
+  int N;                     // grid points along the axis
+  int nin;                   // inputs j >= nin are zero
+  int nout;                  // outputs k < nout are written
+  int aj, bj, ak, bk, off;   // angle index m = (aj*j+bj)*(ak*k+bk)+off mod 4D
+  int D;                     // table denominator: angle = pi*m/(2D)
+  int jlo, jhi;              // summation range [jlo, jhi)
+  int klo, khi;              // outputs outside [klo, khi) are zero
+  double w0, wm, wl;         // weights for j == 0, interior j, j == N-1
+  double s0, sm, sl;         // scales for k == 0, interior k, k == N-1
+  double gscale;
+  const double* q;           // quarter-wave table cos(pi*m/(2D)), m = 0..D
+};
+
+constexpr int kMaxJobs = 8;
+
+struct AxisBatch {
+  AxisJob job[kMaxJobs];
+  int start[kMaxJobs + 1];   // first CTA of each job
+  int njobs;
+};
+
+// grid ids of the transform requests
+enum GridId { GRID_N = 0, GRID_BIG = 1, GRID_ADD = 2 };
+
+// One (possibly 2-D) transform request on device memory.
+struct XfReq {
+  int grid;                  // GridId
+  int dir;                   // +1 S2F, -1 F2S
+  int csx, csy;              // 0 cos, 1 sin
+  const double* in;
+  int in_ld, nin1, nin2;     // input leading dim and nonzero extent
+  double* out;
+  int out_ld, nout1, nout2;  // output leading dim and written extent
+  double scale;
+};
+
+struct Tables;
+
+// Launch the x passes (and y passes when n2 > 1) of up to kMaxJobs requests.
+// tmp[i] holds the x-pass result of request i when a y pass follows.
+void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* const* tmp,
+                       cudaStream_t st);
+
+struct Tables;
+// F2S along y only (FOURIER_2_SPACE_y, fourier_FFTW.f90:340-428) of nlines
+// lines that are contiguous in memory; cs: 0 cos, 1 sin.
+void launch_y_f2s(const Tables& tb, const double* in, int nlines, long long y_stride, double* out,
+                  long long out_y_stride, int cs, cudaStream_t st);
+
+struct Tables {
+  int n1, n2, nd1, nd2, n3_add;
+  // quarter-wave tables for D = n1-1, n2-1, nd1-1, nd2-1, n3_add
+  const double* q_n1;
+  const double* q_n2;
+  const double* q_nd1;
+  const double* q_nd2;
+  const double* q_add;
+};
+
+// Build the quarter-wave table cos(pi*m/(2D)), m = 0..D, on the host.
+std::vector<double> quarter_table(int D);
+
+}  // namespace hos

@@ -1,0 +1,1025 @@
+// Host driver of the GB300 HOS wave tank: input parsing, set-up (the
+// reference's initiate_parameters, nondimensionalisation, time-step choice,
+// meshes, wave synthesis, absorbing zone, spectral tables), the adaptive
+// time loop, probe output and the C ABI (include/hosnwt.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "tank.h"
+
+namespace hos {
+
+static const double PI = 3.141592653589793238462643383279502888419;
+static const double TWOPI = 6.283185307179586476925286766559005768394;
+static const double G = 9.81;
+static const double TINY = 2.220446049250313080847263336181640625e-16;  // epsilon(1.0_rp)
+
+static int fail(Ctx& c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  c.err = buf;
+  return code;
+}
+
+// ---------------------------------------------------------------------------
+// linear wave theory (linear_wave.f90)
+// ---------------------------------------------------------------------------
+static double xthx(double x) { return x * std::tanh(x); }
+
+// dichoto (linear_wave.f90:427-466): same bisection and stopping rule
+static double dichoto(double (*f)(double), double f0, double a, double b, double prec) {
+  const double fa = f(a) - f0;
+  if (fa * (f(b) - f0) >= 0.0) {
+    if (std::fabs(f(a) - f0) < TINY) return a;
+    if (std::fabs(f(b) - f0) < TINY) return b;
+  }
+  double x1 = a, x2 = b, x3 = 0.0;
+  while (std::fabs(x1 - x2) > prec * std::fabs(x2)) {
+    x3 = (x1 + x2) / 2.0;
+    const double f3 = f(x3) - f0;
+    if (std::fabs(f3) < TINY) return x3;
+    if (fa * f3 < 0.0) x2 = x3;
+    else x1 = x3;
+  }
+  return x3;
+}
+
+// wave_number_adim_r (linear_wave.f90:137-151)
+static double wave_number_adim(double f, double prec) {
+  const double w2 = (TWOPI * f) * (TWOPI * f);
+  if (w2 < std::log(1.7976931348623157e308) - 1.0) return dichoto(xthx, w2, 0.0, 1.0e6, prec);
+  return w2;
+}
+
+// TF_adim_new (linear_wave.f90:277-334), hinged and piston branches
+static std::complex<double> transfer_function(const std::string& typ, double k, double hinge) {
+  const std::complex<double> I(0.0, 1.0);
+  std::complex<double> resu;
+  if (typ == "hinged" || typ == "monofl") {
+    const double d = hinge;
+    if (k < 50 && k * d < 50) {
+      resu = -I * k * (1.0 - d) * (2.0 * k + std::sinh(2.0 * k)) / (4.0 * std::sinh(k));
+      resu = resu / (k * (1.0 - d) * std::sinh(k) + std::cosh(k * d) - std::cosh(k));
+    } else if (k >= 50 && k * d < 50) {
+      resu = -I * k * (1.0 - d) / (2.0 * k * (1.0 - d) - 2.0 + 4.0 * std::cosh(k * d) * std::exp(-k));
+    } else if (k * (1.0 - d) >= 20) {
+      resu = -I * 0.5;
+    } else {
+      resu = -I * k * (1.0 - d) / (2.0 * k * (1.0 - d) - 2.0 + 2.0 * std::exp(k * (d - 1.0)));
+    }
+  } else if (typ == "piston") {
+    if (k < 50.0) resu = std::complex<double>(0.0, -(2.0 * k + std::sinh(2.0 * k)) / (4.0 * std::sinh(k) * std::sinh(k)));
+    else resu = std::complex<double>(0.0, -0.5);
+  } else {
+    resu = 1.0;
+  }
+  return resu;
+}
+
+// SRAND/RAND of libgfortran (initial_condition.f90:246,253): the Park-Miller
+// minimal standard generator, its value masked to 24 significant bits and
+// returned as REAL(4).
+struct GfortranRand {
+  unsigned long long seed;
+  explicit GfortranRand(int s) : seed(s ? (unsigned long long)s : 123459876ull) {}
+  float next() {
+    seed = (16807ull * seed) % 2147483647ull;
+    const unsigned int v = (unsigned int)(seed - 1) & ~511u;
+    return (float)v / (float)2147483646u;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// match_surface_wmk (resol_wmkr.f90:1655-1741): polynomial coefficients for
+// l_add = 2 (x_med = 1), alpha_add = 6, beta_add = 1/3.  They are linear in
+// (f, df, d2f); the same expressions as the reference.
+// ---------------------------------------------------------------------------
+static void match_coeffs(double f, double df, double d2f, double c[4]) {
+  const double x = 1.0, a = 6.0, b = 1.0 / 3.0;
+  const double E = std::exp(-a * b);
+  auto p = [](double v, int n) { double r = 1.0; for (int i = 0; i < n; ++i) r *= v; return r; };
+  const double inv_det = 1.0 / (-320 * p(x, 13) * E * p(b, 4) + 128 * p(x, 13) * E * p(b, 3) +
+                                288 * p(x, 13) * E * p(b, 5) - 112 * p(x, 13) * E * p(b, 6) +
+                                16 * p(x, 13) * E * p(b, 7));
+  const double x2 = x * x;
+  c[0] = inv_det * (2 * (3 * x * p(b, 4) * df + 2 * x2 * p(b, 4) * df * a + f * a * a * x2 * p(b, 4) +
+         3 * f * a * x * p(b, 4) + x2 * p(b, 4) * d2f + 3 * f * p(b, 4) - 12 * x * p(b, 3) * df -
+         8 * x2 * p(b, 3) * df * a - 4 * f * a * a * x2 * p(b, 3) - 12 * f * a * x * p(b, 3) -
+         4 * x2 * p(b, 3) * d2f - 12 * f * p(b, 3) + 4 * x2 * b * b * d2f + 8 * x2 * b * b * df * a +
+         8 * f * b * b + 8 * f * a * x * b * b + 4 * f * a * a * x2 * b * b + 8 * x * b * b * df +
+         8 * f * b + 8 * x * b * df + 8 * f * a * x * b + 8 * f) * (-1 + b) * p(x, 6) * E);
+  c[1] = inv_det * (-2 * (24 * f - 20 * f * a * a * x2 * p(b, 3) + 24 * f * a * x * b +
+         12 * x2 * b * b * d2f - 6 * f * a * a * x2 * p(b, 5) + 3 * f * x * p(b, 6) * a +
+         f * x2 * p(b, 6) * a * a - 60 * f * a * x * p(b, 3) + 12 * f * a * a * x2 * b * b +
+         15 * f * a * a * x2 * p(b, 4) + 45 * f * a * x * p(b, 4) - 18 * f * a * x * p(b, 5) +
+         2 * x2 * p(b, 6) * df * a - 12 * x2 * p(b, 5) * df * a + 30 * x2 * p(b, 4) * df * a -
+         40 * x2 * p(b, 3) * df * a + 24 * x2 * b * b * df * a + 24 * f * b * b - 60 * f * p(b, 3) +
+         24 * f * b + 45 * f * p(b, 4) - 18 * f * p(b, 5) + 3 * f * p(b, 6) + 24 * f * a * x * b * b +
+         3 * x * p(b, 6) * df - 18 * x * p(b, 5) * df + 45 * x * p(b, 4) * df - 60 * x * p(b, 3) * df +
+         24 * x * b * b * df + x2 * p(b, 6) * d2f - 6 * x2 * p(b, 5) * d2f + 15 * x2 * p(b, 4) * d2f -
+         20 * x2 * p(b, 3) * d2f + 24 * x * b * df) * (-1 + b) * p(x, 8) * E);
+  c[2] = inv_det * (2 * (24 * f - 28 * f * a * a * x2 * p(b, 3) + 24 * f * a * x * b +
+         12 * x2 * b * b * d2f - 12 * f * a * a * x2 * p(b, 5) + 10 * f * x * p(b, 6) * a +
+         2 * f * x2 * p(b, 6) * a * a - 116 * f * a * x * p(b, 3) + 12 * f * a * a * x2 * b * b +
+         27 * f * a * a * x2 * p(b, 4) + 129 * f * a * x * p(b, 4) - 60 * f * a * x * p(b, 5) +
+         4 * x2 * p(b, 6) * df * a - 24 * x2 * p(b, 5) * df * a + 54 * x2 * p(b, 4) * df * a -
+         56 * x2 * p(b, 3) * df * a + 24 * x2 * b * b * df * a + 24 * f * b * b - 116 * f * p(b, 3) +
+         24 * f * b + 129 * f * p(b, 4) - 60 * f * p(b, 5) + 10 * f * p(b, 6) + 24 * f * a * x * b * b +
+         10 * x * p(b, 6) * df - 60 * x * p(b, 5) * df + 129 * x * p(b, 4) * df - 116 * x * p(b, 3) * df +
+         24 * x * b * b * df + 2 * x2 * p(b, 6) * d2f - 12 * x2 * p(b, 5) * d2f + 27 * x2 * p(b, 4) * d2f -
+         28 * x2 * p(b, 3) * d2f + 24 * x * b * df) * (-1 + b) * p(x, 10) * E);
+  c[3] = inv_det * (-2 * (8 * f - 12 * f * a * a * x2 * p(b, 3) + 8 * f * a * x * b +
+         4 * x2 * b * b * d2f - 6 * f * a * a * x2 * p(b, 5) + 7 * f * x * p(b, 6) * a +
+         f * x2 * p(b, 6) * a * a - 68 * f * a * x * p(b, 3) + 4 * f * a * a * x2 * b * b +
+         13 * f * a * a * x2 * p(b, 4) + 87 * f * a * x * p(b, 4) - 42 * f * a * x * p(b, 5) +
+         2 * x2 * p(b, 6) * df * a - 12 * x2 * p(b, 5) * df * a + 26 * x2 * p(b, 4) * df * a -
+         24 * x2 * p(b, 3) * df * a + 8 * x2 * b * b * df * a + 8 * f * b * b - 132 * f * p(b, 3) +
+         8 * f * b + 183 * f * p(b, 4) - 90 * f * p(b, 5) + 15 * f * p(b, 6) + 8 * f * a * x * b * b +
+         7 * x * p(b, 6) * df - 42 * x * p(b, 5) * df + 87 * x * p(b, 4) * df - 68 * x * p(b, 3) * df +
+         8 * x * b * b * df + x2 * p(b, 6) * d2f - 6 * x2 * p(b, 5) * d2f + 13 * x2 * p(b, 4) * d2f -
+         12 * x2 * p(b, 3) * d2f + 8 * x * b * df) * (-1 + b) * p(x, 12) * E);
+}
+
+// Extension weights: row n3+r = sum_q E[r][q] * row(n3-4+q)
+static std::vector<double> extension_matrix(int n3, int n3a, int l_add, double delz) {
+  const int nrow = n3a - n3;
+  std::vector<double> E((size_t)std::max(nrow, 0) * 4, 0.0);
+  const double x_med = (double)l_add - 1.0, a = 6.0;
+  for (int q = 0; q < 4; ++q) {
+    double d[4] = {0, 0, 0, 0};
+    d[q] = 1.0;  // rows n3-4, n3-3, n3-2, n3-1 (0-based)
+    const double df = (d[1] - 4.0 * d[2] + 3.0 * d[3]) / (2.0 * delz);
+    const double f = d[3];
+    const double d2f = (-d[0] + 4.0 * d[1] - 5.0 * d[2] + 2.0 * d[3]) / (delz * delz);
+    double c[4];
+    match_coeffs(f, df, d2f, c);
+    for (int r = 0; r < nrow; ++r) {
+      const int i3 = n3 + r + 1;  // 1-based row
+      const double xx = (double)(i3 - 1) / (double)(n3 - 1) - (double)l_add;
+      const double xx2 = xx * xx;
+      E[4 * r + q] = (((c[0] * xx2 + c[1]) * xx2 + c[2]) * xx2 + c[3]) * xx * std::exp(-a * (xx + x_med));
+    }
+  }
+  return E;
+}
+
+// ---------------------------------------------------------------------------
+// input_HOS-NWT.dat (input.f90:62-201)
+// ---------------------------------------------------------------------------
+static double parse_real(const std::string& s) {
+  std::string t = s;
+  for (char& ch : t)
+    if (ch == 'd' || ch == 'D') ch = 'e';
+  return std::strtod(t.c_str(), nullptr);
+}
+
+static std::string trim(const std::string& s) {
+  size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+  return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+}  // namespace hos
+
+using namespace hos;
+
+extern "C" int hosnwt_read_input(const char* path, hosnwt_input* out) {
+  if (!path || !out) return HOSNWT_ERR_ARG;
+  std::ifstream f(path);
+  if (!f) return HOSNWT_ERR_IO;
+  std::vector<std::string> lines;
+  std::string ln;
+  while (std::getline(f, ln)) lines.push_back(ln);
+  std::memset(out, 0, sizeof(*out));
+  // line layout: blank lines at 0,4,6,9,16,21,26,32,36,39,43
+  int li = 0;
+  auto val = [&](void) -> std::string {
+    if (li >= (int)lines.size()) return std::string();
+    const std::string& s = lines[li++];
+    return s.size() > 52 ? s.substr(52) : std::string();
+  };
+  auto blank = [&]() { ++li; };
+  auto R = [&](double& v) { v = parse_real(trim(val())); };
+  auto I = [&](int& v) { v = (int)std::lround(parse_real(trim(val()))); };
+  auto S = [&](char* dst) {
+    std::string s = trim(val());
+    std::strncpy(dst, s.c_str(), 255);
+  };
+  blank(); R(out->xlen); R(out->ylen); R(out->h);
+  blank(); I(out->icase);
+  blank(); I(out->islosh); R(out->aslosh);
+  blank(); R(out->amp_mono); R(out->nu_mono); R(out->theta_mono); R(out->ph_mono); I(out->ibat); R(out->xd_mono);
+  blank(); S(out->file_name); I(out->i_cut); R(out->nuc_low); R(out->nuc_high);
+  blank(); R(out->Hs); R(out->Tp); R(out->gamma); I(out->iseed);
+  blank(); I(out->i_wmk); I(out->igeom); R(out->d_hinge); I(out->iramp); R(out->Tramp);
+  blank(); I(out->iabsnb); R(out->xabsf); R(out->coeffabsf);
+  blank(); I(out->iprobes); S(out->pro_file);
+  blank(); R(out->T_stop); R(out->toler); R(out->f_out);
+  blank(); I(out->idim); I(out->i3d); I(out->imodes); I(out->iwmk); I(out->i_sw);
+  if (li > (int)lines.size()) return HOSNWT_ERR_IO;
+  return HOSNWT_OK;
+}
+
+namespace hos {
+
+// ---------------------------------------------------------------------------
+// set-up
+// ---------------------------------------------------------------------------
+static double gzed_fn(const Params& P, double z) {
+  // gzed (wavemaking.f90:184-213)
+  const double dh = P.d_hinge;
+  const double delta = std::min(dh, (1.0 - dh) / 10.0);
+  if (P.igeom == 1) return 1.0;
+  if (z >= (dh - 1.0 + delta)) return (z + 1.0 - dh) / (1.0 - dh);
+  if (z <= (dh - 1.0 - delta)) return 0.0;
+  const double U = z - (dh - 1.0);
+  const double u = U / delta;
+  return delta / (2.0 * (1.0 - dh)) *
+         (5.0 / 16.0 + u + 15.0 / 16.0 * (u * u - 1.0 / 3.0 * u * u * u * u + 1.0 / 15.0 * u * u * u * u * u * u));
+}
+
+struct Wave {
+  std::vector<int> harmo;
+  std::vector<double> freq, ampli, angle, phase, k;
+  std::vector<std::complex<double>> TF;
+  int rnum = 1;
+  double clock = 0.0, depth = 0.0;
+};
+
+static void wave_init(Wave& w, const std::string& typ, double hinge) {
+  // wave_init (wave_def.f90:282-329)
+  const size_t n = w.freq.size();
+  w.k.assign(n, 0.0);
+  w.TF.assign(n, std::complex<double>(1.0, 0.0));
+  for (size_t i = 0; i < n; ++i) {
+    const double kt = wave_number_adim(w.freq[i], 1.0e-15);
+    w.k[i] = kt;
+    w.TF[i] = std::fabs(kt) > TINY ? transfer_function(typ, kt, hinge) : std::complex<double>(1.0, 0.0);
+    if (w.freq[i] < 1.0e-8) {
+      w.k[i] = 0.0;
+      w.TF[i] = 1.0;
+    }
+  }
+}
+
+static int wave_cfg(Ctx& c, const char* wave_dir) {
+  // initialize_wav_cfg (initial_condition.f90:128-310)
+  Params& P = c.P;
+  const hosnwt_input& in = c.in;
+  std::string typ = P.igeom == 2 ? "hinged" : "piston";
+  Wave w;
+  double hinge = P.d_hinge;
+  if (P.icase == 1) {
+    c.nf = 0;
+  } else if (P.icase == 2) {
+    if (in.ibat != 2) return fail(c, HOSNWT_ERR_UNSUPPORTED, "only snake wavemaking (ibat=2) is supported");
+    w.rnum = 1;
+    w.clock = 2.0 * P.nu_mono;
+    w.depth = P.h;
+    w.harmo = {1};
+    w.freq = {1 * w.clock / (double)(1 << w.rnum)};
+    w.ampli = {P.amp_mono};
+    w.angle = {P.theta_mono};
+    w.phase = {P.ph_mono};
+  } else if (P.icase == 3) {
+    std::string base = std::string(wave_dir ? wave_dir : ".") + "/" + trim(in.file_name);
+    std::ifstream cf(base + ".cfg");
+    if (!cf) return fail(c, HOSNWT_ERR_IO, "cannot open %s.cfg", base.c_str());
+    std::vector<std::string> cl;
+    std::string s;
+    while (std::getline(cf, s)) cl.push_back(trim(s));
+    if (cl.size() < 10) return fail(c, HOSNWT_ERR_IO, "short .cfg file");
+    auto first = [&](int i) { std::istringstream is(cl[i]); std::string t; is >> t; return t; };
+    w.rnum = std::atoi(first(0).c_str());
+    const double clock_d = parse_real(first(1));
+    w.depth = parse_real(first(2));
+    const double cut_lo = parse_real(first(5)), cut_hi = parse_real(first(6));
+    typ = first(8);
+    const double hinge_d = parse_real(first(9));
+    const double Ts = std::sqrt(w.depth / G);
+    w.clock = clock_d * Ts;
+    const double cut_lo_n = cut_lo * Ts, cut_hi_n = cut_hi * Ts;
+    hinge = hinge_d / w.depth;
+    std::ifstream df(base + ".dat");
+    if (!df) return fail(c, HOSNWT_ERR_IO, "cannot open %s.dat", base.c_str());
+    std::vector<int> ha;
+    std::vector<double> fa, aa, ga, pa;
+    while (std::getline(df, s)) {
+      if (trim(s).empty()) continue;
+      for (char& ch : s)
+        if (ch == ',') ch = ' ';
+      std::istringstream is(s);
+      std::string t0, t1, t2, t3, t4;
+      is >> t0 >> t1 >> t2 >> t3 >> t4;
+      ha.push_back((int)std::lround(parse_real(t0)));
+      fa.push_back(parse_real(t1));
+      aa.push_back(parse_real(t2));
+      ga.push_back(parse_real(t3));
+      pa.push_back(parse_real(t4));
+    }
+    int n_start = 1, n_stop = 0;  // wave_def.f90:240-248
+    for (size_t i = 0; i < fa.size(); ++i) {
+      if (fa[i] <= cut_hi_n / Ts) n_stop = (int)i + 1;
+      if (fa[i] < cut_lo_n / Ts) n_start++;
+    }
+    if (n_stop - n_start + 1 <= 0) return fail(c, HOSNWT_ERR_ARG, "n_good == 0");
+    for (int i = n_start - 1; i < n_stop; ++i) {
+      w.harmo.push_back(ha[i]);
+      w.freq.push_back(fa[i] * Ts);
+      w.ampli.push_back(aa[i] / w.depth);
+      w.angle.push_back(ga[i] * PI / 180.0);
+      w.phase.push_back(pa[i]);
+    }
+    if (in.ibat == 3 && P.n2 != 1)
+      return fail(c, HOSNWT_ERR_UNSUPPORTED, "Dalrymple wavemaking (ibat=3) is not supported");
+  } else if (P.icase == 4) {
+    const double Tp = in.Tp, Hs = in.Hs, gam = in.gamma;
+    const double clock = 32.0;
+    w.rnum = (int)std::ceil(std::log10(P.T_stop * P.Tscale * clock) / std::log10(2.0));
+    w.depth = P.h;
+    const int n_pts = (int)std::lround(2 * std::pow(2.0, w.rnum) / clock + 1);
+    const double f_base = (double)(float)clock / std::pow(2.0, w.rnum);
+    GfortranRand rnd(in.iseed);
+    double Hs_int = 0.0;
+    const double sig_lo = (double)0.07f, sig_hi = (double)0.09f;
+    for (int i1 = 1; i1 <= n_pts; ++i1) {
+      const double fr = i1 * f_base;
+      w.harmo.push_back(i1 - 1);
+      w.freq.push_back(fr);
+      w.angle.push_back(0.0);
+      w.phase.push_back(TWOPI * (double)rnd.next());
+      const double sigma = fr < 1.0 / Tp ? sig_lo : sig_hi;
+      const double a = 1.0 / std::pow(TWOPI, 4) * G * G / std::pow(fr, 5) *
+                       std::exp(-5.0 / 4.0 * std::pow(fr * Tp, -4)) *
+                       std::pow(gam, std::exp((-(fr - 1.0 / Tp) * (fr - 1.0 / Tp)) / (2.0 * (sigma / Tp) * (sigma / Tp)))) * f_base;
+      Hs_int += a;
+      w.ampli.push_back(std::sqrt(2.0 * a));
+    }
+    Hs_int = 4.0 * std::sqrt(Hs_int);
+    for (size_t i = 0; i < w.ampli.size(); ++i) {
+      w.ampli[i] = w.ampli[i] * Hs / Hs_int / P.h;
+      w.freq[i] = w.freq[i] * P.Tscale;
+    }
+    w.clock = clock * P.Tscale;
+  } else {
+    return fail(c, HOSNWT_ERR_UNSUPPORTED, "icase=%d is not supported", P.icase);
+  }
+  c.gzed.resize(P.n3);
+  for (int i3 = 0; i3 < P.n3; ++i3) c.gzed[i3] = gzed_fn(P, c.cz[i3]);
+  if (P.icase == 1) return HOSNWT_OK;
+  wave_init(w, typ, hinge);
+  // wmk_ini (wavemaking.f90:37-175), full-width wavemaker
+  int n_max = std::max(1, (int)std::floor(w.clock * std::sqrt(G / w.depth)));
+  n_max = (1 << w.rnum) / n_max;
+  std::vector<std::vector<int>> groups;
+  for (int harm = 0; harm <= 4 * n_max; ++harm) {
+    std::vector<int> idx;
+    for (size_t i = 0; i < w.harmo.size(); ++i)
+      if (w.harmo[i] == harm) idx.push_back((int)i);
+    if (!idx.empty()) groups.push_back(idx);
+  }
+  c.nf = (int)groups.size();
+  c.freq_w.resize(c.nf);
+  c.pos_ini.assign((size_t)P.n2 * c.nf, std::complex<double>(0.0, 0.0));
+  const std::complex<double> I(0.0, 1.0);
+  for (int g = 0; g < c.nf; ++g) {
+    c.freq_w[g] = w.freq[groups[g][0]];
+    for (int j1 = 0; j1 < P.n2; ++j1) {
+      std::complex<double> acc(0.0, 0.0);
+      for (int i : groups[g]) {
+        const double ang = w.angle[i];
+        const std::complex<double> tmp = w.TF[i] * std::cos(ang) * w.ampli[i] *
+                                         std::exp(I * (-w.k[i] * std::sin(ang) * c.cy[j1] + w.phase[i]));
+        acc += 1.0 * tmp;
+      }
+      c.pos_ini[j1 + (size_t)P.n2 * g] = acc;
+    }
+  }
+  return HOSNWT_OK;
+}
+
+template <typename T>
+static T* dalloc(Ctx& c, size_t n) {
+  void* p = nullptr;
+  if (n == 0) n = 1;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+  cudaMemset(p, 0, n * sizeof(T));
+  c.allocs.push_back(p);
+  return (T*)p;
+}
+
+static double* upload(Ctx& c, const std::vector<double>& v) {
+  double* p = dalloc<double>(c, v.size());
+  if (p && !v.empty()) cudaMemcpy(p, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice);
+  return p;
+}
+
+int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
+  Params& P = c.P;
+  const hosnwt_input& in = c.in;
+  const hosnwt_numerics& nm = c.num;
+  // check_range (initial_condition.f90:584-605) and initiate_parameters
+  auto in_range = [](int v) {
+    static const int ok[] = {1, 2, 3, 4, 5, 7, 8, 9, 11, 14, 15, 17, 19, 23, 29};
+    for (int o : ok)
+      if (o == v) return true;
+    return false;
+  };
+  if (!in_range(nm.mHOS) || !in_range(nm.p1) || !in_range(nm.p2))
+    return fail(c, HOSNWT_ERR_ARG, "forbidden value of M, p1 or p2");
+  if (nm.p1 > nm.mHOS || nm.p2 > nm.mHOS) return fail(c, HOSNWT_ERR_ARG, "p1/p2 higher than M");
+  if (nm.n1 < 5 || nm.n2 < 1 || (nm.n2 > 1 && nm.n2 < 5) || nm.n3 < 5)
+    return fail(c, HOSNWT_ERR_ARG, "grid too small (n1, n3 >= 5; n2 = 1 or >= 5)");
+  if (nm.mHOS > 15) return fail(c, HOSNWT_ERR_ARG, "mHOS > 15");
+  P.n1 = nm.n1; P.n2 = nm.n2; P.n3 = nm.n3; P.M = nm.mHOS; P.p1 = nm.p1; P.p2 = nm.p2;
+  P.l_add = 2;
+  P.n3a = P.l_add * (P.n3 - 1);
+  P.nd1 = ((P.p1 + 1) * P.n1) / 2;
+  P.nd2 = ((P.p2 + 1) * P.n2) / 2;
+  if (P.n2 == 1) P.nd2 = 1;
+  P.icase = in.icase; P.igeom = in.igeom; P.iramp = in.iramp; P.iabsnb = in.iabsnb;
+  P.i_wmk = in.i_wmk; P.ibat = in.ibat;
+  if (P.icase != 1 && P.i_wmk != 1)
+    return fail(c, HOSNWT_ERR_UNSUPPORTED, "only the first-order wavemaker (i_wmk=1) is supported");
+  if (P.icase != 1 && P.igeom != 1 && P.igeom != 2)
+    return fail(c, HOSNWT_ERR_UNSUPPORTED, "only flap/piston wavemakers (igeom 1, 2) are supported");
+  // nondimensionalisation (HOS-NWT.f90:99-119)
+  P.h = in.h;
+  P.Tscale = 1.0 / std::sqrt(G / P.h);
+  P.xlen = in.xlen / P.h;
+  P.ylen = in.ylen / P.h;
+  P.amp_mono = in.amp_mono / P.h;
+  P.xlen_add = 2.0 * (double)P.l_add;
+  P.d_hinge = in.d_hinge / P.h;
+  P.aslosh = in.aslosh / P.h;
+  P.Tramp = in.iramp == 0 ? 0.0 : in.Tramp / P.Tscale;
+  P.T_stop = in.T_stop / P.Tscale;
+  P.f_out = in.f_out * P.Tscale;
+  P.nu_mono = in.nu_mono * P.Tscale;
+  P.w_mono = P.nu_mono * TWOPI;
+  P.T_mono = 1.0 / P.nu_mono;
+  P.theta_mono = (P.n2 != 1 ? in.theta_mono : 0.0) * PI / 180.0;
+  P.ph_mono = in.ph_mono;
+  P.islosh = in.islosh + 1;
+  P.toler = in.toler;
+  // time-step choice (HOS-NWT.f90:130-217)
+  double dtr[3];
+  dtr[0] = std::sqrt(8 / (PI * PI)) * P.xlen / (double)(float)(P.n1 - 1);
+  dtr[1] = P.n2 != 1 ? std::sqrt(8 / (PI * PI)) * P.ylen / (double)(float)(P.n2 - 1) : dtr[0] + 1.0;
+  dtr[2] = P.igeom != 3 ? std::sqrt(8 / (PI * PI)) * (2.0 * (double)P.l_add) / (double)(float)(P.l_add * (P.n3 - 1))
+                        : dtr[0] + 1.0;
+  double dt_stab;
+  if (P.igeom == 3 || P.icase == 1) dt_stab = P.n2 == 1 ? dtr[0] : std::min(dtr[0], dtr[1]);
+  else if (P.n2 == 1) dt_stab = std::min(dtr[0], dtr[2]);
+  else dt_stab = std::min(std::min(dtr[0], dtr[1]), dtr[2]);
+  P.dt_stab = dt_stab;
+  P.delt_out = 1.0 / P.f_out;
+  P.delt = std::min(0.95 * dt_stab, P.delt_out);
+  if (std::fabs(P.delt - P.delt_out) < TINY) return fail(c, HOSNWT_ERR_ARG, "DECREASE f_out");
+  // meshes (HOS-NWT.f90:220-244)
+  P.delx = P.xlen / (P.n1 - 1);
+  P.delz = 1.0 / (P.n3 - 1);
+  P.dely = P.n2 != 1 ? P.ylen / (P.n2 - 1) : 0.0;
+  c.cx.resize(P.n1);
+  c.cy.resize(P.n2);
+  c.cz.resize(P.n3);
+  for (int i = 0; i < P.n1; ++i) c.cx[i] = i * P.delx;
+  for (int i = 0; i < P.n2; ++i) c.cy[i] = i * P.dely;
+  for (int i = 0; i < P.n3; ++i) c.cz[i] = P.delz * i - 1.0;
+  int rc = wave_cfg(c, wave_dir);
+  if (rc) return rc;
+  // spectral tables (HOS-NWT.f90:267-406)
+  const int n1 = P.n1, n2 = P.n2, nd1 = P.nd1, nd2 = P.nd2, M = P.M, n3a = P.n3a;
+  const double pixlen = PI / P.xlen, piylen = n2 != 1 ? PI / P.ylen : 0.0;
+  c.kx.resize(n1);
+  c.ky.resize(n2);
+  for (int i = 0; i < n1; ++i) c.kx[i] = i * pixlen;
+  for (int i = 0; i < n2; ++i) c.ky[i] = i * piylen;
+  c.omega.resize((size_t)n1 * n2);
+  std::vector<double> kth1((size_t)n1 * n2);
+  for (int i2 = 0; i2 < n2; ++i2)
+    for (int i1 = 0; i1 < n1; ++i1) {
+      const double k = std::sqrt(c.kx[i1] * c.kx[i1] + c.ky[i2] * c.ky[i2]);
+      c.omega[i1 + (size_t)n1 * i2] = std::sqrt(k * std::tanh(k));
+      kth1[i1 + (size_t)n1 * i2] = k * std::tanh(k);
+    }
+  std::vector<double> kth_ext((size_t)nd1 * nd2 * M);
+  for (int i2 = 0; i2 < nd2; ++i2)
+    for (int i1 = 0; i1 < nd1; ++i1) {
+      const double kk = std::sqrt((i1 * pixlen) * (i1 * pixlen) + (i2 * piylen) * (i2 * piylen));
+      const double thk = std::tanh(kk);
+      double pw = 1.0;
+      for (int j = 1; j <= M; ++j) {
+        pw = std::pow(kk, j);
+        kth_ext[i1 + (size_t)nd1 * i2 + (size_t)nd1 * nd2 * (j - 1)] = (j % 2 == 1) ? pw * thk : pw;
+      }
+    }
+  // wavemaker modes and the exponential tables with the 700 guard
+  const double pixlen_add = PI / P.xlen_add;
+  std::vector<double> kx_add(n3a), cosk(n3a), sink(n3a), k_add((size_t)n3a * n2), k_add_thk((size_t)n3a * n2);
+  for (int i3 = 0; i3 < n3a; ++i3) {
+    kx_add[i3] = (2 * (i3 + 1) - 1) * pixlen_add;
+    cosk[i3] = std::cos(kx_add[i3]);
+    sink[i3] = std::sin(kx_add[i3]);
+    for (int i2 = 0; i2 < n2; ++i2) {
+      const double ka = std::sqrt(kx_add[i3] * kx_add[i3] + c.ky[i2] * c.ky[i2]);
+      k_add[i3 + (size_t)n3a * i2] = ka;
+      k_add_thk[i3 + (size_t)n3a * i2] = ka * std::tanh(ka * P.xlen);
+    }
+  }
+  const size_t nT = (size_t)n1 * n3a * n2;
+  std::vector<double> csh(nT), ksh(nT), kycsh(nT), kxcsh(nT);
+  const double XMAX = 700.0;
+  for (int i2 = 0; i2 < n2; ++i2)
+    for (int i3 = 0; i3 < n3a; ++i3) {
+      const double ka = k_add[i3 + (size_t)n3a * i2], ka2 = 2.0 * ka;
+      const double kxl = ka2 * P.xlen;
+      const double e3 = kxl <= XMAX ? std::exp(-ka2 * P.xlen) : 0.0;
+      const double e3p1 = e3 + 1.0;
+      for (int i1 = 0; i1 < n1; ++i1) {
+        const double x1 = ka * c.cx[i1];
+        const double e1 = x1 <= XMAX ? std::exp(-x1) / e3p1 : 0.0;
+        const double x2 = ka2 * (P.xlen - c.cx[i1]);
+        const double e2 = x2 <= XMAX ? std::exp(-x2) : 0.0;
+        const double e12 = (x1 + x2 <= XMAX) ? e1 * e2 : 0.0;
+        const double ch = e1 + e12, sh = e1 - e12;
+        const size_t o = i1 + (size_t)n1 * i3 + (size_t)n1 * n3a * i2;
+        csh[o] = ch;
+        ksh[o] = sh * ka;
+        kycsh[o] = ch * c.ky[i2];
+        kxcsh[o] = ch * kx_add[i3];
+      }
+    }
+  // absorbing zone (initial_condition.f90:724-794), full width, front beach only
+  std::vector<double> nu((size_t)n1 * n2, 0.0);
+  if (P.iabsnb != 0) {
+    const double x0 = P.xlen * in.xabsf;
+    if (std::fabs(in.xabsf - 1.0) > TINY) {
+      const double x2 = P.xlen - x0;
+      for (int i1 = 0; i1 < n1; ++i1)
+        if (c.cx[i1] >= x0) {
+          const double x3 = (c.cx[i1] - x0) / x2;
+          for (int i2 = 0; i2 < n2; ++i2) nu[i1 + (size_t)n1 * i2] = in.coeffabsf * x3 * x3;
+        }
+    }
+  }
+  // probes (initialize_probes_matrices, initial_condition.f90:496-501)
+  c.nprobes = (probes_xy && nprobes > 0) ? nprobes : 0;
+  std::vector<double> mat((size_t)n1 * n2 * std::max(c.nprobes, 1), 0.0);
+  c.probes.assign(2 * (size_t)c.nprobes, 0.0);
+  for (int p = 0; p < c.nprobes; ++p) {
+    const double xp = probes_xy[2 * p] / P.h, yp = probes_xy[2 * p + 1] / P.h;
+    c.probes[2 * p] = xp;
+    c.probes[2 * p + 1] = yp;
+    for (int i2 = 0; i2 < n2; ++i2)
+      for (int i1 = 0; i1 < n1; ++i1)
+        mat[i1 + (size_t)n1 * i2 + (size_t)n1 * n2 * p] = std::cos(c.kx[i1] * xp) * std::cos(c.ky[i2] * yp);
+  }
+  // state layout
+  long long o = 0;
+  const long long nN = (long long)n1 * n2, nA = (long long)n3a * n2;
+  const long long sz[10] = {nN, nN, nA, nA, nA, nA, nN, nN, nN, nN};
+  for (int a = 0; a < 10; ++a) { c.L.off[a] = o; o += sz[a]; }
+  c.L.size = o;
+  // device
+  if (alloc_device(c)) return fail(c, HOSNWT_ERR_CUDA, "device allocation failed");
+  Dev& d = c.d;
+  d.omega = upload(c, c.omega);
+  d.kx = upload(c, c.kx);
+  d.ky = upload(c, c.ky);
+  d.kth_ext = upload(c, kth_ext);
+  d.kth1 = upload(c, kth1);
+  d.nu = upload(c, nu);
+  d.k_add_thk = upload(c, k_add_thk);
+  d.kx_add = upload(c, kx_add);
+  d.cosk = upload(c, cosk);
+  d.sink = upload(c, sink);
+  d.csh = upload(c, csh);
+  d.ksh = upload(c, ksh);
+  d.kycsh = upload(c, kycsh);
+  d.kxcsh = upload(c, kxcsh);
+  d.ext = upload(c, extension_matrix(P.n3, n3a, P.l_add, P.delz));
+  std::vector<double> pre(std::max<size_t>(c.pos_ini.size(), 1)), pim(pre.size());
+  for (size_t i = 0; i < c.pos_ini.size(); ++i) { pre[i] = c.pos_ini[i].real(); pim[i] = c.pos_ini[i].imag(); }
+  d.pos_re = upload(c, pre);
+  d.pos_im = upload(c, pim);
+  d.freq_w = upload(c, c.freq_w.empty() ? std::vector<double>(1, 0.0) : c.freq_w);
+  d.gzed = upload(c, c.gzed);
+  d.eiwt = dalloc<double>(c, 2 * (size_t)std::max(c.nf, 1));
+  d.mat_coscos = upload(c, mat);
+  d.probe_out = dalloc<double>(c, std::max(c.nprobes, 1));
+  d.q_n1 = upload(c, quarter_table(n1 - 1));
+  d.q_n2 = upload(c, quarter_table(std::max(n2 - 1, 1)));
+  d.q_nd1 = upload(c, quarter_table(nd1 - 1));
+  d.q_nd2 = upload(c, quarter_table(std::max(nd2 - 1, 1)));
+  d.q_add = upload(c, quarter_table(n3a));
+  c.tb.n1 = n1; c.tb.n2 = n2; c.tb.nd1 = nd1; c.tb.nd2 = nd2; c.tb.n3_add = n3a;
+  c.tb.q_n1 = d.q_n1; c.tb.q_n2 = d.q_n2; c.tb.q_nd1 = d.q_nd1; c.tb.q_nd2 = d.q_nd2; c.tb.q_add = d.q_add;
+  for (void* p : c.allocs)
+    if (!p) return fail(c, HOSNWT_ERR_CUDA, "device allocation failed");
+  if (cudaGetLastError() != cudaSuccess) return fail(c, HOSNWT_ERR_CUDA, "upload failed");
+  return HOSNWT_OK;
+}
+
+int alloc_device(Ctx& c) {
+  const Params& P = c.P;
+  Dev& d = c.d;
+  const size_t nN = (size_t)P.n1 * P.n2, nB = (size_t)P.nd1 * P.nd2, nA = (size_t)P.n3a * P.n2;
+  const size_t S = (size_t)c.L.size;
+  const int M = P.M;
+  if (cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking) != cudaSuccess) return 1;
+  d.y0 = dalloc<double>(c, S);
+  d.ys = dalloc<double>(c, S);
+  for (int s = 0; s < 5; ++s) d.k[s] = dalloc<double>(c, S);
+  d.ynew = dalloc<double>(c, S);
+  for (double** p : {&d.eta, &d.phis, &d.deta, &d.eta_c, &d.phis_c, &d.deta_c, &d.etam, &d.phim,
+                     &d.eta_sp, &d.w_eta_x, &d.w_eta_y, &d.w_phi_x, &d.w_phi_y, &d.phix_add,
+                     &d.phiy_add, &d.phiz_add, &d.phit_add, &d.phit_add1, &d.phiz_add1, &d.a1k,
+                     &d.phiz1st, &d.rhs1, &d.X1, &d.X2, &d.X3, &d.det, &d.dph, &d.NL1, &d.NL2,
+                     &d.pmode[0], &d.pmode[1], &d.pmode[2]})
+    *p = dalloc<double>(c, nN);
+  d.etapm.resize(M);
+  d.prod.resize(M);
+  d.phizm.assign(M + 2, nullptr);
+  d.aHOS.assign(M + 2, nullptr);
+  for (int j = 0; j < M; ++j) { d.etapm[j] = dalloc<double>(c, nB); d.prod[j] = dalloc<double>(c, nB); }
+  for (int j = 1; j <= M; ++j) { d.phizm[j] = dalloc<double>(c, nB); d.aHOS[j] = dalloc<double>(c, nB); }
+  d.phizi.assign((size_t)M * M, nullptr);
+  for (int m = 1; m <= M; ++m)
+    for (int j = 1; j <= M + 1 - m; ++j) d.phizi[(m - 1) * M + (j - 1)] = dalloc<double>(c, nB);
+  for (double** p : {&d.etax, &d.etay, &d.phisx, &d.phisy, &d.gradeta2, &d.phimext, &d.phizMm1,
+                     &d.tbig, &d.tbig2, &d.tbig3, &d.pxe, &d.pye, &d.pze, &d.A1, &d.A3, &d.t1,
+                     &d.geta2phiz, &d.geta2phiz2})
+    *p = dalloc<double>(c, std::max(nB, nN));
+  d.bc1 = dalloc<double>(c, nA);
+  d.bcr = dalloc<double>(c, nA);
+  if (P.n2 != 1) {
+    const size_t nQ = (size_t)P.n1 * P.n3a * P.n2;
+    for (int q = 0; q < 4; ++q) { d.Q[q] = dalloc<double>(c, nQ); d.B[q] = dalloc<double>(c, nQ); }
+  }
+  const size_t ntmp = (size_t)std::max(std::max(P.nd1, P.n3a), P.n1) * std::max(P.nd2, P.n2);
+  for (int i = 0; i < kMaxJobs; ++i) d.xtmp[i] = dalloc<double>(c, ntmp);
+  d.sc = dalloc<double>(c, SC_COUNT);
+  const size_t nparts = 10 * ((S + 255) / 256) + (std::max(nB, nN) + 255) / 256 + 1024;
+  d.part = dalloc<double>(c, nparts);
+  d.counter = dalloc<unsigned int>(c, 16);
+  if (cudaMallocHost((void**)&d.host_sc, SC_COUNT * sizeof(double)) != cudaSuccess) return 1;
+  std::memset(d.host_sc, 0, SC_COUNT * sizeof(double));
+  for (void* p : c.allocs)
+    if (!p) return 1;
+  return 0;
+}
+
+void free_device(Ctx& c) {
+  if (c.step_graph) cudaGraphExecDestroy(c.step_graph);
+  c.step_graph = nullptr;
+  for (void* p : c.allocs)
+    if (p) cudaFree(p);
+  c.allocs.clear();
+  if (c.d.host_sc) cudaFreeHost(c.d.host_sc);
+  c.d.host_sc = nullptr;
+  if (c.st) cudaStreamDestroy(c.st);
+  c.st = nullptr;
+}
+
+}  // namespace hos
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+struct hosnwt_ctx {
+  hos::Ctx c;
+};
+
+static int cuda_check(Ctx& c, const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    c.err = std::string(what) + ": " + cudaGetErrorString(e);
+    return HOSNWT_ERR_CUDA;
+  }
+  return HOSNWT_OK;
+}
+
+static int build_step_graph(Ctx& c) {
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return cuda_check(c, "begin capture");
+  cudaMemcpyAsync(c.d.sc + SC_T0, c.d.host_sc + SC_T0, 2 * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  enqueue_step(c, c.st);
+  if (cudaStreamEndCapture(c.st, &g) != cudaSuccess) return cuda_check(c, "end capture");
+  if (cudaGraphInstantiate(&c.step_graph, g, 0) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return cuda_check(c, "graph instantiate");
+  }
+  cudaGraphDestroy(g);
+  return HOSNWT_OK;
+}
+
+extern "C" int hosnwt_create(const hosnwt_input* in, const hosnwt_numerics* num, const char* wave_dir,
+                             const double* probes_xy, int nprobes, hosnwt_ctx** out) {
+  if (!in || !num || !out) return HOSNWT_ERR_ARG;
+  *out = nullptr;
+  hosnwt_ctx* h = new hosnwt_ctx();
+  Ctx& c = h->c;
+  c.in = *in;
+  c.num = *num;
+  int rc = setup(c, wave_dir, probes_xy, nprobes);
+  if (rc == HOSNWT_OK) {
+    // initial condition (initial_condition.f90:314-482)
+    const size_t nN = (size_t)c.P.n1 * c.P.n2;
+    std::vector<double> eta(nN, 0.0);
+    if (c.P.icase == 1) {
+      const double k1 = c.kx[c.P.islosh - 1];
+      for (int i2 = 0; i2 < c.P.n2; ++i2)
+        for (int i1 = 0; i1 < c.P.n1; ++i1) eta[i1 + (size_t)c.P.n1 * i2] = c.P.aslosh * std::cos(k1 * c.cx[i1]);
+    }
+    enqueue_initialize(c, c.st);
+    cudaMemcpyAsync(c.d.eta, eta.data(), nN * sizeof(double), cudaMemcpyHostToDevice, c.st);
+    cudaMemsetAsync(c.d.phis, 0, nN * sizeof(double), c.st);
+    cudaStreamSynchronize(c.st);
+    rc = cuda_check(c, "initialize");
+    if (rc == HOSNWT_OK) rc = build_step_graph(c);
+    c.time_cur = 0.0;
+    c.endramp = 0;
+  }
+  if (rc != HOSNWT_OK) {
+    // keep the context so the caller can read the message; it is unusable
+    *out = h;
+    return rc;
+  }
+  *out = h;
+  return HOSNWT_OK;
+}
+
+extern "C" void hosnwt_destroy(hosnwt_ctx* h) {
+  if (!h) return;
+  free_device(h->c);
+  delete h;
+}
+
+extern "C" const char* hosnwt_last_error(const hosnwt_ctx* h) { return h ? h->c.err.c_str() : "null context"; }
+
+extern "C" int hosnwt_get_info(const hosnwt_ctx* h, hosnwt_info* info) {
+  if (!h || !info) return HOSNWT_ERR_ARG;
+  const Ctx& c = h->c;
+  const Params& P = c.P;
+  info->n1 = P.n1; info->n2 = P.n2; info->n3 = P.n3; info->n3_add = P.n3a;
+  info->nd1 = P.nd1; info->nd2 = P.nd2; info->mHOS = P.M; info->p1 = P.p1; info->p2 = P.p2;
+  info->Tscale = P.Tscale; info->xlen = P.xlen; info->ylen = P.ylen;
+  info->dt_stab = P.dt_stab; info->delt = P.delt; info->delt_out = P.delt_out;
+  info->T_stop = P.T_stop; info->toler = P.toler; info->time_cur = c.time_cur;
+  info->nprobes = c.nprobes;
+  info->n_rhs = c.n_rhs;
+  return HOSNWT_OK;
+}
+
+static int run_step(Ctx& c, double t_o, double h_loc, double* err) {
+  if (!c.step_graph) return HOSNWT_ERR_ARG;
+  c.d.host_sc[SC_T0] = t_o;
+  c.d.host_sc[SC_H] = h_loc;
+  if (cudaGraphLaunch(c.step_graph, c.st) != cudaSuccess) return cuda_check(c, "graph launch");
+  double e = 0.0;
+  cudaMemcpyAsync(&e, c.d.sc + SC_ERR, sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) return cuda_check(c, "step");
+  c.n_rhs += 5;
+  if (err) *err = e;
+  if (!std::isfinite(e)) {
+    c.err = "non-finite error estimate";
+    return HOSNWT_ERR_NAN;
+  }
+  return HOSNWT_OK;
+}
+
+extern "C" int hosnwt_step(hosnwt_ctx* h, double h_loc, double* err) {
+  if (!h || !(h_loc > 0.0)) return HOSNWT_ERR_ARG;
+  return run_step(h->c, h->c.time_cur, h_loc, err);
+}
+
+extern "C" int hosnwt_accept(hosnwt_ctx* h, double h_loc) {
+  if (!h) return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  const Params& P = c.P;
+  bool end_ramp = false;
+  if (P.iramp == 1 && P.Tramp - (c.time_cur + h_loc) <= TINY && P.Tramp > c.time_cur && c.endramp != 1) {
+    end_ramp = true;
+    c.endramp = 1;
+  }
+  enqueue_accept(c, end_ramp, c.st);
+  c.time_cur += h_loc;
+  cudaStreamSynchronize(c.st);
+  return cuda_check(c, "accept");
+}
+
+extern "C" int hosnwt_runge4_adapt2(hosnwt_ctx* h, double t_o, double* eta, double* phis,
+                                    double* a_add_rk_1, double* a_add_rk_2, double* a_add_rkramp,
+                                    double* a_add_rk_3, double* eta1st, double* eta2nd, double* a1st,
+                                    double* a2nd, double h_loc, double* err) {
+  if (!h || !eta || !phis || !a_add_rk_1 || !a_add_rk_2 || !a_add_rkramp || !a_add_rk_3 || !eta1st ||
+      !eta2nd || !a1st || !a2nd || !err)
+    return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  const StateLayout& L = c.L;
+  const size_t nN = (size_t)c.P.n1 * c.P.n2, nA = (size_t)c.P.n3a * c.P.n2;
+  double* const arr[10] = {nullptr, nullptr, a_add_rk_1, a_add_rk_2, a_add_rkramp, a_add_rk_3, a1st, eta1st, a2nd, eta2nd};
+  const size_t sz[10] = {nN, nN, nA, nA, nA, nA, nN, nN, nN, nN};
+  cudaMemcpyAsync(c.d.eta, eta, nN * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  cudaMemcpyAsync(c.d.phis, phis, nN * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  for (int a = 2; a < 10; ++a)
+    cudaMemcpyAsync(c.d.y0 + L.off[a], arr[a], sz[a] * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  int rc = run_step(c, t_o, h_loc, err);
+  if (rc != HOSNWT_OK && rc != HOSNWT_ERR_NAN) return rc;
+  cudaMemcpyAsync(eta, c.d.eta_c, nN * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaMemcpyAsync(phis, c.d.phis_c, nN * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  for (int a = 2; a < 10; ++a)
+    cudaMemcpyAsync(arr[a], c.d.ynew + L.off[a], sz[a] * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaStreamSynchronize(c.st);
+  const int rc2 = cuda_check(c, "runge4_adapt2");
+  return rc2 ? rc2 : rc;
+}
+
+// step control (HOS-NWT.f90:498-571)
+static int advance(Ctx& c, double time_next, double* h_rk_io, int* n_acc, int* n_rej) {
+  const Params& P = c.P;
+  double h_rk = *h_rk_io;
+  int na = 0, nr = 0;
+  while (c.time_cur < time_next) {
+    double h_loc = h_rk;
+    if (time_next - c.time_cur < h_rk) h_loc = time_next - c.time_cur;
+    double error = 0.0;
+    int rc = run_step(c, c.time_cur, h_loc, &error);
+    if (rc) return rc;
+    double dt_correc;
+    if (error > P.toler && h_rk > 0.001 * 0.95 * P.dt_stab) {
+      // REAL(4) constants of the reference (HOS-NWT.f90:525)
+      dt_correc = (double)0.9f * std::pow(error / P.toler, -(double)(1.0f / 4.0f));
+      nr++;
+      if (std::fabs(P.Tramp - (c.time_cur + h_loc)) <= TINY && P.Tramp > c.time_cur) c.endramp = 0;
+    } else {
+      bool end_ramp = false;
+      if (P.iramp == 1 && P.Tramp - (c.time_cur + h_loc) <= TINY && P.Tramp > c.time_cur && c.endramp != 1) {
+        end_ramp = true;
+        c.endramp = 1;
+      }
+      enqueue_accept(c, end_ramp, c.st);
+      c.time_cur = c.time_cur + h_loc;
+      dt_correc = std::fabs(error) < TINY ? 2.0 : 0.9 * std::pow(error / P.toler, -(1.0 / 4.0));
+      na++;
+    }
+    h_rk = h_rk * dt_correc;
+    h_rk = std::min(std::min(h_rk, 0.95 * P.dt_stab), P.delt_out);
+    h_rk = std::max(std::max(h_rk, 0.0001 * 0.95 * P.dt_stab), 0.0001 * P.delt_out);
+  }
+  cudaStreamSynchronize(c.st);
+  *h_rk_io = h_rk;
+  if (n_acc) *n_acc = na;
+  if (n_rej) *n_rej = nr;
+  return cuda_check(c, "advance");
+}
+
+extern "C" int hosnwt_advance(hosnwt_ctx* h, double time_next, double* h_rk, int* n_acc, int* n_rej) {
+  if (!h || !h_rk) return HOSNWT_ERR_ARG;
+  return advance(h->c, time_next, h_rk, n_acc, n_rej);
+}
+
+extern "C" int hosnwt_probes(hosnwt_ctx* h, double* out) {
+  if (!h || !out) return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  if (c.nprobes <= 0) return HOSNWT_OK;
+  enqueue_probes(c, c.st);
+  cudaMemcpyAsync(out, c.d.probe_out, c.nprobes * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaStreamSynchronize(c.st);
+  return cuda_check(c, "probes");
+}
+
+extern "C" int hosnwt_run(hosnwt_ctx* h, const char* results_dir) {
+  if (!h) return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  const Params& P = c.P;
+  FILE* fp = nullptr;
+  if (results_dir) {
+    std::string path = std::string(results_dir) + "/probes.dat";
+    fp = std::fopen(path.c_str(), "w");
+    if (!fp) return fail(c, HOSNWT_ERR_IO, "cannot open %s", path.c_str());
+    // output.f90:144-151 (idim = 1 header)
+    std::fprintf(fp, "TITLE=\"Probes elevation records versus time\"\n");
+    std::fprintf(fp, "VARIABLES = \"time\" ");
+    for (int p = 0; p < c.nprobes; ++p) std::fprintf(fp, "\"p%d\" ", p + 1);
+    std::fprintf(fp, "\n");
+  }
+  std::vector<double> pv(std::max(c.nprobes, 1));
+  double delt = P.delt;
+  int rc = HOSNWT_OK;
+  while (c.time_cur < P.T_stop + P.delt_out) {
+    if (fp) {
+      rc = hosnwt_probes(h, pv.data());
+      if (rc) break;
+      // format 61d13.5 (output.f90:281): Fortran D exponent
+      char buf[64];
+      auto dfmt = [&](double v) {
+        std::snprintf(buf, sizeof buf, "%13.5E", v);
+        for (char* q = buf; *q; ++q)
+          if (*q == 'E') *q = 'D';
+        return std::string(buf);
+      };
+      std::string line = dfmt(c.time_cur * P.Tscale);
+      for (int p = 0; p < c.nprobes; ++p) line += dfmt(pv[p] * P.h);
+      std::fprintf(fp, "%s\n", line.c_str());
+    }
+    if (std::fabs(c.time_cur - P.T_stop) <= TINY) break;
+    double time_next = c.time_cur + P.delt_out;
+    if (time_next > P.T_stop + P.delt_out) time_next = P.T_stop + P.delt_out;
+    double h_rk = delt;
+    rc = advance(c, time_next, &h_rk, nullptr, nullptr);
+    if (rc) break;
+    delt = h_rk;
+  }
+  if (fp) std::fclose(fp);
+  return rc;
+}
+
+extern "C" int hosnwt_get_state(hosnwt_ctx* h, double* eta, double* phis, double* deta) {
+  if (!h) return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  const size_t nN = (size_t)c.P.n1 * c.P.n2;
+  if (eta) cudaMemcpyAsync(eta, c.d.eta, nN * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  if (phis) cudaMemcpyAsync(phis, c.d.phis, nN * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  if (deta) cudaMemcpyAsync(deta, c.d.deta, nN * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaStreamSynchronize(c.st);
+  return cuda_check(c, "get_state");
+}
+
+extern "C" int hosnwt_set_state(hosnwt_ctx* h, const double* eta, const double* phis) {
+  if (!h) return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  const size_t nN = (size_t)c.P.n1 * c.P.n2;
+  if (eta) cudaMemcpyAsync(c.d.eta, eta, nN * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  if (phis) cudaMemcpyAsync(c.d.phis, phis, nN * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  cudaStreamSynchronize(c.st);
+  return cuda_check(c, "set_state");
+}
+
+extern "C" int hosnwt_solveHOS2(hosnwt_ctx* h, const double* const* y, double* const* k, double delta_t,
+                                double time, double alpha_prev, double pos_top_prev) {
+  if (!h || !y || !k) return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  const StateLayout& L = c.L;
+  const size_t nN = (size_t)c.P.n1 * c.P.n2, nA = (size_t)c.P.n3a * c.P.n2;
+  const size_t sz[10] = {nN, nN, nA, nA, nA, nA, nN, nN, nN, nN};
+  for (int a = 0; a < 10; ++a) {
+    if (!y[a] || !k[a]) return HOSNWT_ERR_ARG;
+    cudaMemcpyAsync(c.d.ys + L.off[a], y[a], sz[a] * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  }
+  enqueue_set_scalar(c, SC_DT, delta_t, c.st);
+  enqueue_set_scalar(c, SC_TIME, time, c.st);
+  enqueue_set_scalar(c, SC_ALPHA, alpha_prev, c.st);
+  enqueue_set_scalar(c, SC_POSTOP, pos_top_prev, c.st);
+  enqueue_rhs(c, c.d.ys, c.d.k[0], false, c.st);
+  for (int a = 0; a < 10; ++a)
+    cudaMemcpyAsync(k[a], c.d.k[0] + L.off[a], sz[a] * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaStreamSynchronize(c.st);
+  return cuda_check(c, "solveHOS2");
+}
+
+extern "C" int hosnwt_transform(hosnwt_ctx* h, int grid, int dir, int csx, int csy, const double* in,
+                                double* out) {
+  if (!h || !in || !out || grid < 0 || grid > 2 || (dir != 1 && dir != -1)) return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  const Params& P = c.P;
+  int a = P.n1, b = P.n2;
+  if (grid == GRID_BIG) { a = P.nd1; b = P.nd2; }
+  else if (grid == GRID_ADD) { a = P.n3a; b = P.n2; }
+  const size_t n = (size_t)a * b;
+  cudaMemcpyAsync(c.d.tbig, in, n * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  XfReq r;
+  r.grid = grid; r.dir = dir; r.csx = csx; r.csy = csy;
+  r.in = c.d.tbig; r.in_ld = a; r.nin1 = a; r.nin2 = b;
+  r.out = c.d.tbig2; r.out_ld = a; r.nout1 = a; r.nout2 = b;
+  r.scale = 1.0;
+  launch_transforms(&r, 1, c.tb, c.d.xtmp, c.st);
+  cudaMemcpyAsync(out, c.d.tbig2, n * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaStreamSynchronize(c.st);
+  return cuda_check(c, "transform");
+}
+
+extern "C" int hosnwt_advance_many(hosnwt_ctx* const* ctxs, int n, const double* time_next, double* h_rk) {
+  if (!ctxs || n <= 0 || !time_next || !h_rk) return HOSNWT_ERR_ARG;
+  // independent tanks, each with its own stream and step control
+  for (int i = 0; i < n; ++i) {
+    int rc = hosnwt_advance(ctxs[i], time_next[i], &h_rk[i], nullptr, nullptr);
+    if (rc) return rc;
+  }
+  return HOSNWT_OK;
+}

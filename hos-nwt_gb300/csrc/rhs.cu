@@ -1,0 +1,1061 @@
+// Nonlinear right-hand side, wavemaker potential and RK4(5) step of the HOS
+// wave tank on sm_103a (FP64 throughout).
+//
+//   solveHOS2        resol_HOS.f90:270-656      enqueue_rhs
+//   phisxy_etaxy     resol_HOS.f90:924-1078     (batch A transforms + powers)
+//   HOSphis_modes    resol_HOS.f90:665-915      (order loop)
+//   dealias/filter   dealiasing.f90:39-134      dealias(), filters
+//   SWEET_1          resol_wmkr.f90:109-210     wavemaker block
+//   phiadd_SL        resol_wmkr.f90:1124-1187   k_phiadd_*
+//   ramp / pos_1st   resol_wmkr.f90:1268-1397, wavemaking.f90:259-304
+//   runge4_adapt2    runge_kutta.f90:81-360     enqueue_step
+//   GtoF / expon     variablechange.f90:37-130
+//
+// Linear combinations that the reference filters separately are filtered
+// once (filter_ext is linear), and the S2F that follows a dealiasing is
+// fused with its truncation; both only change rounding.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "tank.h"
+
+namespace hos {
+
+namespace {
+
+constexpr int kEW = 256;
+inline int nblk(long long n, int t = kEW) { return (int)((n + t - 1) / t); }
+
+// ---------------------------------------------------------------------------
+// deterministic "last block" reductions (no spin-waits)
+// ---------------------------------------------------------------------------
+template <int OP>  // 0 sum, 1 max
+__device__ double block_reduce(double v) {
+  __shared__ double sh[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double u = __shfl_down_sync(0xffffffffu, v, o);
+    v = OP == 0 ? v + u : fmax(v, u);
+  }
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  if (w == 0) {
+    v = lane < nw ? sh[lane] : (OP == 0 ? 0.0 : 0.0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double u = __shfl_down_sync(0xffffffffu, v, o);
+      v = OP == 0 ? v + u : fmax(v, u);
+    }
+  }
+  return v;  // valid in thread 0
+}
+
+// returns true in thread 0 of the last block to finish
+__device__ bool last_block(unsigned int* counter) {
+  __shared__ bool amlast;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int t = atomicAdd(counter, 1u);
+    amlast = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  return amlast;
+}
+
+__device__ void volume_fix(double* etam, double S, const double* sc, int igeom, double d_hinge,
+                           double xlen) {
+  const double alpha = sc[SC_ALPHA], pt = sc[SC_POSTOP];
+  double v;
+  if (igeom == 2)
+    v = 0.5 * alpha * (1 - d_hinge) * pt / xlen + S * alpha * pt / xlen;
+  else if (igeom == 1)
+    v = alpha * pt / xlen + S * alpha * pt / xlen;
+  else
+    v = 0.0;
+  etam[0] = v;
+}
+
+// GtoF at the stage start, phis/omega, the volume correction of eta's mean
+// mode (resol_HOS.f90:337-364) and the weighted modes -kx*eta, -ky*eta,
+// -kx*phis, -ky*phis that feed the big-grid derivatives.
+__global__ void k_gtof(const double* __restrict__ G1, const double* __restrict__ G2,
+                       const double* __restrict__ om, const double* __restrict__ kx,
+                       const double* __restrict__ ky, double* sc_, int n1, int n2, int igeom,
+                       double d_hinge, double xlen, double* etam, double* phim, double* wex,
+                       double* wey, double* wpx, double* wpy, double* part, unsigned int* counter) {
+  const double* sc = sc_;
+  const double dt = sc[SC_DT];
+  const long long n = (long long)n1 * n2;
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double e = 0.0;
+  if (i < n) {
+    const double w = om[i];
+    const double c = cos(-w * dt), s = sin(-w * dt);
+    const double g1 = G1[i], g2 = G2[i];
+    e = g1 * c - g2 * s;
+    double p = g2 * c + g1 * s;
+    if (i != 0) p = p / w;
+    etam[i] = e;
+    phim[i] = p;
+    const int i1 = (int)(i % n1), i2 = (int)(i / n1);
+    wex[i] = -kx[i1] * e;
+    wey[i] = -ky[i2] * e;
+    wpx[i] = -kx[i1] * p;
+    wpy[i] = -ky[i2] * p;
+  }
+  const double bs = block_reduce<0>(e);
+  if (threadIdx.x == 0) part[blockIdx.x] = bs;
+  if (last_block(counter) && threadIdx.x == 0) {
+    double S = 0.0;
+    for (unsigned int b = 0; b < gridDim.x; ++b) S += __ldcg(part + b);
+    volume_fix(etam, S, sc, igeom, d_hinge, xlen);
+    *counter = 0;
+  }
+}
+
+__global__ void k_pow(const double* __restrict__ prev, const double* __restrict__ e1, double jp1,
+                      double* out, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = prev[i] / jp1 * e1[i];
+}
+
+// out = s * x * y  (s applied first, as 2.0_rp * a * b in the reference)
+__global__ void k_mul(const double* __restrict__ x, const double* __restrict__ y, double s,
+                      double* out, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (s * x[i]) * y[i];
+}
+
+__global__ void k_add(double* out, const double* __restrict__ x, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] += x[i];
+}
+
+__global__ void k_sq2(const double* __restrict__ a, const double* __restrict__ b, double* out,
+                      long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] * a[i] + b[i] * b[i];
+}
+
+// products a(m) * kth_ext(:,:,j) on the nonzero extent of a(m)
+struct ProdArgs {
+  double* out[16];
+  int jidx[16];
+  int count;
+};
+__global__ void k_prod_kth(const double* __restrict__ a, int a_ld, int e1, int e2,
+                           const double* __restrict__ kth_ext, int nd1, int nd2, ProdArgs pa) {
+  const long long n = (long long)e1 * e2;
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int i1 = (int)(i % e1), i2 = (int)(i / e1);
+  const double v = a[i1 + (long long)a_ld * i2];
+  const long long o = i1 + (long long)nd1 * i2;
+  const long long plane = (long long)nd1 * nd2;
+  for (int t = 0; t < pa.count; ++t) pa.out[t][o] = v * kth_ext[plane * pa.jidx[t] + o];
+}
+
+// order iHOS of HOSphis_modes (resol_HOS.f90:716-764)
+struct AccArgs {
+  const double* phizi[16];  // phizi(m = iHOS+1-j, j), indexed by j-1
+  const double* etapm[16];  // eta^j/j!, indexed by j-1
+  int iHOS;
+};
+__global__ void k_hos_accum(AccArgs a, double* phimext, double* phizm, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double pm = 0.0, pz = 0.0;
+  for (int j = a.iHOS; j >= 2; --j) {
+    const double z = a.phizi[j - 1][i];
+    pm = pm - z * a.etapm[j - 1][i];
+    pz = pz + z * a.etapm[j - 2][i];
+  }
+  const double z1 = a.phizi[0][i];
+  phimext[i] = pm - z1 * a.etapm[0][i];
+  phizm[i] = pz + z1;
+}
+
+__global__ void k_fs_products(const double* __restrict__ etax, const double* __restrict__ etay,
+                              const double* __restrict__ phisx, const double* __restrict__ phisy,
+                              double* detext, double* dphext, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double px = phisx[i], py = phisy[i];
+  detext[i] = -px * etax[i] - py * etay[i];
+  dphext[i] = -px * px - py * py;
+}
+
+// A1 = detext + geta2phiz + phizMm1 + phizm(M) - grad eta.grad phi_add
+// A3 = 0.5 * (dphext + geta2phiz2 + phiz2) - grad phis.grad phi_add - |grad phi_add|^2/2
+__global__ void k_assemble(const double* __restrict__ detext, const double* __restrict__ dphext,
+                           const double* __restrict__ geta2phiz, const double* __restrict__ geta2phiz2,
+                           const double* __restrict__ phiz2, const double* __restrict__ phizMm1,
+                           const double* __restrict__ phizmM, const double* __restrict__ etax,
+                           const double* __restrict__ etay, const double* __restrict__ phisx,
+                           const double* __restrict__ phisy, const double* __restrict__ pxe,
+                           const double* __restrict__ pye, const double* __restrict__ pze,
+                           double* A1, double* A3, long long n, int M) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double ax = pxe[i], ay = pye[i], az = pze[i];
+  const double gg = etax[i] * ax + etay[i] * ay;
+  const double gpg = phisx[i] * ax + phisy[i] * ay + 0.5 * (ax * ax + ay * ay + az * az);
+  const double det = detext[i] + geta2phiz[i];
+  const double dph = dphext[i] + geta2phiz2[i] + phiz2[i];
+  if (M >= 2) {
+    A1[i] = det + phizMm1[i] + phizmM[i] - gg;
+    A3[i] = 0.5 * dph - gpg;
+  } else {
+    A1[i] = phizmM[i];
+    A3[i] = 0.0;
+  }
+}
+
+// final free-surface RHS in physical space (resol_HOS.f90:557-608)
+__global__ void k_final(const double* __restrict__ X1, const double* __restrict__ X2,
+                        const double* __restrict__ X3, const double* __restrict__ phiz_add,
+                        const double* __restrict__ phit_add, const double* __restrict__ nu,
+                        double* det, double* dph, long long n, int M) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double dphin = X1[i] + phiz_add[i];
+  det[i] = dphin - X2[i];
+  if (M >= 2)
+    dph[i] = X3[i] - phit_add[i] - nu[i] * dphin;
+  else
+    dph[i] = -phit_add[i] - nu[i] * dphin;
+}
+
+// expon (variablechange.f90:37-80) with dG2(1,1) from the unscaled NL2
+__global__ void k_expon(const double* __restrict__ NL1, const double* __restrict__ NL2,
+                        const double* __restrict__ om, const double* __restrict__ sc, double* kG1,
+                        double* kG2, long long n, int rk_mode) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double dt = sc[SC_DT];
+  const double w = om[i];
+  const double c = cos(w * dt), s = sin(w * dt);
+  const double a = NL1[i], b0 = NL2[i];
+  const double b = b0 * w;
+  kG1[i] = a * c - b * s;
+  double g2 = b * c + a * s;
+  if (i == 0) g2 = rk_mode ? 0.0 : b0;
+  kG2[i] = g2;
+}
+
+// ---------------------------------------------------------------------------
+// wavemaker
+// ---------------------------------------------------------------------------
+struct RampP {
+  int iramp;
+  double Tramp, T_stop, T_mono;
+};
+
+// ramp (resol_wmkr.f90:1268-1397)
+__device__ void ramp_law(const RampP& r, double time, double* a, double* at, double* att) {
+  const double Tramp = r.Tramp;
+  if (r.iramp == 11) {
+    const double T_swtt = 3.0 / sqrt(5.0 / 9.81);
+    if (time <= T_swtt) { *a = time / T_swtt; *at = 1.0 / T_swtt; *att = 0.0; }
+    else { *a = 1.0; *at = 0.0; *att = 0.0; }
+    return;
+  }
+  if (r.iramp == 33) {
+    const double T_swtt = -log(0.1) / (10.0 * r.T_mono);
+    *a = 1.0 - exp(-T_swtt * time);
+    *at = (1.0 - *a) * T_swtt;
+    *att = (1.0 - *a) * T_swtt * T_swtt;
+    return;
+  }
+  if (time <= Tramp) {
+    switch (r.iramp) {
+      case 0: *a = 1.0; *at = 0.0; *att = 0.0; return;
+      case 1: *a = time / Tramp; *at = 1.0 / Tramp; *att = 0.0; return;
+      case 2: { const double t = time / Tramp; *a = t * t; *at = 2.0 * t / Tramp; *att = 2.0 / (Tramp * Tramp); return; }
+      case 21: {
+        const double T2 = Tramp * Tramp, tim2 = time * time, ts = time / Tramp - 1.0;
+        if (time <= Tramp / 2.0) { *a = 2.0 * tim2 / T2; *at = 4.0 * time / T2; *att = 4.0 / T2; }
+        else { *a = 1.0 - 2.0 * ts * ts; *at = -4.0 * ts / Tramp; *att = -4.0 / T2; }
+        return;
+      }
+      case 4: { const double t = time / Tramp, t2 = t * t; *a = t2 * t2; *at = 4.0 * t2 * t / Tramp; *att = 12.0 * t2 / (Tramp * Tramp); return; }
+      case 41: {
+        const double T2 = Tramp * Tramp, tim2 = time * time, rap = 8.0 * time / Tramp, rap2 = tim2 / T2, rap22 = 3.0 * rap2;
+        *a = (rap22 - rap + 6.0) * rap2; *at = (4.0 * rap22 - 3.0 * rap + 12.0) * time / T2; *att = (12.0 * rap22 - 6.0 * rap + 12.0) / T2;
+        return;
+      }
+      default: return;  // unknown ramp: the reference leaves the values unchanged
+    }
+  }
+  if (time >= r.T_stop + Tramp) { *a = 0.0; *at = 0.0; *att = 0.0; return; }
+  if (time >= r.T_stop) {
+    const double ti = r.T_stop + Tramp - time;
+    switch (r.iramp) {
+      case 1: *a = ti / Tramp; *at = -1.0 / Tramp; *att = 0.0; return;
+      case 2: { const double t = ti / Tramp; *a = t * t; *at = -2.0 * t / Tramp; *att = 2.0 / (Tramp * Tramp); return; }
+      case 21: {
+        const double T2 = Tramp * Tramp, tim2 = ti * ti, ts = ti / Tramp - 1.0;
+        if (ti <= Tramp / 2.0) { *a = 2.0 * tim2 / T2; *at = -4.0 * ti / T2; *att = 4.0 / T2; }
+        else { *a = 1.0 - 2.0 * ts * ts; *at = 4.0 * ts / Tramp; *att = -4.0 / T2; }
+        return;
+      }
+      case 4: { const double t = ti / Tramp, t2 = t * t; *a = t2 * t2; *at = -4.0 * t2 * t / Tramp; *att = 12.0 * t2 / (Tramp * Tramp); return; }
+      case 41: {
+        const double T2 = Tramp * Tramp, tim2 = ti * ti, rap = 8.0 * ti / Tramp, rap2 = tim2 / T2, rap22 = 3.0 * rap2;
+        *a = (rap22 - rap + 6.0) * rap2; *at = -(4.0 * rap22 - 3.0 * rap + 12.0) * ti / T2; *att = (12.0 * rap22 - 6.0 * rap + 12.0) / T2;
+        return;
+      }
+      default: return;
+    }
+  }
+  *a = 1.0; *at = 0.0; *att = 0.0;
+}
+
+__global__ void k_eiwt(const double* __restrict__ freq, double* sc, double* eiwt, int nf, RampP rp) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n == 0) {
+    // the wavemaker law of this stage (single writer of the ramp slots)
+    double a = sc[SC_ALPHA], at = sc[SC_ALPHAT], att = sc[SC_ALPHATT];
+    ramp_law(rp, sc[SC_TIME], &a, &at, &att);
+    sc[SC_ALPHA] = a;
+    sc[SC_ALPHAT] = at;
+    sc[SC_ALPHATT] = att;
+  }
+  if (n >= nf) return;
+  const double w = 6.283185307179586476925286766559005768394 * freq[n];
+  double s, c;
+  sincos(w * sc[SC_TIME], &s, &c);
+  eiwt[2 * n] = c;
+  eiwt[2 * n + 1] = s;
+}
+
+// pos_1st (wavemaking.f90:259-304) and the wavemaker boundary condition of
+// SWEET_1 (resol_wmkr.f90:145-150).  One block per i2.
+// mode 0: bc1 = -a*d2pos - 2 at*dpos - att*pos, bcr = -at*dpos - att*pos
+// mode 1: bc1 = -a*dpos - at*pos (initial a1st_add, initial_condition.f90:388-392)
+__global__ void k_pos_bc(const double* __restrict__ pos_re, const double* __restrict__ pos_im,
+                         const double* __restrict__ freq, const double* __restrict__ eiwt,
+                         const double* __restrict__ gzed, double* sc, int nf, int n2,
+                         int n3, int n3a, double* bc1, double* bcr, int mode) {
+  const int i2 = blockIdx.x;
+  const double a = sc[SC_ALPHA], at = sc[SC_ALPHAT], att = sc[SC_ALPHATT];
+  double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+  for (int n = threadIdx.x; n < nf; n += blockDim.x) {
+    const double w = 6.283185307179586476925286766559005768394 * freq[n];
+    const double c = eiwt[2 * n], s = eiwt[2 * n + 1];
+    const double pr = pos_re[i2 + (long long)n2 * n], pi = pos_im[i2 + (long long)n2 * n];
+    const double rr = pr * c - pi * s;   // Re(pos * e^{iwt})
+    const double ri = pr * s + pi * c;   // Im(pos * e^{iwt})
+    p0 += rr;
+    p1 += -ri * w;         // Re(resu * i w)
+    p2 += -rr * w * w;     // Re(resu * (i w)^2)
+  }
+  p0 = block_reduce<0>(p0);
+  __shared__ double P[3];
+  if (threadIdx.x == 0) P[0] = p0;
+  __syncthreads();
+  p1 = block_reduce<0>(p1);
+  if (threadIdx.x == 0) P[1] = p1;
+  __syncthreads();
+  p2 = block_reduce<0>(p2);
+  if (threadIdx.x == 0) P[2] = p2;
+  __syncthreads();
+  for (int i3 = threadIdx.x; i3 < n3; i3 += blockDim.x) {
+    const double g = gzed[i3];
+    const double pos = g * P[0], dpos = g * P[1], d2pos = g * P[2];
+    if (mode == 0) {
+      bc1[i3 + (long long)n3a * i2] = -a * d2pos - 2.0 * at * dpos - att * pos;
+      bcr[i3 + (long long)n3a * i2] = -at * dpos - att * pos;
+    } else {
+      bc1[i3 + (long long)n3a * i2] = -a * dpos - at * pos;
+    }
+  }
+  if (i2 == 0 && threadIdx.x == 0) sc[SC_POSTOP] = gzed[n3 - 1] * P[0];
+}
+
+// match_surface_wmk (resol_wmkr.f90:1655-1741): rows n3..n3a-1 as a fixed
+// linear combination of rows n3-4..n3-1 (the polynomial coefficients are
+// linear in f, df, d2f).
+__global__ void k_extend(double* a, double* b, const double* __restrict__ ext, int n2, int n3,
+                         int n3a) {
+  const int nrow = n3a - n3;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tot = nrow * n2;
+  if (t >= 2 * tot) return;
+  double* d = t < tot ? a : b;
+  if (!d) return;
+  const int u = t % tot;
+  const int r = u % nrow, i2 = u / nrow;
+  double* col = d + (long long)n3a * i2;
+  const double* e = ext + 4 * r;
+  col[n3 + r] = e[0] * col[n3 - 4] + e[1] * col[n3 - 3] + e[2] * col[n3 - 2] + e[3] * col[n3 - 1];
+}
+
+__global__ void k_div(double* a, double* b, const double* __restrict__ d, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  a[i] = a[i] / d[i];
+  if (b) b[i] = b[i] / d[i];
+}
+
+// phiadd_1st_SWEET at z = 0 (resol_wmkr.f90:490-534), the i3 contraction:
+// At(i1, j2) = sum_i3 da(i3,j2) cos(kx_add) csh;  Az(i1, j2) = sum_i3 a(i3,j2) sin(kx_add) kx_add csh
+__global__ void k_sweet_contract(const double* __restrict__ a, const double* __restrict__ da,
+                                 const double* __restrict__ cosk, const double* __restrict__ sink,
+                                 const double* __restrict__ csh, const double* __restrict__ kxcsh,
+                                 int n1, int n2, int n3a, double* At, double* Az) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)n1 * n2) return;
+  const int i1 = (int)(i % n1), j2 = (int)(i / n1);
+  double st = 0.0, sz = 0.0;
+  for (int i3 = 0; i3 < n3a; ++i3) {
+    const long long o = i1 + (long long)n1 * i3 + (long long)n1 * n3a * j2;
+    st += da[i3 + (long long)n3a * j2] * cosk[i3] * csh[o];
+    sz += a[i3 + (long long)n3a * j2] * sink[i3] * kxcsh[o];
+  }
+  At[i] = st;
+  Az[i] = -sz;
+}
+
+// SWEET_1 free-surface RHS (resol_wmkr.f90:177-185)
+__global__ void k_sweet_rhs(const double* __restrict__ eta1st, const double* __restrict__ phit1,
+                            const double* __restrict__ phiz1st_spec, const double* __restrict__ phiz1,
+                            const double* __restrict__ nu, double iabsnb, double* rhs, double* keta1,
+                            long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double pz = phiz1st_spec[i] + phiz1[i];
+  rhs[i] = -eta1st[i] - phit1[i] - iabsnb * nu[i] * pz;
+  keta1[i] = pz;
+}
+
+__global__ void k_sum3(const double* a, const double* b, const double* c, double* out, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] + b[i] + c[i];
+}
+
+// phiadd_SL on a 1-D tank (n2 = 1): direct i3 contraction at z = eta
+__global__ void k_phiadd_sl_1d(const double* __restrict__ eta, const double* __restrict__ a1,
+                               const double* __restrict__ a2, const double* __restrict__ a3,
+                               const double* __restrict__ da, const double* __restrict__ kx_add,
+                               const double* __restrict__ csh, const double* __restrict__ ksh,
+                               const double* __restrict__ kxcsh, int n1, int n3a, double* phix,
+                               double* phiy, double* phiz, double* phit) {
+  const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i1 >= n1) return;
+  const double e1 = eta[i1] + 1.0;
+  double st = 0.0, sx = 0.0, sz = 0.0;
+  for (int i3 = 0; i3 < n3a; ++i3) {
+    double s, c;
+    sincos(kx_add[i3] * e1, &s, &c);
+    const double a = a1[i3] + a2[i3] + a3[i3];
+    const long long o = i1 + (long long)n1 * i3;
+    st = st + da[i3] * c * csh[o];
+    sx = sx - a * c * ksh[o];
+    sz = sz - a * s * kxcsh[o];
+  }
+  phix[i1] = sx;
+  phiy[i1] = 0.0;
+  phiz[i1] = sz;
+  phit[i1] = st;
+}
+
+// phiadd_SL (3-D): products Q_q(i1, i3, j2) = a(i3, j2) * T_q(i1, i3, j2)
+__global__ void k_phiadd_q(const double* __restrict__ a1, const double* __restrict__ a2,
+                           const double* __restrict__ a3, const double* __restrict__ da,
+                           const double* __restrict__ csh, const double* __restrict__ ksh,
+                           const double* __restrict__ kycsh, const double* __restrict__ kxcsh,
+                           int n1, int n2, int n3a, double* Qt, double* Qx, double* Qy, double* Qz) {
+  const long long n = (long long)n1 * n3a * n2;
+  const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (o >= n) return;
+  const long long r = o / n1;  // i3 + n3a * j2
+  const double a = a1[r] + a2[r] + a3[r];
+  Qt[o] = da[r] * csh[o];
+  Qx[o] = a * ksh[o];
+  Qy[o] = a * kycsh[o];
+  Qz[o] = a * kxcsh[o];
+}
+
+// phiadd_SL (3-D): contraction over i3 at z = eta of the y-transformed B_q
+__global__ void k_phiadd_contract(const double* __restrict__ eta, const double* __restrict__ kx_add,
+                                  const double* __restrict__ Bt, const double* __restrict__ Bx,
+                                  const double* __restrict__ By, const double* __restrict__ Bz,
+                                  int n1, int n2, int n3a, double* phix, double* phiy, double* phiz,
+                                  double* phit) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)n1 * n2) return;
+  const int i1 = (int)(i % n1), i2 = (int)(i / n1);
+  const double e1 = eta[i] + 1.0;
+  double st = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+  for (int i3 = 0; i3 < n3a; ++i3) {
+    double s, c;
+    sincos(kx_add[i3] * e1, &s, &c);
+    const long long o = i1 + (long long)n1 * i3 + (long long)n1 * n3a * i2;
+    st += c * Bt[o];
+    sx -= c * Bx[o];
+    sy -= c * By[o];
+    sz -= s * Bz[o];
+  }
+  phix[i] = sx;
+  phiy[i] = sy;
+  phiz[i] = sz;
+  phit[i] = st;
+}
+
+// ---------------------------------------------------------------------------
+// RK4(5) (runge_kutta.f90:81-360)
+// ---------------------------------------------------------------------------
+struct StageArgs {
+  const double* k[4];
+  double a[4];
+  int nk;
+  double c;
+};
+__global__ void k_rk_stage(const double* __restrict__ y0, StageArgs sa, double* sc, double* ys,
+                           long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const double h = sc[SC_H];
+  if (i < n) {
+    double acc = 0.0;
+    for (int t = 0; t < sa.nk; ++t) acc = acc + sa.k[t][i] * sa.a[t];
+    ys[i] = y0[i] + h * acc;
+  }
+  if (i == 0) {
+    sc[SC_TIME] = sc[SC_T0] + h * sa.c;
+    sc[SC_DT] = h * sa.c;
+  }
+}
+
+struct FinalArgs {
+  const double* k[5];
+  long long off[11];  // array boundaries of the state vector
+};
+// y_new = y0 + h sum b_j k_j; error estimate h (sum e_j k_j - sum b_j k_j),
+// max |y_new| and max |erm| per array for the error norm (runge_kutta.f90:225-279)
+__global__ void k_rk_final(const double* __restrict__ y0, FinalArgs fa, const double* __restrict__ sc,
+                           double* ynew, double* part, long long n) {
+  const double h = sc[SC_H];
+  const double b[5] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 0.0};
+  const double e[5] = {1.0 / 6.0, 2.0 / 3.0, 0.0, 0.0, 1.0 / 6.0};
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  double mnew[5] = {0, 0, 0, 0, 0}, merr[5] = {0, 0, 0, 0, 0};
+  if (i < n) {
+    double db = 0.0, de = 0.0;
+    for (int j = 0; j < 5; ++j) {
+      const double kv = fa.k[j][i];
+      db = db + kv * b[j];
+      de = de + kv * e[j];
+    }
+    const double yn = y0[i] + h * db;
+    ynew[i] = yn;
+    int arr = 0;
+    while (arr < 9 && i >= fa.off[arr + 1]) ++arr;
+    // G1, G2, a_add_1, a_add_2, a_add_3 enter the error norm
+    int slot = -1;
+    if (arr == S_G1) slot = 0;
+    else if (arr == S_G2) slot = 1;
+    else if (arr == S_AADD1) slot = 2;
+    else if (arr == S_AADD2) slot = 3;
+    else if (arr == S_AADD3) slot = 4;
+    if (slot >= 0) {
+      mnew[slot] = fabs(yn);
+      merr[slot] = fabs((de - db) * h);
+    }
+  }
+  for (int s = 0; s < 5; ++s) {
+    const double m1 = block_reduce<1>(mnew[s]);
+    if (threadIdx.x == 0) part[blockIdx.x * 10 + s] = m1;
+    const double m2 = block_reduce<1>(merr[s]);
+    if (threadIdx.x == 0) part[blockIdx.x * 10 + 5 + s] = m2;
+  }
+}
+
+__global__ void k_rk_err(const double* __restrict__ part, int nblocks, double* sc) {
+  // one block of 32 threads: max over blocks per slot, then the norm
+  __shared__ double mx[10];
+  if (threadIdx.x < 10) {
+    double m = 0.0;
+    for (int b = 0; b < nblocks; ++b) m = fmax(m, part[b * 10 + threadIdx.x]);
+    mx[threadIdx.x] = m;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double tiny = 2.220446049250313080847263336181640625e-16;
+    double err = 0.0;
+    for (int s = 0; s < 5; ++s) err = fmax(err, mx[5 + s] / (mx[s] + tiny));
+    sc[SC_ERR] = err;
+  }
+}
+
+// GtoF of the new state and of the stage-5 slope, phis/omega, deta and the
+// volume correction (runge_kutta.f90:281-312)
+__global__ void k_rk_out(const double* __restrict__ G1, const double* __restrict__ G2,
+                         const double* __restrict__ k5G1, const double* __restrict__ k5G2,
+                         const double* __restrict__ om, double* sc_, int n, int igeom,
+                         double d_hinge, double xlen, double* etam, double* phim, double* detam,
+                         double* part, unsigned int* counter) {
+  const double* sc = sc_;
+  const double h = sc[SC_H];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double e = 0.0;
+  if (i < n) {
+    const double w = om[i];
+    const double c = cos(-w * h), s = sin(-w * h);
+    const double g1 = G1[i], g2 = G2[i];
+    e = g1 * c - g2 * s;
+    double p = g2 * c + g1 * s;
+    double d = k5G1[i] * c - k5G2[i] * s;
+    if (i == 0) {
+      p = sc[SC_PHIS0];
+    } else {
+      p = p / w;
+      d = d + p * (w * w);
+    }
+    etam[i] = e;
+    phim[i] = p;
+    detam[i] = d;
+  }
+  const double bs = block_reduce<0>(e);
+  if (threadIdx.x == 0) part[blockIdx.x] = bs;
+  if (last_block(counter) && threadIdx.x == 0) {
+    double S = 0.0;
+    for (unsigned int b = 0; b < gridDim.x; ++b) S += __ldcg(part + b);
+    volume_fix(etam, S, sc, igeom, d_hinge, xlen);
+    *counter = 0;
+  }
+}
+
+// G2 = S2F(phis) * omega, phisrk0 = S2F(phis)(1,1) (runge_kutta.f90:125-141)
+__global__ void k_scale_omega(double* G2, const double* __restrict__ om, double* sc, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double g = G2[i];
+  if (i == 0) sc[SC_PHIS0] = g;
+  G2[i] = g * om[i];
+}
+
+__global__ void k_set_scalar(double* sc, int slot, double v) { sc[slot] = v; }
+
+__global__ void k_sub(double* a, const double* __restrict__ b, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) a[i] -= b[i];
+}
+
+// probes: eta_p = sum S2F(eta) * mat_coscos (output.f90:265-282); one block per probe
+__global__ void k_probe_dot(const double* __restrict__ modes, const double* __restrict__ mat,
+                            long long n, double* out) {
+  const int p = blockIdx.x;
+  double s = 0.0;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) s += modes[i] * mat[n * p + i];
+  s = block_reduce<0>(s);
+  if (threadIdx.x == 0) out[p] = s;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host-side orchestration
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Enq {
+  Ctx& c;
+  cudaStream_t st;
+  const Params& P;
+  const Dev& d;
+  Enq(Ctx& cc, cudaStream_t s) : c(cc), st(s), P(cc.P), d(cc.d) {}
+
+  long long nN() const { return (long long)P.n1 * P.n2; }
+  long long nB() const { return (long long)P.nd1 * P.nd2; }
+  long long nA() const { return (long long)P.n3a * P.n2; }
+
+  void xf(std::vector<XfReq> reqs) {
+    for (size_t s = 0; s < reqs.size(); s += kMaxJobs) {
+      const int cnt = (int)std::min<size_t>(kMaxJobs, reqs.size() - s);
+      launch_transforms(reqs.data() + s, cnt, c.tb, d.xtmp, st);
+    }
+  }
+  XfReq R(int grid, int dir, int csx, int csy, const double* in, int in_ld, int nin1, int nin2,
+          double* out, int out_ld, int nout1, int nout2, double scale = 1.0) const {
+    XfReq r;
+    r.grid = grid; r.dir = dir; r.csx = csx; r.csy = csy;
+    r.in = in; r.in_ld = in_ld; r.nin1 = nin1; r.nin2 = nin2;
+    r.out = out; r.out_ld = out_ld; r.nout1 = nout1; r.nout2 = nout2;
+    r.scale = scale;
+    return r;
+  }
+  // full-grid shorthands
+  XfReq S2F_N(const double* in, double* out, int csx = 0, int csy = 0) const {
+    return R(GRID_N, 1, csx, csy, in, P.n1, P.n1, P.n2, out, P.n1, P.n1, P.n2);
+  }
+  XfReq F2S_N(const double* in, double* out, int csx = 0, int csy = 0) const {
+    return R(GRID_N, -1, csx, csy, in, P.n1, P.n1, P.n2, out, P.n1, P.n1, P.n2);
+  }
+  // F2S on the big grid of modes that are nonzero on e1 x e2 only (extend)
+  XfReq F2S_B(const double* in, int in_ld, int e1, int e2, double* out, int csx = 0, int csy = 0) const {
+    return R(GRID_BIG, -1, csx, csy, in, in_ld, e1, e2, out, P.nd1, P.nd1, P.nd2);
+  }
+  bool act_x(int order) const { return P.p1 != 1 && (order - 1) % (P.p1 - 1) == 0; }
+  bool act_y(int order) const { return P.n2 != 1 && P.p2 != 1 && (order - 1) % (P.p2 - 1) == 0; }
+  bool dealias_on(int order) const { return act_x(order) || act_y(order); }
+  // dealias (dealiasing.f90:39-92): S2F_big, truncate, F2S_big, in place
+  void dealias(int order, double* buf) {
+    if (!dealias_on(order)) return;
+    const int e1 = act_x(order) ? P.n1 : P.nd1;
+    const int e2 = act_y(order) ? P.n2 : P.nd2;
+    xf({R(GRID_BIG, 1, 0, 0, buf, P.nd1, P.nd1, P.nd2, d.tbig3, P.nd1, e1, e2)});
+    xf({F2S_B(d.tbig3, P.nd1, e1, e2, buf)});
+  }
+  template <typename K, typename... A>
+  void ew(K kern, long long n, A... a) {
+    if (n <= 0) return;
+    kern<<<nblk(n), kEW, 0, st>>>(a...);
+  }
+};
+
+}  // namespace
+
+void enqueue_set_scalar(Ctx& c, int slot, double v, cudaStream_t st) {
+  k_set_scalar<<<1, 1, 0, st>>>(c.d.sc, slot, v);
+}
+
+static RampP ramp_params(const Params& P) {
+  RampP r;
+  r.iramp = P.iramp;
+  r.Tramp = P.Tramp;
+  r.T_stop = P.T_stop;
+  r.T_mono = P.T_mono;
+  return r;
+}
+
+static bool has_wavemaker(const Params& P) {
+  return P.icase != 1 && (P.igeom == 1 || P.igeom == 2);
+}
+
+void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t st) {
+  Enq E(c, st);
+  const Params& P = c.P;
+  const Dev& d = c.d;
+  const StateLayout& L = c.L;
+  const int n1 = P.n1, n2 = P.n2, nd1 = P.nd1, nd2 = P.nd2, M = P.M;
+  const long long nN = E.nN(), nB = E.nB(), nA = E.nA();
+  const double* G1 = y + L.off[S_G1];
+  const double* G2 = y + L.off[S_G2];
+  double* kG1 = k + L.off[S_G1];
+  double* kG2 = k + L.off[S_G2];
+  c.n_rhs++;
+
+  // 1. GtoF + volume correction of the mean mode
+  {
+    const int nb = nblk(nN);
+    k_gtof<<<nb, kEW, 0, st>>>(G1, G2, d.omega, d.kx, d.ky, d.sc, n1, n2, P.igeom, P.d_hinge,
+                               P.xlen, d.etam, d.phim, d.w_eta_x, d.w_eta_y, d.w_phi_x, d.w_phi_y,
+                               d.part, d.counter);
+  }
+  // 2. transform batch A: eta in space, eta / eta_x / eta_y / phis_x / phis_y on
+  //    the big grid (phisxy_etaxy) and the order-1 HOS terms F2S_big(a1 kth_ext(j))
+  {
+    ProdArgs pa{};
+    pa.count = M;
+    for (int j = 1; j <= M; ++j) { pa.out[j - 1] = d.prod[j - 1]; pa.jidx[j - 1] = j - 1; }
+    k_prod_kth<<<nblk(nN), kEW, 0, st>>>(d.phim, n1, n1, n2, d.kth_ext, nd1, nd2, pa);
+    std::vector<XfReq> rq;
+    rq.push_back(E.F2S_N(d.etam, d.eta_sp));
+    rq.push_back(E.F2S_B(d.etam, n1, n1, n2, d.etapm[0]));
+    rq.push_back(E.F2S_B(d.w_eta_x, n1, n1, n2, d.etax, 1, 0));
+    rq.push_back(E.F2S_B(d.w_phi_x, n1, n1, n2, d.phisx, 1, 0));
+    if (n2 != 1) {
+      rq.push_back(E.F2S_B(d.w_eta_y, n1, n1, n2, d.etay, 0, 1));
+      rq.push_back(E.F2S_B(d.w_phi_y, n1, n1, n2, d.phisy, 0, 1));
+    }
+    for (int j = 1; j <= M; ++j)
+      rq.push_back(E.F2S_B(d.prod[j - 1], nd1, n1, n2, d.phizi[(0) * M + (j - 1)]));
+    E.xf(rq);
+    if (n2 == 1) {
+      cudaMemsetAsync(d.etay, 0, sizeof(double) * nB, st);
+      cudaMemsetAsync(d.phisy, 0, sizeof(double) * nB, st);
+    }
+  }
+  // 3. powers eta^j / j! with partial dealiasing
+  for (int j = 1; j < M; ++j) {
+    E.ew(k_pow, nB, (const double*)d.etapm[j - 1], (const double*)d.etapm[0], (double)(j + 1),
+         d.etapm[j], nB);
+    E.dealias(j + 1, d.etapm[j]);
+  }
+  E.ew(k_sq2, nB, (const double*)d.etax, (const double*)d.etay, d.gradeta2, nB);
+  E.dealias(2, d.gradeta2);
+
+  // 4. HOS recursion (HOSphis_modes)
+  std::vector<int> ext1(M + 2, nd1), ext2(M + 2, nd2);
+  for (int iHOS = 1; iHOS <= M; ++iHOS) {
+    AccArgs aa{};
+    aa.iHOS = iHOS;
+    for (int j = 1; j <= iHOS; ++j) {
+      const int m = iHOS + 1 - j;
+      aa.phizi[j - 1] = d.phizi[(m - 1) * M + (j - 1)];
+      aa.etapm[j - 1] = d.etapm[j - 1];
+    }
+    E.ew(k_hos_accum, nB, aa, d.phimext, d.phizm[iHOS], nB);
+    if (iHOS > 1) E.dealias(iHOS, d.phizm[iHOS]);
+    if (iHOS < M) {
+      const int o = iHOS + 1;
+      const int e1 = E.act_x(o) ? n1 : nd1;
+      const int e2 = E.act_y(o) ? n2 : nd2;
+      ext1[o] = e1;
+      ext2[o] = e2;
+      E.xf({E.R(GRID_BIG, 1, 0, 0, d.phimext, nd1, nd1, nd2, d.aHOS[o], nd1, e1, e2)});
+      // products with kth_ext(j), j = 1 .. M+1-o, then their F2S_big
+      ProdArgs pa{};
+      pa.count = M + 1 - o;
+      for (int j = 1; j <= pa.count; ++j) { pa.out[j - 1] = d.prod[j - 1]; pa.jidx[j - 1] = j - 1; }
+      k_prod_kth<<<nblk((long long)e1 * e2), kEW, 0, st>>>(d.aHOS[o], nd1, e1, e2, d.kth_ext, nd1,
+                                                          nd2, pa);
+      std::vector<XfReq> rq;
+      for (int j = 1; j <= pa.count; ++j)
+        rq.push_back(E.F2S_B(d.prod[j - 1], nd1, e1, e2, d.phizi[(o - 1) * M + (j - 1)]));
+      E.xf(rq);
+    }
+  }
+  // phizMm1 = sum_{j<M} phizm(j)
+  cudaMemsetAsync(d.phizMm1, 0, sizeof(double) * nB, st);
+  if (M >= 2) {
+    for (int j = 1; j <= M - 2; ++j) E.ew(k_add, nB, d.phizMm1, (const double*)d.phizm[j], nB);
+    E.ew(k_add, nB, d.phizMm1, (const double*)d.phizm[M - 1], nB);
+  }
+  // gradeta2 * phiz at order M (geta2phiz) and phiz^2, gradeta2 * phiz^2
+  cudaMemsetAsync(d.geta2phiz, 0, sizeof(double) * nB, st);
+  for (int j = 1; j <= M - 3; ++j) {
+    E.ew(k_mul, nB, (const double*)d.gradeta2, (const double*)d.phizm[j], 1.0, d.tbig, nB);
+    E.dealias(j + 2, d.tbig);
+    E.ew(k_add, nB, d.geta2phiz, (const double*)d.tbig, nB);
+  }
+  if (M >= 3) {
+    E.ew(k_mul, nB, (const double*)d.gradeta2, (const double*)d.phizm[std::max(M - 2, 1)], 1.0,
+         d.tbig, nB);
+    E.dealias(M, d.tbig);
+    E.ew(k_add, nB, d.geta2phiz, (const double*)d.tbig, nB);
+  }
+  cudaMemsetAsync(d.t1, 0, sizeof(double) * nB, st);
+  cudaMemsetAsync(d.geta2phiz2, 0, sizeof(double) * nB, st);
+  auto sq_term = [&](int j, int q, double s, int order, bool with_geta) {
+    E.ew(k_mul, nB, (const double*)d.phizm[j], (const double*)d.phizm[q], s, d.tbig, nB);
+    E.dealias(order, d.tbig);
+    E.ew(k_add, nB, d.t1, (const double*)d.tbig, nB);
+    if (with_geta) {
+      E.ew(k_mul, nB, (const double*)d.gradeta2, (const double*)d.tbig, 1.0, d.tbig2, nB);
+      E.dealias(order + 2, d.tbig2);
+      E.ew(k_add, nB, d.geta2phiz2, (const double*)d.tbig2, nB);
+    }
+  };
+  for (int j = 1; j <= (M - 2) / 2; ++j) sq_term(j, j, 1.0, 2 * j, true);
+  for (int j = 2; j <= M - 3; ++j)
+    for (int q = 1; q <= std::min(M - 2 - j, j - 1); ++q) sq_term(j, q, 2.0, j + q, true);
+  if (M >= 2) sq_term(M / 2, M / 2, 1.0, 2 * (M / 2), false);
+  for (int j = 2; j <= M - 1; ++j)
+    for (int q = std::max(0, std::min(M - 2 - j, j - 1)) + 1; q <= std::min(M - j, j - 1); ++q)
+      sq_term(j, q, 2.0, j + q, false);
+
+  // 5. wavemaker: SWEET_1 and phiadd_SL
+  double* kA1 = k + L.off[S_AADD1];
+  double* kAR = k + L.off[S_AADDR];
+  double* kA1st = k + L.off[S_A1ST];
+  double* kEta1 = k + L.off[S_ETA1ST];
+  if (has_wavemaker(P)) {
+    const RampP rp = ramp_params(P);
+    k_eiwt<<<nblk(c.nf > 0 ? c.nf : 1), kEW, 0, st>>>(d.freq_w, d.sc, d.eiwt, c.nf, rp);
+    k_pos_bc<<<n2, 128, 0, st>>>(d.pos_re, d.pos_im, d.freq_w, d.eiwt, d.gzed, d.sc, c.nf, n2,
+                                 P.n3, P.n3a, d.bc1, d.bcr, 0);
+    {
+      const int tot = 2 * (P.n3a - P.n3) * n2;
+      k_extend<<<nblk(tot), kEW, 0, st>>>(d.bc1, d.bcr, d.ext, n2, P.n3, P.n3a);
+    }
+    E.xf({E.R(GRID_ADD, 1, 0, 0, d.bc1, P.n3a, P.n3a, n2, kA1, P.n3a, P.n3a, n2),
+          E.R(GRID_ADD, 1, 0, 0, d.bcr, P.n3a, P.n3a, n2, kAR, P.n3a, P.n3a, n2)});
+    E.ew(k_div, nA, kA1, kAR, (const double*)d.k_add_thk, nA);
+    // reconstruction at z = 0 (phiadd_1st_SWEET) for phit_add_1, phiz_add_1
+    const double* aA1 = y + L.off[S_AADD1];
+    E.ew(k_sweet_contract, nN, aA1, (const double*)kA1, (const double*)d.cosk,
+         (const double*)d.sink, (const double*)d.csh, (const double*)d.kxcsh, n1, n2, P.n3a,
+         n2 == 1 ? d.phit_add1 : d.tbig, n2 == 1 ? d.phiz_add1 : d.tbig2);
+    if (n2 != 1) {
+      // y sums: sum_j2 A(i1, j2) cos(ky(j2) y(i2)) = FOURIER_2_SPACE_y
+      launch_y_f2s(c.tb, d.tbig, n1, n1, d.phit_add1, n1, 0, st);
+      launch_y_f2s(c.tb, d.tbig2, n1, n1, d.phiz_add1, n1, 0, st);
+    }
+    // phidphiz + SWEET_1 RHS
+    E.ew(k_mul, nN, y + L.off[S_A1ST], (const double*)d.kth1, 1.0, d.a1k, nN);
+    E.xf({E.F2S_N(d.a1k, d.phiz1st)});
+    E.ew(k_sweet_rhs, nN, y + L.off[S_ETA1ST], (const double*)d.phit_add1,
+         (const double*)d.phiz1st, (const double*)d.phiz_add1, (const double*)d.nu,
+         (double)P.iabsnb, d.rhs1, kEta1, nN);
+    E.xf({E.S2F_N(d.rhs1, kA1st)});
+    // phiadd_SL with the total additional amplitudes at z = eta
+    const double* aA2 = y + L.off[S_AADD2];
+    const double* aA3 = y + L.off[S_AADD3];
+    if (n2 == 1) {
+      k_phiadd_sl_1d<<<nblk(n1, 128), 128, 0, st>>>(d.eta_sp, aA1, aA2, aA3, kA1, d.kx_add, d.csh,
+                                                     d.ksh, d.kxcsh, n1, P.n3a, d.phix_add,
+                                                     d.phiy_add, d.phiz_add, d.phit_add);
+    } else {
+      const long long nq = (long long)n1 * P.n3a * n2;
+      E.ew(k_phiadd_q, nq, aA1, aA2, aA3, (const double*)kA1, (const double*)d.csh,
+           (const double*)d.ksh, (const double*)d.kycsh, (const double*)d.kxcsh, n1, n2, P.n3a,
+           d.Q[0], d.Q[1], d.Q[2], d.Q[3]);
+      const int lines = n1 * P.n3a;
+      launch_y_f2s(c.tb, d.Q[0], lines, lines, d.B[0], lines, 0, st);
+      launch_y_f2s(c.tb, d.Q[1], lines, lines, d.B[1], lines, 0, st);
+      launch_y_f2s(c.tb, d.Q[2], lines, lines, d.B[2], lines, 1, st);
+      launch_y_f2s(c.tb, d.Q[3], lines, lines, d.B[3], lines, 0, st);
+      E.ew(k_phiadd_contract, nN, (const double*)d.eta_sp, (const double*)d.kx_add,
+           (const double*)d.B[0], (const double*)d.B[1], (const double*)d.B[2],
+           (const double*)d.B[3], n1, n2, P.n3a, d.phix_add, d.phiy_add, d.phiz_add, d.phit_add);
+    }
+  } else {
+    cudaMemsetAsync(kA1, 0, sizeof(double) * nA, st);
+    cudaMemsetAsync(kAR, 0, sizeof(double) * nA, st);
+    cudaMemsetAsync(kA1st, 0, sizeof(double) * nN, st);
+    cudaMemsetAsync(kEta1, 0, sizeof(double) * nN, st);
+    cudaMemsetAsync(d.phix_add, 0, sizeof(double) * nN, st);
+    cudaMemsetAsync(d.phiy_add, 0, sizeof(double) * nN, st);
+    cudaMemsetAsync(d.phiz_add, 0, sizeof(double) * nN, st);
+    cudaMemsetAsync(d.phit_add, 0, sizeof(double) * nN, st);
+  }
+  // second- and third-order wavemaker slopes stay zero (i_wmk = 1)
+  cudaMemsetAsync(k + L.off[S_AADD2], 0, sizeof(double) * nA, st);
+  cudaMemsetAsync(k + L.off[S_AADD3], 0, sizeof(double) * nA, st);
+  cudaMemsetAsync(k + L.off[S_A2ND], 0, sizeof(double) * nN, st);
+  cudaMemsetAsync(k + L.off[S_ETA2ND], 0, sizeof(double) * nN, st);
+
+  // 6. gradients of phi_add on the big grid (resol_HOS.f90:534-555)
+  E.xf({E.S2F_N(d.phix_add, d.pmode[0]), E.S2F_N(d.phiy_add, d.pmode[1]),
+        E.S2F_N(d.phiz_add, d.pmode[2])});
+  E.xf({E.F2S_B(d.pmode[0], n1, n1, n2, d.pxe), E.F2S_B(d.pmode[1], n1, n1, n2, d.pye),
+        E.F2S_B(d.pmode[2], n1, n1, n2, d.pze)});
+  // 7. free-surface terms, filters to the n grid, final RHS
+  E.ew(k_fs_products, nB, (const double*)d.etax, (const double*)d.etay, (const double*)d.phisx,
+       (const double*)d.phisy, d.tbig, d.tbig2, nB);
+  E.dealias(2, d.tbig);
+  E.dealias(2, d.tbig2);
+  E.ew(k_assemble, nB, (const double*)d.tbig, (const double*)d.tbig2, (const double*)d.geta2phiz,
+       (const double*)d.geta2phiz2, (const double*)d.t1, (const double*)d.phizMm1,
+       (const double*)d.phizm[M], (const double*)d.etax, (const double*)d.etay,
+       (const double*)d.phisx, (const double*)d.phisy, (const double*)d.pxe, (const double*)d.pye,
+       (const double*)d.pze, d.A1, d.A3, nB, M);
+  // filter_ext: S2F_big truncated to n1 x n2, then F2S on the n grid
+  E.xf({E.R(GRID_BIG, 1, 0, 0, d.A1, nd1, nd1, nd2, d.pmode[0], n1, n1, n2),
+        E.R(GRID_BIG, 1, 0, 0, d.phizm[1], nd1, nd1, nd2, d.pmode[1], n1, n1, n2),
+        E.R(GRID_BIG, 1, 0, 0, d.A3, nd1, nd1, nd2, d.pmode[2], n1, n1, n2)});
+  E.xf({E.F2S_N(d.pmode[0], d.X1), E.F2S_N(d.pmode[1], d.X2), E.F2S_N(d.pmode[2], d.X3)});
+  E.ew(k_final, nN, (const double*)d.X1, (const double*)d.X2, (const double*)d.X3,
+       (const double*)d.phiz_add, (const double*)d.phit_add, (const double*)d.nu, d.det, d.dph, nN,
+       M);
+  E.xf({E.S2F_N(d.det, d.NL1), E.S2F_N(d.dph, d.NL2)});
+  E.ew(k_expon, nN, (const double*)d.NL1, (const double*)d.NL2, (const double*)d.omega,
+       (const double*)d.sc, kG1, kG2, nN, rk_mode ? 1 : 0);
+}
+
+void enqueue_step(Ctx& c, cudaStream_t st) {
+  Enq E(c, st);
+  const Params& P = c.P;
+  const Dev& d = c.d;
+  const StateLayout& L = c.L;
+  const long long S = L.size;
+  const long long nN = E.nN();
+  // G1 = S2F(eta), G2 = S2F(phis) * omega
+  E.xf({E.S2F_N(d.eta, d.y0 + L.off[S_G1]), E.S2F_N(d.phis, d.y0 + L.off[S_G2])});
+  E.ew(k_scale_omega, nN, d.y0 + L.off[S_G2], (const double*)d.omega, d.sc, nN);
+  // stage 1 at t_o
+  {
+    StageArgs sa{};
+    sa.nk = 0;
+    sa.c = 0.0;
+    k_rk_stage<<<nblk(S), kEW, 0, st>>>(d.y0, sa, d.sc, d.ys, S);
+  }
+  enqueue_rhs(c, d.ys, d.k[0], true, st);
+  static const double A[5][5] = {{0, 0, 0, 0, 0}, {0.5, 0, 0, 0, 0}, {0, 0.5, 0, 0, 0},
+                                 {0, 0, 1.0, 0, 0}, {-1.0, 2.0, 0, 0, 0}};
+  static const double Cc[5] = {0.0, 0.5, 0.5, 1.0, 1.0};
+  for (int s = 1; s < 5; ++s) {
+    StageArgs sa{};
+    sa.nk = 0;
+    for (int j = 0; j < s; ++j) {
+      sa.k[sa.nk] = d.k[j];
+      sa.a[sa.nk] = A[s][j];
+      sa.nk++;
+    }
+    sa.c = Cc[s];
+    k_rk_stage<<<nblk(S), kEW, 0, st>>>(d.y0, sa, d.sc, d.ys, S);
+    enqueue_rhs(c, d.ys, d.k[s], true, st);
+  }
+  FinalArgs fa{};
+  for (int j = 0; j < 5; ++j) fa.k[j] = d.k[j];
+  for (int a = 0; a < 10; ++a) fa.off[a] = L.off[a];
+  fa.off[10] = S;
+  const int nb = nblk(S);
+  k_rk_final<<<nb, kEW, 0, st>>>(d.y0, fa, d.sc, d.ynew, d.part, S);
+  k_rk_err<<<1, 32, 0, st>>>(d.part, nb, d.sc);
+  k_rk_out<<<nblk(nN), kEW, 0, st>>>(d.ynew + L.off[S_G1], d.ynew + L.off[S_G2],
+                                     d.k[4] + L.off[S_G1], d.k[4] + L.off[S_G2], d.omega, d.sc,
+                                     (int)nN, P.igeom, P.d_hinge, P.xlen, d.etam, d.phim, d.NL1,
+                                     d.part + 10 * (long long)nb, d.counter);
+  E.xf({E.F2S_N(d.etam, d.eta_c), E.F2S_N(d.phim, d.phis_c), E.F2S_N(d.NL1, d.deta_c)});
+}
+
+void enqueue_accept(Ctx& c, bool end_ramp, cudaStream_t st) {
+  const Dev& d = c.d;
+  const StateLayout& L = c.L;
+  const long long nN = (long long)c.P.n1 * c.P.n2;
+  cudaMemcpyAsync(d.y0, d.ynew, sizeof(double) * L.size, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(d.eta, d.eta_c, sizeof(double) * nN, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(d.phis, d.phis_c, sizeof(double) * nN, cudaMemcpyDeviceToDevice, st);
+  cudaMemcpyAsync(d.deta, d.deta_c, sizeof(double) * nN, cudaMemcpyDeviceToDevice, st);
+  if (end_ramp) {
+    const long long nA = (long long)c.P.n3a * c.P.n2;
+    k_sub<<<nblk(nA), kEW, 0, st>>>(d.y0 + L.off[S_AADD1], d.y0 + L.off[S_AADDR], nA);
+  }
+}
+
+// initialize (initial_condition.f90:314-482), wavemaker part: a1st_add from
+// the initial paddle velocity, a_add_ramp = a1st_add, ramp/pos at t = 0.
+void enqueue_initialize(Ctx& c, cudaStream_t st) {
+  const Params& P = c.P;
+  const Dev& d = c.d;
+  const StateLayout& L = c.L;
+  Enq E(c, st);
+  cudaMemsetAsync(d.y0, 0, sizeof(double) * L.size, st);
+  cudaMemsetAsync(d.deta, 0, sizeof(double) * E.nN(), st);
+  enqueue_set_scalar(c, SC_TIME, 0.0, st);
+  enqueue_set_scalar(c, SC_ALPHA, 0.0, st);
+  enqueue_set_scalar(c, SC_ALPHAT, 0.0, st);
+  enqueue_set_scalar(c, SC_ALPHATT, 0.0, st);
+  enqueue_set_scalar(c, SC_POSTOP, 0.0, st);
+  if (!has_wavemaker(P)) return;
+  const RampP rp = ramp_params(P);
+  const long long nA = E.nA();
+  k_eiwt<<<nblk(c.nf > 0 ? c.nf : 1), kEW, 0, st>>>(d.freq_w, d.sc, d.eiwt, c.nf, rp);
+  k_pos_bc<<<P.n2, 128, 0, st>>>(d.pos_re, d.pos_im, d.freq_w, d.eiwt, d.gzed, d.sc, c.nf,
+                                 P.n2, P.n3, P.n3a, d.bc1, d.bcr, 1);
+  {
+    const int tot = (P.n3a - P.n3) * P.n2;
+    k_extend<<<nblk(tot), kEW, 0, st>>>(d.bc1, nullptr, d.ext, P.n2, P.n3, P.n3a);
+  }
+  double* a1 = d.y0 + L.off[S_AADD1];
+  E.xf({E.R(GRID_ADD, 1, 0, 0, d.bc1, P.n3a, P.n3a, P.n2, a1, P.n3a, P.n3a, P.n2)});
+  E.ew(k_div, nA, a1, (double*)nullptr, (const double*)d.k_add_thk, nA);
+  cudaMemcpyAsync(d.y0 + L.off[S_AADDR], a1, sizeof(double) * nA, cudaMemcpyDeviceToDevice, st);
+}
+
+void enqueue_probes(Ctx& c, cudaStream_t st) {
+  if (c.nprobes <= 0) return;
+  Enq E(c, st);
+  E.xf({E.S2F_N(c.d.eta, c.d.NL2)});
+  k_probe_dot<<<c.nprobes, 256, 0, st>>>(c.d.NL2, c.d.mat_coscos, E.nN(), c.d.probe_out);
+}
+
+}  // namespace hos

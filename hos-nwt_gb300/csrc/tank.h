@@ -1,0 +1,131 @@
+// The tank context: parameters, host tables and device buffers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "hosnwt.h"
+#include "hosnwt_internal.h"
+
+namespace hos {
+
+// Device scalar slots (one double array on the device).
+enum Scalar {
+  SC_T0 = 0,       // t_o of the RK step
+  SC_H = 1,        // h_loc
+  SC_TIME = 2,     // time of the current stage
+  SC_DT = 3,       // h_loc * c_s of the current stage
+  SC_ALPHA = 4,    // ramp alpha, alphat, alphatt of the last wavemaker law
+  SC_ALPHAT = 5,   // evaluation (the reference's globals)
+  SC_ALPHATT = 6,
+  SC_POSTOP = 7,   // pos1st(n3, 1) of the last evaluation
+  SC_ERR = 8,      // embedded error of the last step
+  SC_PHIS0 = 9,    // phisrk0 (mean mode of phis)
+  SC_COUNT = 16
+};
+
+// Offsets of the 10 RK arrays inside one state vector (runge_kutta.f90:81-93).
+struct StateLayout {
+  long long off[10];
+  long long size;
+};
+enum StateIdx { S_G1 = 0, S_G2, S_AADD1, S_AADD2, S_AADDR, S_AADD3, S_A1ST, S_ETA1ST, S_A2ND, S_ETA2ND };
+
+struct Params {
+  // numerics
+  int n1, n2, n3, n3a, nd1, nd2, M, p1, p2, l_add;
+  // case
+  int icase, igeom, iramp, iabsnb, i_wmk, ibat;
+  // nondimensional
+  double h, Tscale, xlen, ylen, xlen_add, d_hinge, Tramp, T_stop, f_out;
+  double nu_mono, w_mono, T_mono, amp_mono, theta_mono, ph_mono, aslosh;
+  int islosh;
+  double toler, dt_stab, delt, delt_out;
+  double delx, dely, delz;
+};
+
+struct Dev {
+  // tables
+  double *omega = nullptr, *kx = nullptr, *ky = nullptr, *kth_ext = nullptr, *kth1 = nullptr;
+  double *nu = nullptr, *k_add_thk = nullptr, *kx_add = nullptr, *cosk = nullptr, *sink = nullptr;
+  double *csh = nullptr, *ksh = nullptr, *kycsh = nullptr, *kxcsh = nullptr;  // [i1 + n1*i3 + n1*n3a*j2]
+  double *ext = nullptr;        // (n3a - n3) x 4 extension weights
+  double *pos_re = nullptr, *pos_im = nullptr;  // pos_ini (n2 x nf)
+  double *freq_w = nullptr, *gzed = nullptr;
+  double *eiwt = nullptr;       // 2*nf scratch: cos/sin(w t)
+  double *mat_coscos = nullptr;
+  double *q_n1 = nullptr, *q_n2 = nullptr, *q_nd1 = nullptr, *q_nd2 = nullptr, *q_add = nullptr;
+  // RK state
+  double *y0 = nullptr, *ys = nullptr, *k[5] = {}, *ynew = nullptr;
+  double *eta = nullptr, *phis = nullptr, *deta = nullptr;
+  double *eta_c = nullptr, *phis_c = nullptr, *deta_c = nullptr;
+  // RHS workspace, free-surface grid
+  double *etam = nullptr, *phim = nullptr, *eta_sp = nullptr;
+  double *w_eta_x = nullptr, *w_eta_y = nullptr, *w_phi_x = nullptr, *w_phi_y = nullptr;
+  double *phix_add = nullptr, *phiy_add = nullptr, *phiz_add = nullptr, *phit_add = nullptr;
+  double *phit_add1 = nullptr, *phiz_add1 = nullptr, *a1k = nullptr, *phiz1st = nullptr, *rhs1 = nullptr;
+  double *pmode[3] = {};        // S2F of phix/phiy/phiz_add
+  double *X1 = nullptr, *X2 = nullptr, *X3 = nullptr, *det = nullptr, *dph = nullptr;
+  double *NL1 = nullptr, *NL2 = nullptr;
+  // big grid
+  std::vector<double*> etapm, phizm, aHOS, prod;
+  std::vector<double*> phizi;   // (m, j) packed
+  double *etax = nullptr, *etay = nullptr, *phisx = nullptr, *phisy = nullptr, *gradeta2 = nullptr;
+  double *phimext = nullptr, *phizMm1 = nullptr, *tbig = nullptr, *tbig2 = nullptr, *tbig3 = nullptr;
+  double *pxe = nullptr, *pye = nullptr, *pze = nullptr, *A1 = nullptr, *A3 = nullptr;
+  double *t1 = nullptr, *geta2phiz = nullptr, *geta2phiz2 = nullptr;
+  // wavemaker grid
+  double *bc1 = nullptr, *bcr = nullptr;
+  // 3-D phiadd_SL workspace (n1 * n3a * n2 each)
+  double *Q[5] = {}, *B[5] = {};
+  // transform temporaries
+  double *xtmp[kMaxJobs] = {};
+  // scalars and reductions
+  double *sc = nullptr;
+  double *part = nullptr;       // partial sums / maxima
+  unsigned int *counter = nullptr;
+  double *probe_out = nullptr;
+  double *host_sc = nullptr;    // pinned mirror of the scalar slots
+};
+
+struct Ctx {
+  hosnwt_input in{};
+  hosnwt_numerics num{};
+  Params P{};
+  std::string err;
+  // host tables kept for the oracle-free host logic
+  std::vector<double> kx, ky, cx, cy, cz, omega;
+  std::vector<std::complex<double>> pos_ini;  // n2 x nf, i2 fastest
+  std::vector<double> freq_w, gzed;
+  std::vector<double> probes;  // nondimensional (x, y)
+  int nprobes = 0;
+  int nf = 0;
+  StateLayout L{};
+  Dev d{};
+  Tables tb{};
+  cudaStream_t st = nullptr;
+  cudaGraphExec_t step_graph = nullptr;
+  double time_cur = 0.0;
+  int endramp = 0;
+  long long n_rhs = 0;
+  int nparts = 0;
+  std::vector<void*> allocs;
+};
+
+// host setup (host.cpp)
+int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes);
+
+// device pipeline (rhs.cu)
+int alloc_device(Ctx& c);
+void free_device(Ctx& c);
+void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t st);
+void enqueue_step(Ctx& c, cudaStream_t st);
+void enqueue_initialize(Ctx& c, cudaStream_t st);
+void enqueue_probes(Ctx& c, cudaStream_t st);
+void enqueue_accept(Ctx& c, bool end_ramp, cudaStream_t st);
+void enqueue_set_scalar(Ctx& c, int slot, double v, cudaStream_t st);
+
+}  // namespace hos

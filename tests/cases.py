@@ -1,0 +1,23 @@
+"""Small tank configurations shared by the parity tests (sizes the CPU
+oracle finishes in seconds)."""
+from oracle.hos_oracle import default_input
+
+# 2-D tank (n2 = 1), regular wave with a flap wavemaker
+REG_1D = dict(inp=default_input(T_stop=30.0, amp_mono=0.025, nu_mono=1.0, toler=1e-7, f_out=10.0),
+              n1=65, n2=1, n3=17, mHOS=3, p1=3, p2=1)
+# higher order, p < M (partial dealiasing active at several orders)
+REG_1D_M5 = dict(inp=default_input(T_stop=30.0, amp_mono=0.04, nu_mono=0.8, toler=1e-7, f_out=10.0),
+                 n1=65, n2=1, n3=17, mHOS=5, p1=3, p2=1)
+# 3-D tank, oblique regular wave (snake wavemaker)
+REG_3D = dict(inp=default_input(T_stop=20.0, amp_mono=0.02, nu_mono=0.7, theta_mono=20.0, toler=1e-7,
+                                f_out=4.0, ylen=20.0),
+              n1=33, n2=17, n3=9, mHOS=3, p1=3, p2=3)
+# sloshing (no wavemaker)
+SLOSH = dict(inp=default_input(icase=1, islosh=3, aslosh=0.05, iabsnb=0, T_stop=5.0, toler=1e-8, f_out=2.0),
+             n1=33, n2=1, n3=9, mHOS=4, p1=4, p2=1)
+# JONSWAP with libgfortran random phases (icase 4), piston wavemaker
+JONSWAP_1D = dict(inp=default_input(icase=4, Hs=0.05, Tp=1.2, gamma=3.3, iseed=513, igeom=1, T_stop=8.0,
+                                    toler=1e-7, f_out=10.0),
+                  n1=65, n2=1, n3=17, mHOS=3, p1=3, p2=1)
+
+ALL = {"reg1d": REG_1D, "reg1d_m5": REG_1D_M5, "reg3d": REG_3D, "slosh": SLOSH, "jonswap1d": JONSWAP_1D}
