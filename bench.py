@@ -1,0 +1,323 @@
+"""Benchmark of the HOS-NWT hot path: RK4(5) steps per second of the 2-D
+irregular tank (n1 = 1025, n3 = 65, M = 5, p1 = 5; 512-component JONSWAP,
+Hs = 0.10 m, Tp = 1.4 s; synthetic seeded phases).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cuda|reference]
+
+One step = one adaptive RK4(5) step of runge4_adapt2 (five nonlinear
+right-hand sides, error estimate) at the CFL-limited step size, followed by
+the accept of HOS-NWT.f90's step control.  `value` is measured with CUDA
+events on the library's stream with the state resident on the device, the L2
+cache flushed between steps (a 256 MiB write outside the timed events);
+`e2e` is the same step through hosnwt_runge4_adapt2 on pinned host arrays
+(host-to-device copy of the 10 state arrays and device-to-host copy of the
+results inside each timed call).  Under torchrun every rank runs its own
+replica tank (the path does not shard); value = total steps/s.
+
+--impl reference times the CPU restatement of the reference (the oracle:
+numpy/scipy FP64, single thread like the Fortran reference) on the same tank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "hos-nwt_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+import workloads  # noqa: E402
+
+METRIC = "RK4(5) steps/s (sim-s/wall-s reported alongside)"
+UNIT = "steps/s"
+
+
+def _workload_config(w, info=None):
+    cfg = {"workload": "irregular_2d: 2-D JONSWAP tank 50 m x 5 m, flap, 512 components, "
+                       "n1=1025 n3=65 M=5 p1=5, RK4(5) tol 1e-7",
+           "n1": w["n1"], "n3": w["n3"], "mHOS": w["mHOS"], "p1": w["p1"],
+           "wave_components": 512, "seed": 513,
+           "l2": "flushed between steps (256 MiB write outside the timed events)",
+           "parallelism": "replicas"}
+    if info is not None:
+        cfg["nd1"] = info["nd1"]
+        cfg["dt_nondim"] = info["delt"]
+        cfg["dt_s"] = info["delt"] * info["Tscale"]
+    return cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for i, n in enumerate(names):
+                    if r[5 + i].lower().startswith("active"):
+                        reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def _measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "of measured"
+    return 6800.0, "of fallback"
+
+
+def _profile_traffic():
+    """Per-launch DRAM traffic of the dominant kernel from the committed ncu
+    summary (profiles/xform_x_pass_irregular_2d.md), if present."""
+    p = os.path.join(ROOT, "profiles", "xform_x_pass_irregular_2d.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(w, budget_s=15.0, max_steps=400):
+    """The oracle (numpy/scipy FP64, one thread) on a bounded sample of the
+    same tank: as many RK4(5) steps as fit in about `budget_s` seconds."""
+    from oracle.hos_oracle import Tank as OTank
+    o = OTank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
+              wave_files_dir=w["wave_dir"])
+    h = o.delt
+    st = o.state_tuple()
+    res, _, _, _ = o.runge4_adapt2(0.0, *st, h)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    t = 0.0
+    while n < max_steps and time.perf_counter() - t0 < budget_s:
+        res, err, deta, _ = o.runge4_adapt2(t, *st, h)
+        t += h
+        n += 1
+    el = time.perf_counter() - t0
+    return {"value": n / el, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} RK4(5) steps of the irregular_2d tank (n1=1025, M=5) with the numpy/scipy "
+                      f"oracle, {el:.1f} s on one host core"}
+
+
+def run_reference(args, w):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle.hos_oracle import Tank as OTank
+    o = OTank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
+              wave_files_dir=w["wave_dir"])
+    h = o.delt
+    st = list(o.state_tuple())
+    t = 0.0
+    for _ in range(args.warmup):
+        res, err, deta, _ = o.runge4_adapt2(t, *st, h)
+        st = [res[k] for k in ("eta", "phis", "a_add_1", "a_add_2", "a_add_ramp", "a_add_3",
+                               "eta1st", "eta2nd", "a1st", "a2nd")]
+        t += h
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res, err, deta, _ = o.runge4_adapt2(t, *st, h)
+        st = [res[k] for k in ("eta", "phis", "a_add_1", "a_add_2", "a_add_ramp", "a_add_3",
+                               "eta1st", "eta2nd", "a1st", "a2nd")]
+        t += h
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": _workload_config(w),
+            "sim_s_per_wall_s": v * h * o.Tscale,
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"{args.steps} RK4(5) steps of the same tank on one host core "
+                                       "(CPU restatement of the Fortran reference; it is not buildable "
+                                       "here: no gfortran/FFTW)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_cuda(args, w):
+    import torch
+    import hosnwt
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device (the product has no CPU path)")
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    tank = hosnwt.Tank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
+                       probes=w["probes"], wave_dir=w["wave_dir"])
+    info = tank.info()
+    h = info["delt"]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def l2_flush():
+        flush.zero_()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        tank.step(h)
+        tank.accept(h)
+    l2_flush()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms0 = tank.info()["device_ms"]
+        wall0 = time.perf_counter()
+        for _ in range(args.steps):
+            l2_flush()
+            tank.step(h)
+            tank.accept(h)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+        dev_ms = tank.info()["device_ms"] - ms0
+    if dist is not None:
+        t = torch.tensor([dev_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+        dist.barrier()
+    value = world * args.steps / (dev_ms * 1e-3)
+    info = tank.info()
+
+    # e2e: the drop-in call with pinned host arrays, copies inside the timed call
+    n1, n2, na = info["n1"], info["n2"], info["n3_add"]
+    shapes = [(n1, n2)] * 2 + [(na, n2)] * 4 + [(n1, n2)] * 4
+    pinned = []
+    for s in shapes:
+        buf = torch.empty(s[0] * s[1], dtype=torch.float64, pin_memory=True)
+        pinned.append(buf.numpy().reshape(s, order="F"))
+    tank.get_rk_state(pinned)
+    t_o = info["time_cur"]
+    for _ in range(max(1, args.warmup)):
+        tank.runge4_adapt2_inplace(t_o, pinned, h)
+        t_o += h
+    e2e_s = 0.0
+    for _ in range(args.steps):
+        l2_flush()
+        t0 = time.perf_counter()
+        tank.runge4_adapt2_inplace(t_o, pinned, h)
+        e2e_s += time.perf_counter() - t0
+        t_o += h
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * args.steps / e2e_s
+    io_bytes = 8 * sum(s[0] * s[1] for s in shapes)
+
+    # roofline of the dominant kernel: the x pass of the big-grid transforms
+    # (a batch of four FOURIER_2_SPACE_BIG of extended n1 modes), timed alone
+    nd1 = info["nd1"]
+    ms = tank.time_transform("big", -1, "cos", "cos", (n1, 1), (nd1, 1), batch=4, nrep=50)
+    alg_bytes = 16.0 * nd1 * 4          # 8-byte read + 8-byte write per output element
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    peak, peak_src = _measured_peaks()
+    fp64_peak = hosnwt.fp64_peak_gflops()
+    fp64_flops = 2.0 * n1 * nd1 * 4     # one FMA per (input, output) pair of the direct sum
+    fp64_achieved = fp64_flops / (ms * 1e-3) / 1e9
+    traffic = _profile_traffic()
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": _workload_config(w, info),
+                "sim_s_per_wall_s": value / world * h * info["Tscale"],
+                "wall_ms_per_step": 1e3 * wall / args.steps,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes,
+                        "d2h_bytes_per_step": io_bytes},
+                "gpu_launches": info["kernels_per_step"] * args.steps + 4 * args.steps,
+                "clocks": clk.summary(),
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic,
+                             "peak_source": peak_src,
+                             "kernel": "axis_pass_lanes_k (x pass, 4 x F2S_big of n1 modes)",
+                             "ms_per_launch": ms,
+                             "fp64": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64_peak,
+                                      "frac": fp64_achieved / fp64_peak,
+                                      "note": "the pass is FP64-pipe bound on GB300; peak measured "
+                                              "live with a DFMA loop"}},
+                }
+        if world == 1:
+            line["cpu_baseline"] = cpu_baseline(w)
+        print(json.dumps(line), flush=True)
+    tank.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="cuda", choices=("cuda", "reference"))
+    args = ap.parse_args()
+    with tempfile.TemporaryDirectory() as tmp:
+        w = workloads.irregular_2d(tmp)
+        if args.impl == "reference":
+            run_reference(args, w)
+        else:
+            run_cuda(args, w)
+
+
+if __name__ == "__main__":
+    main()

@@ -52,6 +52,14 @@ struct AxisJob {
   double s0, sm, sl;         // scales for k == 0, interior k, k == N-1
   double gscale;
   const double* q;           // quarter-wave table cos(pi*m/(2D)), m = 0..D
+  // work decomposition of the x pass (set by the launcher)
+  int mode;                  // 0 direct, 1 output symmetry k <-> D-k, 2 input symmetry j <-> D-j
+  int nlane;                 // lane outputs: tiles of 32 cover [0, nlane)
+  int ntile;
+  int nchunk, chunk;         // the sum is split over nchunk CTAs of `chunk` terms
+  int ta, tb;                // term range [ta, tb) (interior terms or symmetric pairs)
+  double* part;              // nlines * ntile * nchunk * 64 partial sums (nchunk > 1)
+  unsigned int* cnt;         // nlines * ntile arrival counters (nchunk > 1)
 };
 
 constexpr int kMaxJobs = 8;
@@ -92,6 +100,11 @@ void launch_y_f2s(const Tables& tb, const double* in, int nlines, long long y_st
 
 struct Tables {
   int n1, n2, nd1, nd2, n3_add;
+  int nsm;                   // SMs of the device (sizes the split of the sums)
+  double* part;              // scratch for partial sums of split transforms
+  long long part_cap;        // capacity (doubles)
+  unsigned int* cnt;         // arrival counters (zero between launches)
+  int cnt_cap;
   // quarter-wave tables for D = n1-1, n2-1, nd1-1, nd2-1, n3_add
   const double* q_n1;
   const double* q_n2;
@@ -99,6 +112,9 @@ struct Tables {
   const double* q_nd2;
   const double* q_add;
 };
+
+// FP64 FMA throughput of the current device in GFLOP/s.
+double measure_fp64_peak_gflops();
 
 // Build the quarter-wave table cos(pi*m/(2D)), m = 0..D, on the host.
 std::vector<double> quarter_table(int D);

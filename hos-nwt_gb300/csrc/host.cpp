@@ -444,6 +444,7 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
   if (nm.n1 < 5 || nm.n2 < 1 || (nm.n2 > 1 && nm.n2 < 5) || nm.n3 < 5)
     return fail(c, HOSNWT_ERR_ARG, "grid too small (n1, n3 >= 5; n2 = 1 or >= 5)");
   if (nm.mHOS > 15) return fail(c, HOSNWT_ERR_ARG, "mHOS > 15");
+  if (nm.n3 > 257) return fail(c, HOSNWT_ERR_ARG, "n3 > 257 (n3_add is limited to 512)");
   P.n1 = nm.n1; P.n2 = nm.n2; P.n3 = nm.n3; P.M = nm.mHOS; P.p1 = nm.p1; P.p2 = nm.p2;
   P.l_add = 2;
   P.n3a = P.l_add * (P.n3 - 1);
@@ -627,6 +628,16 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
   d.q_nd2 = upload(c, quarter_table(std::max(nd2 - 1, 1)));
   d.q_add = upload(c, quarter_table(n3a));
   c.tb.n1 = n1; c.tb.n2 = n2; c.tb.nd1 = nd1; c.tb.nd2 = nd2; c.tb.n3_add = n3a;
+  {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    c.tb.nsm = sms > 0 ? sms : 1;
+    c.tb.part_cap = 64LL * 4 * c.tb.nsm * 16;   // partials of the split sums
+    c.tb.cnt_cap = 4 * c.tb.nsm * 16;
+    c.tb.part = dalloc<double>(c, (size_t)c.tb.part_cap);
+    c.tb.cnt = dalloc<unsigned int>(c, (size_t)c.tb.cnt_cap);
+  }
   c.tb.q_n1 = d.q_n1; c.tb.q_n2 = d.q_n2; c.tb.q_nd1 = d.q_nd1; c.tb.q_nd2 = d.q_nd2; c.tb.q_add = d.q_add;
   for (void* p : c.allocs)
     if (!p) return fail(c, HOSNWT_ERR_CUDA, "device allocation failed");
@@ -684,6 +695,9 @@ int alloc_device(Ctx& c) {
 }
 
 void free_device(Ctx& c) {
+  if (c.ev0) cudaEventDestroy(c.ev0);
+  if (c.ev1) cudaEventDestroy(c.ev1);
+  c.ev0 = c.ev1 = nullptr;
   if (c.step_graph) cudaGraphExecDestroy(c.step_graph);
   c.step_graph = nullptr;
   for (void* p : c.allocs)
@@ -720,6 +734,16 @@ static int build_step_graph(Ctx& c) {
   cudaMemcpyAsync(c.d.sc + SC_T0, c.d.host_sc + SC_T0, 2 * sizeof(double), cudaMemcpyHostToDevice, c.st);
   enqueue_step(c, c.st);
   if (cudaStreamEndCapture(c.st, &g) != cudaSuccess) return cuda_check(c, "end capture");
+  size_t nn = 0;
+  cudaGraphGetNodes(g, nullptr, &nn);
+  std::vector<cudaGraphNode_t> nodes(nn);
+  cudaGraphGetNodes(g, nodes.data(), &nn);
+  c.kernels_per_step = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    cudaGraphNodeGetType(nd, &t);
+    if (t == cudaGraphNodeTypeKernel) c.kernels_per_step++;
+  }
   if (cudaGraphInstantiate(&c.step_graph, g, 0) != cudaSuccess) {
     cudaGraphDestroy(g);
     return cuda_check(c, "graph instantiate");
@@ -783,17 +807,32 @@ extern "C" int hosnwt_get_info(const hosnwt_ctx* h, hosnwt_info* info) {
   info->T_stop = P.T_stop; info->toler = P.toler; info->time_cur = c.time_cur;
   info->nprobes = c.nprobes;
   info->n_rhs = c.n_rhs;
+  info->kernels_per_step = c.kernels_per_step;
+  info->device_ms = c.dev_ms;
   return HOSNWT_OK;
+}
+
+static void timed_begin(Ctx& c) {
+  if (!c.ev0) { cudaEventCreate(&c.ev0); cudaEventCreate(&c.ev1); }
+  cudaEventRecord(c.ev0, c.st);
+}
+static void timed_end(Ctx& c) { cudaEventRecord(c.ev1, c.st); }
+static void timed_collect(Ctx& c) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, c.ev0, c.ev1) == cudaSuccess) c.dev_ms += ms;
 }
 
 static int run_step(Ctx& c, double t_o, double h_loc, double* err) {
   if (!c.step_graph) return HOSNWT_ERR_ARG;
   c.d.host_sc[SC_T0] = t_o;
   c.d.host_sc[SC_H] = h_loc;
+  timed_begin(c);
   if (cudaGraphLaunch(c.step_graph, c.st) != cudaSuccess) return cuda_check(c, "graph launch");
+  timed_end(c);
   double e = 0.0;
   cudaMemcpyAsync(&e, c.d.sc + SC_ERR, sizeof(double), cudaMemcpyDeviceToHost, c.st);
   if (cudaStreamSynchronize(c.st) != cudaSuccess) return cuda_check(c, "step");
+  timed_collect(c);
   c.n_rhs += 5;
   if (err) *err = e;
   if (!std::isfinite(e)) {
@@ -817,9 +856,12 @@ extern "C" int hosnwt_accept(hosnwt_ctx* h, double h_loc) {
     end_ramp = true;
     c.endramp = 1;
   }
+  timed_begin(c);
   enqueue_accept(c, end_ramp, c.st);
+  timed_end(c);
   c.time_cur += h_loc;
   cudaStreamSynchronize(c.st);
+  timed_collect(c);
   return cuda_check(c, "accept");
 }
 
@@ -961,6 +1003,25 @@ extern "C" int hosnwt_get_state(hosnwt_ctx* h, double* eta, double* phis, double
   return cuda_check(c, "get_state");
 }
 
+extern "C" int hosnwt_get_rk_state(hosnwt_ctx* h, double* eta, double* phis, double* a_add_1,
+                                   double* a_add_2, double* a_add_ramp, double* a_add_3,
+                                   double* eta1st, double* eta2nd, double* a1st, double* a2nd) {
+  if (!h || !eta || !phis || !a_add_1 || !a_add_2 || !a_add_ramp || !a_add_3 || !eta1st || !eta2nd ||
+      !a1st || !a2nd)
+    return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  const StateLayout& L = c.L;
+  const size_t nN = (size_t)c.P.n1 * c.P.n2, nA = (size_t)c.P.n3a * c.P.n2;
+  double* const arr[10] = {nullptr, nullptr, a_add_1, a_add_2, a_add_ramp, a_add_3, a1st, eta1st, a2nd, eta2nd};
+  const size_t sz[10] = {nN, nN, nA, nA, nA, nA, nN, nN, nN, nN};
+  cudaMemcpyAsync(eta, c.d.eta, nN * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaMemcpyAsync(phis, c.d.phis, nN * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  for (int a = 2; a < 10; ++a)
+    cudaMemcpyAsync(arr[a], c.d.y0 + L.off[a], sz[a] * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaStreamSynchronize(c.st);
+  return cuda_check(c, "get_rk_state");
+}
+
 extern "C" int hosnwt_set_state(hosnwt_ctx* h, const double* eta, const double* phis) {
   if (!h) return HOSNWT_ERR_ARG;
   Ctx& c = h->c;
@@ -1022,4 +1083,58 @@ extern "C" int hosnwt_advance_many(hosnwt_ctx* const* ctxs, int n, const double*
     if (rc) return rc;
   }
   return HOSNWT_OK;
+}
+
+extern "C" int hosnwt_time_transform(hosnwt_ctx* h, int grid, int dir, int csx, int csy, int nin1,
+                                     int nin2, int nout1, int nout2, int batch, int nrep,
+                                     double* ms_per_launch) {
+  if (!h || !ms_per_launch || batch < 1 || batch > kMaxJobs || nrep < 1) return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  const Params& P = c.P;
+  int a = P.n1, b = P.n2;
+  if (grid == GRID_BIG) { a = P.nd1; b = P.nd2; }
+  else if (grid == GRID_ADD) { a = P.n3a; b = P.n2; }
+  if (nin1 < 1 || nin1 > a || nout1 < 1 || nout1 > a || nin2 < 1 || nin2 > b || nout2 < 1 || nout2 > b)
+    return HOSNWT_ERR_ARG;
+  const size_t n = (size_t)a * b;
+  std::vector<double*> bufs;
+  for (int i = 0; i < 2 * batch; ++i) {
+    double* p = nullptr;
+    if (cudaMalloc(&p, n * sizeof(double)) != cudaSuccess) {
+      for (double* q : bufs) cudaFree(q);
+      return fail(c, HOSNWT_ERR_CUDA, "time_transform: allocation failed");
+    }
+    std::vector<double> ones(n, 1.0);
+    cudaMemcpy(p, ones.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    bufs.push_back(p);
+  }
+  std::vector<XfReq> rq(batch);
+  for (int i = 0; i < batch; ++i) {
+    XfReq& r = rq[i];
+    r.grid = grid; r.dir = dir; r.csx = csx; r.csy = csy;
+    r.in = bufs[2 * i]; r.in_ld = a; r.nin1 = nin1; r.nin2 = nin2;
+    r.out = bufs[2 * i + 1]; r.out_ld = a; r.nout1 = nout1; r.nout2 = nout2;
+    r.scale = 1.0;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int w = 0; w < 3; ++w) launch_transforms(rq.data(), batch, c.tb, c.d.xtmp, c.st);
+  cudaEventRecord(e0, c.st);
+  for (int r = 0; r < nrep; ++r) launch_transforms(rq.data(), batch, c.tb, c.d.xtmp, c.st);
+  cudaEventRecord(e1, c.st);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (double* q : bufs) cudaFree(q);
+  *ms_per_launch = ms / nrep;
+  return cuda_check(c, "time_transform");
+}
+
+extern "C" int hosnwt_fp64_peak(double* gflops) {
+  if (!gflops) return HOSNWT_ERR_ARG;
+  *gflops = measure_fp64_peak_gflops();
+  return *gflops > 0 ? HOSNWT_OK : HOSNWT_ERR_CUDA;
 }

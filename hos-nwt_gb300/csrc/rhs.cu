@@ -404,22 +404,42 @@ __global__ void k_div(double* a, double* b, const double* __restrict__ d, long l
 }
 
 // phiadd_1st_SWEET at z = 0 (resol_wmkr.f90:490-534), the i3 contraction:
-// At(i1, j2) = sum_i3 da(i3,j2) cos(kx_add) csh;  Az(i1, j2) = sum_i3 a(i3,j2) sin(kx_add) kx_add csh
-__global__ void k_sweet_contract(const double* __restrict__ a, const double* __restrict__ da,
-                                 const double* __restrict__ cosk, const double* __restrict__ sink,
-                                 const double* __restrict__ csh, const double* __restrict__ kxcsh,
-                                 int n1, int n2, int n3a, double* At, double* Az) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= (long long)n1 * n2) return;
-  const int i1 = (int)(i % n1), j2 = (int)(i / n1);
-  double st = 0.0, sz = 0.0;
-  for (int i3 = 0; i3 < n3a; ++i3) {
-    const long long o = i1 + (long long)n1 * i3 + (long long)n1 * n3a * j2;
-    st += da[i3 + (long long)n3a * j2] * cosk[i3] * csh[o];
-    sz += a[i3 + (long long)n3a * j2] * sink[i3] * kxcsh[o];
+// At(i1, j2) = sum_i3 da(i3,j2) cos(kx_add) csh;  Az(i1, j2) = -sum_i3 a(i3,j2) sin(kx_add) kx_add csh
+// Block (16 x 8): 16 outputs i1, the i3 range split in 8 chunks, combined in
+// shared memory in a fixed order.
+constexpr int kCx = 16, kCy = 8;
+__global__ void __launch_bounds__(kCx * kCy) k_sweet_contract(
+    const double* __restrict__ a, const double* __restrict__ da, const double* __restrict__ cosk,
+    const double* __restrict__ sink, const double* __restrict__ csh, const double* __restrict__ kxcsh,
+    int n1, int n2, int n3a, double* At, double* Az) {
+  __shared__ double sa[512], sd[512];
+  __shared__ double rt[kCy][kCx], rz[kCy][kCx];
+  const int j2 = blockIdx.y;
+  const int tx = threadIdx.x % kCx, ty = threadIdx.x / kCx;
+  const int i1 = blockIdx.x * kCx + tx;
+  for (int t = threadIdx.x; t < n3a; t += blockDim.x) {
+    sa[t] = a[t + (long long)n3a * j2] * sink[t];
+    sd[t] = da[t + (long long)n3a * j2] * cosk[t];
   }
-  At[i] = st;
-  Az[i] = -sz;
+  __syncthreads();
+  const int ch = (n3a + kCy - 1) / kCy;
+  double st = 0.0, sz = 0.0;
+  if (i1 < n1) {
+    for (int i3 = ty * ch; i3 < min(n3a, (ty + 1) * ch); ++i3) {
+      const long long o = i1 + (long long)n1 * i3 + (long long)n1 * n3a * j2;
+      st = fma(sd[i3], csh[o], st);
+      sz = fma(sa[i3], kxcsh[o], sz);
+    }
+  }
+  rt[ty][tx] = st;
+  rz[ty][tx] = sz;
+  __syncthreads();
+  if (ty == 0 && i1 < n1) {
+    double t = 0.0, z = 0.0;
+    for (int c = 0; c < kCy; ++c) { t += rt[c][tx]; z += rz[c][tx]; }
+    At[i1 + (long long)n1 * j2] = t;
+    Az[i1 + (long long)n1 * j2] = -z;
+  }
 }
 
 // SWEET_1 free-surface RHS (resol_wmkr.f90:177-185)
@@ -439,30 +459,55 @@ __global__ void k_sum3(const double* a, const double* b, const double* c, double
   if (i < n) out[i] = a[i] + b[i] + c[i];
 }
 
-// phiadd_SL on a 1-D tank (n2 = 1): direct i3 contraction at z = eta
-__global__ void k_phiadd_sl_1d(const double* __restrict__ eta, const double* __restrict__ a1,
-                               const double* __restrict__ a2, const double* __restrict__ a3,
-                               const double* __restrict__ da, const double* __restrict__ kx_add,
-                               const double* __restrict__ csh, const double* __restrict__ ksh,
-                               const double* __restrict__ kxcsh, int n1, int n3a, double* phix,
-                               double* phiy, double* phiz, double* phit) {
-  const int i1 = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i1 >= n1) return;
-  const double e1 = eta[i1] + 1.0;
-  double st = 0.0, sx = 0.0, sz = 0.0;
-  for (int i3 = 0; i3 < n3a; ++i3) {
-    double s, c;
-    sincos(kx_add[i3] * e1, &s, &c);
-    const double a = a1[i3] + a2[i3] + a3[i3];
-    const long long o = i1 + (long long)n1 * i3;
-    st = st + da[i3] * c * csh[o];
-    sx = sx - a * c * ksh[o];
-    sz = sz - a * s * kxcsh[o];
+// phiadd_SL on a 1-D tank (n2 = 1): the i3 contraction at z = eta.
+// kx_add(i3) = (2 i3 + 1) pi / 4, so cos/sin(kx_add(i3) (eta + 1)) follow
+// from one sincos per chunk start and rotations by 2 phi, phi = pi (eta+1)/4.
+__global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
+    const double* __restrict__ eta, const double* __restrict__ a1, const double* __restrict__ a2,
+    const double* __restrict__ a3, const double* __restrict__ da, const double* __restrict__ kx_add,
+    const double* __restrict__ csh, const double* __restrict__ ksh, const double* __restrict__ kxcsh,
+    int n1, int n3a, double* phix, double* phiy, double* phiz, double* phit) {
+  __shared__ double sa[512], sd[512];
+  __shared__ double r[3][kCy][kCx];
+  const int tx = threadIdx.x % kCx, ty = threadIdx.x / kCx;
+  const int i1 = blockIdx.x * kCx + tx;
+  for (int t = threadIdx.x; t < n3a; t += blockDim.x) {
+    sa[t] = a1[t] + a2[t] + a3[t];
+    sd[t] = da[t];
   }
-  phix[i1] = sx;
-  phiy[i1] = 0.0;
-  phiz[i1] = sz;
-  phit[i1] = st;
+  __syncthreads();
+  const int ch = (n3a + kCy - 1) / kCy;
+  double st = 0.0, sx = 0.0, sz = 0.0;
+  if (i1 < n1) {
+    const double e1 = eta[i1] + 1.0;
+    const int i3a = ty * ch, i3b = min(n3a, (ty + 1) * ch);
+    if (i3a < i3b) {
+      double s, c, s2, c2;
+      sincos(kx_add[i3a] * e1, &s, &c);
+      sincos(2.0 * kx_add[0] * e1, &s2, &c2);  // rotation by 2 phi
+      for (int i3 = i3a; i3 < i3b; ++i3) {
+        const long long o = i1 + (long long)n1 * i3;
+        st = fma(sd[i3] * c, csh[o], st);
+        sx = fma(-sa[i3] * c, ksh[o], sx);
+        sz = fma(-sa[i3] * s, kxcsh[o], sz);
+        const double cn = c * c2 - s * s2;
+        s = s * c2 + c * s2;
+        c = cn;
+      }
+    }
+  }
+  r[0][ty][tx] = st;
+  r[1][ty][tx] = sx;
+  r[2][ty][tx] = sz;
+  __syncthreads();
+  if (ty == 0 && i1 < n1) {
+    double t = 0.0, x = 0.0, z = 0.0;
+    for (int q = 0; q < kCy; ++q) { t += r[0][q][tx]; x += r[1][q][tx]; z += r[2][q][tx]; }
+    phix[i1] = x;
+    phiy[i1] = 0.0;
+    phiz[i1] = z;
+    phit[i1] = t;
+  }
 }
 
 // phiadd_SL (3-D): products Q_q(i1, i3, j2) = a(i3, j2) * T_q(i1, i3, j2)
@@ -880,9 +925,9 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     E.ew(k_div, nA, kA1, kAR, (const double*)d.k_add_thk, nA);
     // reconstruction at z = 0 (phiadd_1st_SWEET) for phit_add_1, phiz_add_1
     const double* aA1 = y + L.off[S_AADD1];
-    E.ew(k_sweet_contract, nN, aA1, (const double*)kA1, (const double*)d.cosk,
-         (const double*)d.sink, (const double*)d.csh, (const double*)d.kxcsh, n1, n2, P.n3a,
-         n2 == 1 ? d.phit_add1 : d.tbig, n2 == 1 ? d.phiz_add1 : d.tbig2);
+    k_sweet_contract<<<dim3((n1 + kCx - 1) / kCx, n2), kCx * kCy, 0, st>>>(
+        aA1, kA1, d.cosk, d.sink, d.csh, d.kxcsh, n1, n2, P.n3a, n2 == 1 ? d.phit_add1 : d.tbig,
+        n2 == 1 ? d.phiz_add1 : d.tbig2);
     if (n2 != 1) {
       // y sums: sum_j2 A(i1, j2) cos(ky(j2) y(i2)) = FOURIER_2_SPACE_y
       launch_y_f2s(c.tb, d.tbig, n1, n1, d.phit_add1, n1, 0, st);
@@ -899,7 +944,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     const double* aA2 = y + L.off[S_AADD2];
     const double* aA3 = y + L.off[S_AADD3];
     if (n2 == 1) {
-      k_phiadd_sl_1d<<<nblk(n1, 128), 128, 0, st>>>(d.eta_sp, aA1, aA2, aA3, kA1, d.kx_add, d.csh,
+      k_phiadd_sl_1d<<<(n1 + kCx - 1) / kCx, kCx * kCy, 0, st>>>(d.eta_sp, aA1, aA2, aA3, kA1, d.kx_add, d.csh,
                                                      d.ksh, d.kxcsh, n1, P.n3a, d.phix_add,
                                                      d.phiy_add, d.phiz_add, d.phit_add);
     } else {

@@ -111,6 +111,9 @@ struct Ctx {
   double time_cur = 0.0;
   int endramp = 0;
   long long n_rhs = 0;
+  int kernels_per_step = 0;
+  double dev_ms = 0.0;            // device time of steps and accepts (CUDA events)
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int nparts = 0;
   std::vector<void*> allocs;
 };

@@ -11,6 +11,7 @@
 // not HBM: an x pass spreads one line over many CTAs (8 warps split the sum,
 // lanes own outputs), a y pass gives one row per lane (coalesced loads,
 // warp-uniform twiddles) and several outputs per thread.
+#include <algorithm>
 #include <cmath>
 
 #include "hosnwt_internal.h"
@@ -32,70 +33,169 @@ __device__ __forceinline__ int mod4d(long long v, int D4) {
 
 constexpr int kXThreads = 256;   // 8 warps
 constexpr int kXWarps = kXThreads / 32;
+constexpr int kMaxPairChunk = 1024;  // staged symmetric pairs per CTA (mode 2)
 
-// x pass: one CTA = (job, line, tile of 32 outputs); the 8 warps split the
-// summation range, lanes own outputs.
+// x pass: one CTA = (job, line, tile of 32 lane outputs, chunk of the sum).
+// Lanes own outputs, the 8 warps split the CTA's chunk, chunks of one tile
+// are combined in a fixed order by the last CTA to arrive (no spin-waits).
+//   mode 0: direct sum over the interior terms plus the two end terms
+//   mode 1: output symmetry: lane k accumulates even-j and odd-j sums E, O
+//           and writes out[k] and out[D-k] (full outputs, D = N-1)
+//   mode 2: input symmetry: terms are pairs (j, D-j) staged in shared memory
+//           as u = x_j + x_{D-j}, v = x_j - x_{D-j} (outputs k <= D/2)
 __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b) {
-  __shared__ double red[kXWarps][32];
+  __shared__ double red[kXWarps][32][2];
+  __shared__ double su[kMaxPairChunk], sv[kMaxPairChunk];
+  __shared__ bool amlast;
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const AxisJob& J = b.job[jb];
-  const int local = blockIdx.x - b.start[jb];
-  const int ntile = (J.nout + 31) / 32;
-  const int line = local / ntile;
-  const int tile = local - line * ntile;
+  int local = blockIdx.x - b.start[jb];
+  const int chunk_id = local % J.nchunk;
+  local /= J.nchunk;
+  const int tile = local % J.ntile;
+  const int line = local / J.ntile;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int k = tile * 32 + lane;
-  const int D4 = 4 * J.D;
+  const int D = J.D, D4 = 4 * D;
   const double* __restrict__ x = J.in + (long long)line * J.in_sl;
+  const int kk = J.ak * k + J.bk;
+  const int inc = mod4d((long long)J.aj * kk, D4);
+  const bool lane_on = k < J.nlane;
 
-  double acc = 0.0;
-  const bool active = (k < J.nout) && (k >= J.klo) && (k < J.khi);
-  if (active) {
-    const int j_end = min(J.jhi, J.nin);
-    const int kk = J.ak * k + J.bk;
-    // interior range [max(jlo,1), min(j_end, N-1)) split over warps
-    const int a0 = max(J.jlo, 1), a1 = min(j_end, J.N - 1);
-    if (a1 > a0) {
-      const int len = a1 - a0;
-      const int chunk = (len + kXWarps - 1) / kXWarps;
-      const int ja = a0 + warp * chunk;
-      const int jz = min(a1, ja + chunk);
-      if (jz > ja) {
-        int m = mod4d((long long)(J.aj * ja + J.bj) * kk + J.off, D4);
-        const int inc = mod4d((long long)J.aj * kk, D4);
-        double s = 0.0;
+  // this CTA's share [ca, cb) of the term range
+  const int ca = J.ta + chunk_id * J.chunk;
+  const int cb = min(J.tb, ca + J.chunk);
+  double e = 0.0, o = 0.0;  // mode 1: even / odd j sums; else e only
+  if (J.mode == 2) {
+    for (int t = threadIdx.x; t < cb - ca; t += kXThreads) {
+      const int j = ca + t;
+      const double xa = __ldg(x + (long long)j * J.in_sk);
+      const double xb = __ldg(x + (long long)(D - j) * J.in_sk);
+      su[t] = xa + xb;
+      sv[t] = xa - xb;
+    }
+    __syncthreads();
+  }
+  if (cb > ca) {
+    const int len = cb - ca;
+    const int per = (len + kXWarps - 1) / kXWarps;
+    const int ja = ca + warp * per;
+    const int jz = min(cb, ja + per);
+    if (lane_on && jz > ja) {
+      int m = mod4d((long long)(J.aj * ja + J.bj) * kk + J.off, D4);
+      if (J.mode == 1) {
         const double* __restrict__ xp = x + (long long)ja * J.in_sk;
         for (int j = ja; j < jz; ++j) {
-          s = fma(__ldg(xp), twiddle(J.q, J.D, m), s);
+          const double t = __ldg(xp);
+          if (j & 1) o = fma(t, twiddle(J.q, D, m), o);
+          else e = fma(t, twiddle(J.q, D, m), e);
           xp += J.in_sk;
           m += inc;
           if (m >= D4) m -= D4;
         }
-        acc = J.wm * s;
-      }
-    }
-    if (warp == 0) {
-      if (J.jlo == 0 && 0 < j_end) {
-        const int m = mod4d((long long)J.bj * kk + J.off, D4);
-        acc = fma(J.w0 * __ldg(x), twiddle(J.q, J.D, m), acc);
-      }
-      const int jl = J.N - 1;
-      if (jl > 0 && jl >= J.jlo && jl < j_end) {
-        const int m = mod4d((long long)(J.aj * jl + J.bj) * kk + J.off, D4);
-        acc = fma(J.wl * __ldg(x + (long long)jl * J.in_sk), twiddle(J.q, J.D, m), acc);
+      } else if (J.mode == 2) {
+        // cos: even k pairs with u; sin: even k pairs with v
+        const bool use_u = ((k & 1) == 0) == (J.off == 0);
+        const double* sp = use_u ? su : sv;
+        for (int j = ja; j < jz; ++j) {
+          e = fma(sp[j - ca], twiddle(J.q, D, m), e);
+          m += inc;
+          if (m >= D4) m -= D4;
+        }
+      } else {
+        const double* __restrict__ xp = x + (long long)ja * J.in_sk;
+        for (int j = ja; j < jz; ++j) {
+          e = fma(__ldg(xp), twiddle(J.q, D, m), e);
+          xp += J.in_sk;
+          m += inc;
+          if (m >= D4) m -= D4;
+        }
       }
     }
   }
-  red[warp][lane] = acc;
+  e *= J.wm;
+  o *= J.wm;
+  // end terms and the unpaired middle term, once per tile (chunk 0, warp 0)
+  if (chunk_id == 0 && warp == 0 && lane_on) {
+    const int j_end = min(J.jhi, J.nin);
+    if (J.mode == 2) {
+      if (J.jlo == 0) {  // pair (0, D) with the end weight
+        const double xa = __ldg(x), xb = __ldg(x + (long long)D * J.in_sk);
+        const double t = ((k & 1) == 0) ? xa + xb : xa - xb;
+        e = fma(J.w0 * t, twiddle(J.q, D, mod4d((long long)J.bj * kk + J.off, D4)), e);
+      }
+      if ((D & 1) == 0) {
+        const int jm = D / 2;
+        if (jm >= J.jlo && jm < J.jhi && jm > 0) {
+          const int mm = mod4d((long long)(J.aj * jm + J.bj) * kk + J.off, D4);
+          e = fma(J.wm * __ldg(x + (long long)jm * J.in_sk), twiddle(J.q, D, mm), e);
+        }
+      }
+    } else {
+      if (J.jlo == 0 && 0 < j_end) {
+        const int mm = mod4d((long long)J.bj * kk + J.off, D4);
+        e = fma(J.w0 * __ldg(x), twiddle(J.q, D, mm), e);
+      }
+      const int jl = J.N - 1;
+      if (jl > 0 && jl >= J.jlo && jl < j_end) {
+        const int mm = mod4d((long long)(J.aj * jl + J.bj) * kk + J.off, D4);
+        const double t = J.wl * __ldg(x + (long long)jl * J.in_sk) * twiddle(J.q, D, mm);
+        if (J.mode == 1 && (jl & 1)) o += t;
+        else e += t;
+      }
+    }
+  }
+  red[warp][lane][0] = e;
+  red[warp][lane][1] = o;
   __syncthreads();
-  if (warp == 0 && k < J.nout) {
-    double t = 0.0;
+  double E = 0.0, O = 0.0;
+  if (warp == 0) {
 #pragma unroll
-    for (int w = 0; w < kXWarps; ++w) t += red[w][lane];
-    double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
-    double v = active ? t * sc * J.gscale : 0.0;
-    J.out[(long long)line * J.out_sl + (long long)k * J.out_sk] = v;
+    for (int w = 0; w < kXWarps; ++w) {
+      E += red[w][lane][0];
+      O += red[w][lane][1];
+    }
+  }
+  if (J.nchunk > 1) {
+    double* pp = J.part + ((long long)(line * J.ntile + tile) * J.nchunk) * 64;
+    if (warp == 0) {
+      pp[chunk_id * 64 + 2 * lane] = E;
+      pp[chunk_id * 64 + 2 * lane + 1] = O;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned int* c = J.cnt + (line * J.ntile + tile);
+      const unsigned int t = atomicAdd(c, 1u);
+      amlast = (t == (unsigned int)J.nchunk - 1);
+      if (amlast) *c = 0u;
+    }
+    __syncthreads();
+    if (!amlast) return;
+    if (warp == 0) {
+      E = 0.0;
+      O = 0.0;
+      for (int c = 0; c < J.nchunk; ++c) {
+        E += __ldcg(pp + c * 64 + 2 * lane);
+        O += __ldcg(pp + c * 64 + 2 * lane + 1);
+      }
+    }
+  }
+  if (warp != 0 || !lane_on) return;
+  const double g = J.gscale;
+  auto scale = [&](int kq) { return (kq == 0) ? J.s0 : ((kq == J.N - 1) ? J.sl : J.sm); };
+  auto active = [&](int kq) { return kq >= J.klo && kq < J.khi; };
+  double* out = J.out + (long long)line * J.out_sl;
+  if (J.mode == 1) {
+    const bool is_sin = (J.off != 0);
+    const double yk = E + O;
+    const double yr = is_sin ? (O - E) : (E - O);
+    if (k < J.nout) out[(long long)k * J.out_sk] = active(k) ? yk * scale(k) * g : 0.0;
+    const int kr = D - k;
+    if (kr != k && kr < J.nout) out[(long long)kr * J.out_sk] = active(kr) ? yr * scale(kr) * g : 0.0;
+  } else {
+    if (k < J.nout) out[(long long)k * J.out_sk] = active(k) ? E * scale(k) * g : 0.0;
   }
 }
 
@@ -221,11 +321,75 @@ int axis_kind(int grid_axis_is_z, int dir, int cs) {
   return cs ? K_S1_F2S : K_C1_F2S;
 }
 
-void launch_batch_x(AxisBatch& b, cudaStream_t st) {
+// Decide the symmetry mode and the split of every x-pass job, then launch.
+void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
+  long long tiles_total = 0;
+  for (int i = 0; i < b.njobs; ++i) {
+    AxisJob& J = b.job[i];
+    const bool c1s1 = (J.aj == 2 && J.bj == 0 && J.ak == 1 && J.bk == 0);  // REDFT00 / RODFT00 kinds
+    const int D = J.D;
+    const int j_end = std::min(J.jhi, J.nin);
+    if (c1s1 && J.nout == J.N && D >= 4) {
+      J.mode = 1;
+      J.nlane = D / 2 + 1;
+      J.ta = std::max(J.jlo, 1);
+      J.tb = std::min(j_end, J.N - 1);
+    } else if (c1s1 && J.nin >= J.N && J.nout <= D / 2 + 1 && D >= 4 &&
+               J.w0 == J.wl) {
+      J.mode = 2;
+      J.nlane = J.nout;
+      J.ta = std::max(J.jlo, 1);
+      J.tb = (D + 1) / 2;  // pairs j < D - j
+    } else {
+      J.mode = 0;
+      J.nlane = J.nout;
+      J.ta = std::max(J.jlo, 1);
+      J.tb = std::min(j_end, J.N - 1);
+    }
+    if (J.tb < J.ta) J.tb = J.ta;
+    J.ntile = (J.nlane + 31) / 32;
+    tiles_total += (long long)J.nlines * J.ntile;
+  }
+  const long long target = 4LL * std::max(tb.nsm, 1);
+  long long part_need = 0, cnt_need = 0;
   int total = 0;
   for (int i = 0; i < b.njobs; ++i) {
+    AxisJob& J = b.job[i];
+    int terms = J.tb - J.ta;
+    int nchunk = 1;
+    if (tiles_total < target && terms > 512)
+      nchunk = std::min((int)((target + tiles_total - 1) / tiles_total), (terms + 255) / 256);
+    if (J.mode == 2) nchunk = std::max(nchunk, (terms + kMaxPairChunk - 1) / kMaxPairChunk);
+    int chunk = std::max(1, (terms + nchunk - 1) / std::max(nchunk, 1));
+    nchunk = std::max(1, (terms + chunk - 1) / chunk);
+    J.part = nullptr;
+    J.cnt = nullptr;
+    if (nchunk > 1) {
+      const long long np = (long long)J.nlines * J.ntile * nchunk * 64;
+      const long long nc = (long long)J.nlines * J.ntile;
+      if (part_need + np <= tb.part_cap && cnt_need + nc <= tb.cnt_cap) {
+        J.part = tb.part + part_need;
+        J.cnt = tb.cnt + cnt_need;
+        part_need += np;
+        cnt_need += nc;
+      } else {
+        // not enough scratch for a split sum: one CTA per tile, direct mode
+        if (J.mode == 2) {
+          J.mode = 0;
+          J.nlane = J.nout;
+          J.ntile = (J.nlane + 31) / 32;
+          J.ta = std::max(J.jlo, 1);
+          J.tb = std::max(J.ta, std::min(std::min(J.jhi, J.nin), J.N - 1));
+          terms = J.tb - J.ta;
+        }
+        nchunk = 1;
+        chunk = std::max(terms, 1);
+      }
+    }
+    J.nchunk = nchunk;
+    J.chunk = chunk;
     b.start[i] = total;
-    total += b.job[i].nlines * ((b.job[i].nout + 31) / 32);
+    total += J.nlines * J.ntile * J.nchunk;
   }
   b.start[b.njobs] = total;
   if (total > 0) axis_pass_lanes_k<<<total, kXThreads, 0, st>>>(b);
@@ -306,8 +470,47 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
       Y.gscale = R.scale;
     }
   }
-  launch_batch_x(bx, st);
+  launch_batch_x(bx, tb, st);
   if (by.njobs) launch_batch_y(by, st);
+}
+
+namespace {
+__global__ void k_dfma_peak(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+}  // namespace
+
+double measure_fp64_peak_gflops() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 4, threads = 256, iters = 2048;
+  double* out = nullptr;
+  if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1.0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    cudaEventRecord(e0);
+    k_dfma_peak<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+  return flops / (best * 1e-3) / 1e9;
 }
 
 void launch_y_f2s(const Tables& tb, const double* in, int nlines, long long y_stride, double* out,

@@ -25,7 +25,8 @@ ERRORS = {1: "ARG", 2: "CUDA", 3: "NAN", 4: "TIMEOUT", 5: "DT_UNDERFLOW", 6: "IO
 C_FUNCTIONS = ("hosnwt_read_input", "hosnwt_create", "hosnwt_destroy", "hosnwt_last_error",
                "hosnwt_get_info", "hosnwt_runge4_adapt2", "hosnwt_step", "hosnwt_accept",
                "hosnwt_advance", "hosnwt_run", "hosnwt_get_state", "hosnwt_set_state",
-               "hosnwt_probes", "hosnwt_solveHOS2", "hosnwt_transform", "hosnwt_advance_many")
+               "hosnwt_probes", "hosnwt_solveHOS2", "hosnwt_transform", "hosnwt_advance_many",
+               "hosnwt_time_transform", "hosnwt_fp64_peak", "hosnwt_get_rk_state")
 
 
 class HosInput(ctypes.Structure):
@@ -56,7 +57,8 @@ class HosInfo(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("n1", "n2", "n3", "n3_add", "nd1", "nd2", "mHOS", "p1", "p2")] + \
         [(n, ctypes.c_double) for n in ("Tscale", "xlen", "ylen", "dt_stab", "delt", "delt_out",
                                         "T_stop", "toler", "time_cur")] + \
-        [("nprobes", ctypes.c_int), ("n_rhs", ctypes.c_longlong)]
+        [("nprobes", ctypes.c_int), ("n_rhs", ctypes.c_longlong), ("kernels_per_step", ctypes.c_int),
+         ("device_ms", ctypes.c_double)]
 
 
 _lib = None
@@ -92,6 +94,9 @@ def load_library(path=LIB_PATH):
                                      ctypes.c_double, ctypes.c_double]
     lib.hosnwt_transform.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp]
     lib.hosnwt_advance_many.argtypes = [P(vp), ctypes.c_int, dp, dp]
+    lib.hosnwt_time_transform.argtypes = [vp] + [ctypes.c_int] * 10 + [dp]
+    lib.hosnwt_fp64_peak.argtypes = [dp]
+    lib.hosnwt_get_rk_state.argtypes = [vp] + [dp] * 10
     _lib = lib
     return lib
 
@@ -114,6 +119,14 @@ def make_input(d):
         else:
             setattr(s, name, str(v).encode())
     return s
+
+
+def fp64_peak_gflops():
+    """FP64 FMA throughput of the current device (GFLOP/s)."""
+    v = ctypes.c_double()
+    if load_library().hosnwt_fp64_peak(ctypes.byref(v)) != HOSNWT_OK:
+        raise HosError("hosnwt_fp64_peak failed")
+    return v.value
 
 
 def read_input(path):
@@ -219,6 +232,14 @@ class Tank:
         self._check(rc, "transform")
         return out
 
+    def time_transform(self, grid, direction, csx, csy, nin, nout, batch=1, nrep=20):
+        ms = ctypes.c_double()
+        rc = self.lib.hosnwt_time_transform(self._h, GRID[grid], int(direction), CS[csx], CS[csy],
+                                            int(nin[0]), int(nin[1]), int(nout[0]), int(nout[1]),
+                                            int(batch), int(nrep), ctypes.byref(ms))
+        self._check(rc, "time_transform")
+        return ms.value
+
     def step(self, h_loc):
         err = ctypes.c_double()
         self._check(self.lib.hosnwt_step(self._h, float(h_loc), ctypes.byref(err)), "step")
@@ -243,6 +264,25 @@ class Tank:
         deta = np.zeros((self.n1, self.n2), order="F")
         self._check(self.lib.hosnwt_get_state(self._h, _dptr(eta), _dptr(phis), _dptr(deta)), "get_state")
         return eta, phis, deta
+
+    def get_rk_state(self, out=None):
+        """The 10 arrays of runge4_adapt2 (eta, phis, a_add_1, a_add_2,
+        a_add_ramp, a_add_3, eta1st, eta2nd, a1st, a2nd); `out` may supply
+        preallocated Fortran-ordered arrays (e.g. pinned host memory)."""
+        n1, n2, na = self.n1, self.n2, self.n3_add
+        shapes = [(n1, n2)] * 2 + [(na, n2)] * 4 + [(n1, n2)] * 4
+        arrs = out if out is not None else [np.zeros(s, order="F") for s in shapes]
+        rc = self.lib.hosnwt_get_rk_state(self._h, *[_dptr(a) for a in arrs])
+        self._check(rc, "get_rk_state")
+        return arrs
+
+    def runge4_adapt2_inplace(self, t_o, arrs, h_loc):
+        """runge4_adapt2 on caller-owned Fortran-ordered arrays (no copies)."""
+        err = ctypes.c_double()
+        rc = self.lib.hosnwt_runge4_adapt2(self._h, float(t_o), *[_dptr(a) for a in arrs],
+                                           float(h_loc), ctypes.byref(err))
+        self._check(rc, "runge4_adapt2")
+        return err.value
 
     def set_state(self, eta, phis):
         e = np.array(eta, dtype=np.float64, order="F", copy=True)

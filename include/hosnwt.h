@@ -72,7 +72,10 @@ typedef struct hosnwt_info {
   double Tscale, xlen, ylen, dt_stab, delt, delt_out, T_stop, toler;
   double time_cur;
   int nprobes;
-  long long n_rhs; /* right-hand sides evaluated so far */
+  long long n_rhs;         /* right-hand sides evaluated so far */
+  int kernels_per_step;    /* kernel launches in one RK4(5) step graph */
+  double device_ms;        /* device time of all steps and accepts so far
+                              (CUDA events on the context's stream) */
 } hosnwt_info;
 
 typedef struct hosnwt_ctx hosnwt_ctx;
@@ -118,6 +121,12 @@ int hosnwt_run(hosnwt_ctx* ctx, const char* results_dir);
 
 /* Copy the physical state to host arrays (n1 x n2 each; NULL to skip). */
 int hosnwt_get_state(hosnwt_ctx* ctx, double* eta, double* phis, double* deta);
+/* Copy the 10 arrays runge4_adapt2 advances (same order and shapes) from
+ * the device state (the reference's eta, phis, a1st_add, a2nd_add,
+ * a_add_ramp, a3rd_add, eta1st, eta2nd, a1st, a2nd). */
+int hosnwt_get_rk_state(hosnwt_ctx* ctx, double* eta, double* phis, double* a_add_1,
+                        double* a_add_2, double* a_add_ramp, double* a_add_3, double* eta1st,
+                        double* eta2nd, double* a1st, double* a2nd);
 /* Replace eta and phis (physical space, n1 x n2) on the device. */
 int hosnwt_set_state(hosnwt_ctx* ctx, const double* eta, const double* phis);
 
@@ -141,6 +150,16 @@ int hosnwt_solveHOS2(hosnwt_ctx* ctx, const double* const* y, double* const* k,
  * (fourier_FFTW.f90:235-653). */
 int hosnwt_transform(hosnwt_ctx* ctx, int grid, int dir, int csx, int csy,
                      const double* in, double* out);
+
+/* Measurement hooks (no counterpart in the reference).
+ * hosnwt_time_transform: average device time (ms, CUDA events on the
+ * context's stream) of `nrep` launches of one batched transform of `batch`
+ * requests on the given grid with nonzero input extent nin1 x nin2 and
+ * written output extent nout1 x nout2.
+ * hosnwt_fp64_peak: FP64 FMA throughput of the current device (GFLOP/s). */
+int hosnwt_time_transform(hosnwt_ctx* ctx, int grid, int dir, int csx, int csy, int nin1, int nin2,
+                          int nout1, int nout2, int batch, int nrep, double* ms_per_launch);
+int hosnwt_fp64_peak(double* gflops);
 
 /* Batched ensemble (independent tanks, no collective): advance every context
  * to time_next (its own nondimensional clock) with per-tank adaptive dt.
