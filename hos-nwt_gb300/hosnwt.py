@@ -26,7 +26,8 @@ C_FUNCTIONS = ("hosnwt_read_input", "hosnwt_create", "hosnwt_destroy", "hosnwt_l
                "hosnwt_get_info", "hosnwt_runge4_adapt2", "hosnwt_step", "hosnwt_accept",
                "hosnwt_advance", "hosnwt_run", "hosnwt_get_state", "hosnwt_set_state",
                "hosnwt_probes", "hosnwt_solveHOS2", "hosnwt_transform", "hosnwt_advance_many",
-               "hosnwt_time_transform", "hosnwt_fp64_peak", "hosnwt_get_rk_state")
+               "hosnwt_time_transform", "hosnwt_fp64_peak", "hosnwt_get_rk_state",
+               "hosnwt_transform_noalloc")
 
 
 class HosInput(ctypes.Structure):
@@ -97,6 +98,8 @@ def load_library(path=LIB_PATH):
     lib.hosnwt_time_transform.argtypes = [vp] + [ctypes.c_int] * 10 + [dp]
     lib.hosnwt_fp64_peak.argtypes = [dp]
     lib.hosnwt_get_rk_state.argtypes = [vp] + [dp] * 10
+    lib.hosnwt_transform_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     _lib = lib
     return lib
 
@@ -141,6 +144,16 @@ def read_input(path):
         v = getattr(s, name)
         out[name] = v.decode() if isinstance(v, bytes) else v
     return out
+
+
+def transform_noalloc(direction, cs, n, nlines, in_ptr, out_ptr, stream=0):
+    """hosnwt_transform_noalloc on device pointers (integers): the transform
+    for callers that cannot allocate device memory; see include/hosnwt.h."""
+    rc = load_library().hosnwt_transform_noalloc(int(direction), CS[cs] if isinstance(cs, str) else int(cs),
+                                                 int(n), int(nlines), ctypes.c_void_p(in_ptr),
+                                                 ctypes.c_void_p(out_ptr), ctypes.c_void_p(stream))
+    if rc != HOSNWT_OK:
+        raise HosError(f"hosnwt_transform_noalloc failed ({ERRORS.get(rc, rc)})")
 
 
 GRID = {"n": 0, "big": 1, "add": 2}

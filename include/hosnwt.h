@@ -161,6 +161,26 @@ int hosnwt_time_transform(hosnwt_ctx* ctx, int grid, int dir, int csx, int csy, 
                           int nout1, int nout2, int batch, int nrep, double* ms_per_launch);
 int hosnwt_fp64_peak(double* gflops);
 
+/* No counterpart in the reference.  A transform for callers that cannot
+ * allocate device memory: hosts whose GPU memory is owned by their own pool
+ * or a fixed budget reserved at start-up, and time loops that must not let
+ * cudaMalloc/cudaFree synchronise the device.  It needs no context and
+ * allocates nothing: the caller passes device arrays `in` and `out` of
+ * `nlines` lines of n doubles each (line stride n); the result equals
+ * hosnwt_transform on the free-surface grid of a 2-D tank (n2 = 1) with
+ * n1 = n: SPACE_2_FOURIER (dir = +1) or FOURIER_2_SPACE (dir = -1), cs 0 cos
+ * (REDFT00), 1 sin (RODFT00 on the interior).  Work goes on `stream` (a
+ * cudaStream_t; NULL for the legacy default stream).
+ * Its only extra memory is one fixed array of about 2.3 MB in the library,
+ * held by every GPU that loads it until the process exits; lengths
+ * 5 <= n <= HOSNWT_NOALLOC_MAX_N, anything else returns HOSNWT_ERR_ARG.
+ * The first call on each device looks up that array's device address; make
+ * that first call before any stream capture.  Every call shares the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+#define HOSNWT_NOALLOC_MAX_N 16385
+int hosnwt_transform_noalloc(int dir, int cs, int n, int nlines, const double* in, double* out,
+                             void* stream);
+
 /* Batched ensemble (independent tanks, no collective): advance every context
  * to time_next (its own nondimensional clock) with per-tank adaptive dt.
  * Launches of different tanks are interleaved on their own streams. */
