@@ -60,6 +60,9 @@ struct AxisJob {
   int ta, tb;                // term range [ta, tb) (interior terms or symmetric pairs)
   double* part;              // nlines * ntile * nchunk * 64 partial sums (nchunk > 1)
   unsigned int* cnt;         // nlines * ntile arrival counters (nchunk > 1)
+  // two-level passes (REDFT00 / RODFT00 kinds with D = A * B)
+  int A, B;                  // 0 when the direct sum is used
+  double* cs;                // nlines * B * (A + 1) * 2 partial cos/sin sums
 };
 
 constexpr int kMaxJobs = 8;
@@ -105,6 +108,8 @@ struct Tables {
   long long part_cap;        // capacity (doubles)
   unsigned int* cnt;         // arrival counters (zero between launches)
   int cnt_cap;
+  double* cs;                // scratch of the two-level passes (may be null)
+  long long cs_cap;
   // quarter-wave tables for D = n1-1, n2-1, nd1-1, nd2-1, n3_add
   const double* q_n1;
   const double* q_n2;

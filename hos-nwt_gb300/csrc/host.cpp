@@ -637,6 +637,10 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
     c.tb.cnt_cap = 4 * c.tb.nsm * 16;
     c.tb.part = dalloc<double>(c, (size_t)c.tb.part_cap);
     c.tb.cnt = dalloc<unsigned int>(c, (size_t)c.tb.cnt_cap);
+    // two-level pass scratch: up to kMaxJobs x-pass jobs over nd2 lines,
+    // B (A+1) 2 <= 2 (D+2) doubles per line for any factor pair
+    c.tb.cs_cap = (long long)kMaxJobs * std::max(nd2, n2) * 4LL * (std::max(nd1, n1) + 2);
+    c.tb.cs = dalloc<double>(c, (size_t)c.tb.cs_cap);
   }
   c.tb.q_n1 = d.q_n1; c.tb.q_n2 = d.q_n2; c.tb.q_nd1 = d.q_nd1; c.tb.q_nd2 = d.q_nd2; c.tb.q_add = d.q_add;
   for (void* p : c.allocs)

@@ -33,19 +33,26 @@ __device__ __forceinline__ int mod4d(long long v, int D4) {
 
 constexpr int kXThreads = 256;   // 8 warps
 constexpr int kXWarps = kXThreads / 32;
-constexpr int kMaxPairChunk = 1024;  // staged symmetric pairs per CTA (mode 2)
+constexpr int kMaxPairChunk = 1024;  // staged terms per CTA
+
+__device__ __forceinline__ double twiddle_s(const double* q, int D, int m) {
+  int mm = (m > 2 * D) ? 4 * D - m : m;
+  return (mm > D) ? -q[2 * D - mm] : q[mm];
+}
 
 // x pass: one CTA = (job, line, tile of 32 lane outputs, chunk of the sum).
-// Lanes own outputs, the 8 warps split the CTA's chunk, chunks of one tile
-// are combined in a fixed order by the last CTA to arrive (no spin-waits).
+// The quarter-wave table of the job and the CTA's chunk of inputs are staged
+// in shared memory; lanes own outputs (twiddles are gathered from shared
+// memory, inputs are broadcast), the 8 warps split the chunk, and the chunks
+// of one tile are combined in a fixed order by the last CTA to arrive.
 //   mode 0: direct sum over the interior terms plus the two end terms
 //   mode 1: output symmetry: lane k accumulates even-j and odd-j sums E, O
 //           and writes out[k] and out[D-k] (full outputs, D = N-1)
-//   mode 2: input symmetry: terms are pairs (j, D-j) staged in shared memory
-//           as u = x_j + x_{D-j}, v = x_j - x_{D-j} (outputs k <= D/2)
+//   mode 2: input symmetry: terms are pairs (j, D-j) staged as
+//           u = x_j + x_{D-j}, v = x_j - x_{D-j} (outputs k <= D/2)
 __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b) {
+  extern __shared__ double smem[];
   __shared__ double red[kXWarps][32][2];
-  __shared__ double su[kMaxPairChunk], sv[kMaxPairChunk];
   __shared__ bool amlast;
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
@@ -62,58 +69,77 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b
   const int kk = J.ak * k + J.bk;
   const int inc = mod4d((long long)J.aj * kk, D4);
   const bool lane_on = k < J.nlane;
+  const long long sk = J.in_sk;
 
-  // this CTA's share [ca, cb) of the term range
+  double* q = smem;                    // D + 1 table entries
+  double* su = smem + (D + 1);         // staged inputs (or u)
+  double* sv = su + kMaxPairChunk;     // v (mode 2)
+  for (int t = threadIdx.x; t <= D; t += kXThreads) q[t] = __ldg(J.q + t);
   const int ca = J.ta + chunk_id * J.chunk;
   const int cb = min(J.tb, ca + J.chunk);
+  // cos: even k pairs with u; sin: even k pairs with v (mode 2)
+  const bool use_v = (J.mode == 2) && (((k & 1) == 0) != (J.off == 0));
   double e = 0.0, o = 0.0;  // mode 1: even / odd j sums; else e only
-  if (J.mode == 2) {
-    for (int t = threadIdx.x; t < cb - ca; t += kXThreads) {
-      const int j = ca + t;
-      const double xa = __ldg(x + (long long)j * J.in_sk);
-      const double xb = __ldg(x + (long long)(D - j) * J.in_sk);
-      su[t] = xa + xb;
-      sv[t] = xa - xb;
+  for (int sa = ca; sa < cb; sa += kMaxPairChunk) {
+    const int sb = min(cb, sa + kMaxPairChunk);
+    __syncthreads();  // previous stage consumed
+    if (J.mode == 2) {
+      for (int t = threadIdx.x; t < sb - sa; t += kXThreads) {
+        const int j = sa + t;
+        const double xa = __ldg(x + (long long)j * sk);
+        const double xb = __ldg(x + (long long)(D - j) * sk);
+        su[t] = xa + xb;
+        sv[t] = xa - xb;
+      }
+    } else {
+      for (int t = threadIdx.x; t < sb - sa; t += kXThreads) su[t] = __ldg(x + (long long)(sa + t) * sk);
     }
     __syncthreads();
-  }
-  if (cb > ca) {
-    const int len = cb - ca;
+    const int len = sb - sa;
     const int per = (len + kXWarps - 1) / kXWarps;
-    const int ja = ca + warp * per;
-    const int jz = min(cb, ja + per);
+    const int ja = sa + warp * per;
+    const int jz = min(sb, ja + per);
     if (lane_on && jz > ja) {
       int m = mod4d((long long)(J.aj * ja + J.bj) * kk + J.off, D4);
       if (J.mode == 1) {
-        const double* __restrict__ xp = x + (long long)ja * J.in_sk;
-        for (int j = ja; j < jz; ++j) {
-          const double t = __ldg(xp);
-          if (j & 1) o = fma(t, twiddle(J.q, D, m), o);
-          else e = fma(t, twiddle(J.q, D, m), e);
-          xp += J.in_sk;
+        int j = ja;
+        if (j & 1) {  // align to an even j
+          o = fma(su[j - sa], twiddle_s(q, D, m), o);
           m += inc;
           if (m >= D4) m -= D4;
+          ++j;
         }
-      } else if (J.mode == 2) {
-        // cos: even k pairs with u; sin: even k pairs with v
-        const bool use_u = ((k & 1) == 0) == (J.off == 0);
-        const double* sp = use_u ? su : sv;
-        for (int j = ja; j < jz; ++j) {
-          e = fma(sp[j - ca], twiddle(J.q, D, m), e);
+        for (; j + 1 < jz; j += 2) {
+          const double te = twiddle_s(q, D, m);
           m += inc;
           if (m >= D4) m -= D4;
+          const double to = twiddle_s(q, D, m);
+          m += inc;
+          if (m >= D4) m -= D4;
+          e = fma(su[j - sa], te, e);
+          o = fma(su[j + 1 - sa], to, o);
         }
+        if (j < jz) e = fma(su[j - sa], twiddle_s(q, D, m), e);
       } else {
-        const double* __restrict__ xp = x + (long long)ja * J.in_sk;
-        for (int j = ja; j < jz; ++j) {
-          e = fma(__ldg(xp), twiddle(J.q, D, m), e);
-          xp += J.in_sk;
+        const double* sp = use_v ? sv : su;
+        double e2 = 0.0;
+        int j = ja;
+        for (; j + 1 < jz; j += 2) {
+          const double t0 = twiddle_s(q, D, m);
           m += inc;
           if (m >= D4) m -= D4;
+          const double t1 = twiddle_s(q, D, m);
+          m += inc;
+          if (m >= D4) m -= D4;
+          e = fma(sp[j - sa], t0, e);
+          e2 = fma(sp[j + 1 - sa], t1, e2);
         }
+        if (j < jz) e = fma(sp[j - sa], twiddle_s(q, D, m), e);
+        e += e2;
       }
     }
   }
+  if (cb <= ca) __syncthreads();  // table staged even when this CTA has no terms
   e *= J.wm;
   o *= J.wm;
   // end terms and the unpaired middle term, once per tile (chunk 0, warp 0)
@@ -121,26 +147,26 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b
     const int j_end = min(J.jhi, J.nin);
     if (J.mode == 2) {
       if (J.jlo == 0) {  // pair (0, D) with the end weight
-        const double xa = __ldg(x), xb = __ldg(x + (long long)D * J.in_sk);
+        const double xa = __ldg(x), xb = __ldg(x + (long long)D * sk);
         const double t = ((k & 1) == 0) ? xa + xb : xa - xb;
-        e = fma(J.w0 * t, twiddle(J.q, D, mod4d((long long)J.bj * kk + J.off, D4)), e);
+        e = fma(J.w0 * t, twiddle_s(q, D, mod4d((long long)J.bj * kk + J.off, D4)), e);
       }
       if ((D & 1) == 0) {
         const int jm = D / 2;
         if (jm >= J.jlo && jm < J.jhi && jm > 0) {
           const int mm = mod4d((long long)(J.aj * jm + J.bj) * kk + J.off, D4);
-          e = fma(J.wm * __ldg(x + (long long)jm * J.in_sk), twiddle(J.q, D, mm), e);
+          e = fma(J.wm * __ldg(x + (long long)jm * sk), twiddle_s(q, D, mm), e);
         }
       }
     } else {
       if (J.jlo == 0 && 0 < j_end) {
         const int mm = mod4d((long long)J.bj * kk + J.off, D4);
-        e = fma(J.w0 * __ldg(x), twiddle(J.q, D, mm), e);
+        e = fma(J.w0 * __ldg(x), twiddle_s(q, D, mm), e);
       }
       const int jl = J.N - 1;
       if (jl > 0 && jl >= J.jlo && jl < j_end) {
         const int mm = mod4d((long long)(J.aj * jl + J.bj) * kk + J.off, D4);
-        const double t = J.wl * __ldg(x + (long long)jl * J.in_sk) * twiddle(J.q, D, mm);
+        const double t = J.wl * __ldg(x + (long long)jl * sk) * twiddle_s(q, D, mm);
         if (J.mode == 1 && (jl & 1)) o += t;
         else e += t;
       }
@@ -260,6 +286,112 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
   }
 }
 
+// Two-level passes for REDFT00 / RODFT00 kinds when D = A * B.  With
+// j = B j1 + j2, pi j k / D = pi j1 k / A + pi j2 k / D, so
+//   cos-kind: y_k = sum_j2 [cos(pi j2 k/D) C(j2,k) - sin(pi j2 k/D) S(j2,k)]
+//   sin-kind: y_k = sum_j2 [cos(pi j2 k/D) S(j2,k) + sin(pi j2 k/D) C(j2,k)]
+// with C, S = sum_j1 w_j x_j cos / sin(pi j1 k / A), which depend on k only
+// through k mod 2A (C even, S odd about A).  Pass 1 computes C, S for
+// k' = 0..A; pass 2 combines them.  Work: 2 (A+1) nin + 2 B nout FMAs
+// instead of about nin * nout / 2 for the direct sum.
+constexpr int kTThreads = 256;
+constexpr int kTSplit = 8;                    // lanes sharing one output's sum
+constexpr int kTOut = kTThreads / kTSplit;    // outputs per CTA
+
+__device__ __forceinline__ double group_sum(double v) {
+#pragma unroll
+  for (int o = kTSplit / 2; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o, kTSplit);
+  return v;
+}
+
+__global__ void __launch_bounds__(kTThreads) two_level_pass1(const AxisBatch b) {
+  int jb = 0;
+  while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
+  const AxisJob& J = b.job[jb];
+  const int nout1 = J.B * (J.A + 1);
+  const int per_line = (nout1 + kTOut - 1) / kTOut;
+  const int local = blockIdx.x - b.start[jb];
+  const int line = local / per_line;
+  const int sub = threadIdx.x % kTSplit;
+  const int t = (local - line * per_line) * kTOut + threadIdx.x / kTSplit;
+  const bool on = t < nout1;
+  const int j2 = on ? t / (J.A + 1) : 0, kp = on ? t - j2 * (J.A + 1) : 0;
+  const int D = J.D, D4 = 4 * D;
+  const double* __restrict__ x = J.in + (long long)line * J.in_sl;
+  const int j_end = on ? min(J.jhi, J.nin) : 0;  // terms j in [jlo, j_end)
+  // cos(pi j1 kp / A) = cos(pi * 2 B j1 kp / (2D)): table step 2 B kp per j1
+  const long long step1 = (2LL * J.B * kp) % D4;
+  const int inc = (int)((step1 * kTSplit) % D4);
+  int m = (int)((step1 * sub) % D4);
+  double c = 0.0, s = 0.0;
+  for (int j = j2 + sub * J.B; j < j_end; j += kTSplit * J.B) {
+    if (j >= J.jlo) {
+      const double w = (j == 0) ? J.w0 : ((j == J.N - 1) ? J.wl : J.wm);
+      const double v = w * __ldg(x + (long long)j * J.in_sk);
+      c = fma(v, twiddle(J.q, D, m), c);
+      int ms = m - D;
+      if (ms < 0) ms += D4;
+      s = fma(v, twiddle(J.q, D, ms), s);
+    }
+    m += inc;
+    if (m >= D4) m -= D4;
+  }
+  c = group_sum(c);
+  s = group_sum(s);
+  if (on && sub == 0) {
+    double* cs = J.cs + (((long long)line * J.B + j2) * (J.A + 1) + kp) * 2;
+    cs[0] = c;
+    cs[1] = s;
+  }
+}
+
+__global__ void __launch_bounds__(kTThreads) two_level_pass2(const AxisBatch b) {
+  int jb = 0;
+  while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
+  const AxisJob& J = b.job[jb];
+  const int per_line = (J.nout + kTOut - 1) / kTOut;
+  const int local = blockIdx.x - b.start[jb];
+  const int line = local / per_line;
+  const int sub = threadIdx.x % kTSplit;
+  const int k = (local - line * per_line) * kTOut + threadIdx.x / kTSplit;
+  const bool on = k < J.nout && k >= J.klo && k < J.khi;
+  const int D = J.D, D4 = 4 * D, A = J.A;
+  int kp = on ? k % (2 * A) : 0;
+  double ssign = 1.0;
+  if (kp > A) {
+    kp = 2 * A - kp;
+    ssign = -1.0;
+  }
+  const bool is_sin = (J.off != 0);
+  const double* cs = J.cs + ((long long)line * J.B * (A + 1) + kp) * 2;
+  const long long step2 = on ? (2LL * k) % D4 : 0;
+  const int inc = (int)((step2 * kTSplit) % D4);
+  int m = (int)((step2 * sub) % D4);
+  double acc = 0.0;
+  const int jz = on ? J.B : 0;
+  for (int j2 = sub; j2 < jz; j2 += kTSplit) {
+    const double C = __ldg(cs + (long long)j2 * (A + 1) * 2);
+    const double S = ssign * __ldg(cs + (long long)j2 * (A + 1) * 2 + 1);
+    const double cw = twiddle(J.q, D, m);
+    int ms = m - D;
+    if (ms < 0) ms += D4;
+    const double sw = twiddle(J.q, D, ms);
+    if (is_sin) acc = fma(cw, S, fma(sw, C, acc));
+    else acc = fma(cw, C, fma(-sw, S, acc));
+    m += inc;
+    if (m >= D4) m -= D4;
+  }
+  acc = group_sum(acc);
+  if (sub != 0 || k >= J.nout) return;
+  double* out = J.out + (long long)line * J.out_sl + (long long)k * J.out_sk;
+  if (!on) {
+    *out = 0.0;
+    return;
+  }
+  const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
+  *out = acc * sc * J.gscale;
+}
+
 // Fill the kind-dependent parameters of a pass.
 void set_kind(AxisJob& J, int kind, int N, const double* q) {
   J.N = N;
@@ -321,6 +453,42 @@ int axis_kind(int grid_axis_is_z, int dir, int cs) {
   return cs ? K_S1_F2S : K_C1_F2S;
 }
 
+// Choose D = A * B minimising the two-level work 2 (A+1) nin + 2 B nout;
+// A = 0 when the direct sum (about nin * nout / 2 FMAs) is cheaper.
+void pick_factors(int D, int nin, int nout, int* Aout, int* Bout) {
+  *Aout = *Bout = 0;
+  const double direct = 0.5 * (double)nin * (double)nout;
+  double best = 0.6 * direct;  // two passes must pay for the second launch
+  for (int A = 2; A <= D / 2; ++A) {
+    if (D % A) continue;
+    const int B = D / A;
+    if (B < 2) continue;
+    const double cost = 2.0 * (A + 1) * (double)nin + 2.0 * B * (double)nout;
+    if (cost < best) {
+      best = cost;
+      *Aout = A;
+      *Bout = B;
+    }
+  }
+}
+
+void launch_two_level(AxisBatch& b, cudaStream_t st) {
+  int total = 0;
+  for (int i = 0; i < b.njobs; ++i) {
+    b.start[i] = total;
+    total += b.job[i].nlines * ((b.job[i].B * (b.job[i].A + 1) + kTOut - 1) / kTOut);
+  }
+  b.start[b.njobs] = total;
+  if (total > 0) two_level_pass1<<<total, kTThreads, 0, st>>>(b);
+  total = 0;
+  for (int i = 0; i < b.njobs; ++i) {
+    b.start[i] = total;
+    total += b.job[i].nlines * ((b.job[i].nout + kTOut - 1) / kTOut);
+  }
+  b.start[b.njobs] = total;
+  if (total > 0) two_level_pass2<<<total, kTThreads, 0, st>>>(b);
+}
+
 // Decide the symmetry mode and the split of every x-pass job, then launch.
 void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
   long long tiles_total = 0;
@@ -359,7 +527,6 @@ void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
     int nchunk = 1;
     if (tiles_total < target && terms > 512)
       nchunk = std::min((int)((target + tiles_total - 1) / tiles_total), (terms + 255) / 256);
-    if (J.mode == 2) nchunk = std::max(nchunk, (terms + kMaxPairChunk - 1) / kMaxPairChunk);
     int chunk = std::max(1, (terms + nchunk - 1) / std::max(nchunk, 1));
     nchunk = std::max(1, (terms + chunk - 1) / chunk);
     J.part = nullptr;
@@ -373,15 +540,7 @@ void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
         part_need += np;
         cnt_need += nc;
       } else {
-        // not enough scratch for a split sum: one CTA per tile, direct mode
-        if (J.mode == 2) {
-          J.mode = 0;
-          J.nlane = J.nout;
-          J.ntile = (J.nlane + 31) / 32;
-          J.ta = std::max(J.jlo, 1);
-          J.tb = std::max(J.ta, std::min(std::min(J.jhi, J.nin), J.N - 1));
-          terms = J.tb - J.ta;
-        }
+        // not enough scratch for a split sum: one CTA per tile
         nchunk = 1;
         chunk = std::max(terms, 1);
       }
@@ -392,7 +551,15 @@ void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
     total += J.nlines * J.ntile * J.nchunk;
   }
   b.start[b.njobs] = total;
-  if (total > 0) axis_pass_lanes_k<<<total, kXThreads, 0, st>>>(b);
+  size_t smem = 0;
+  for (int i = 0; i < b.njobs; ++i)
+    smem = std::max(smem, sizeof(double) * ((size_t)b.job[i].D + 1 + 2 * (size_t)kMaxPairChunk));
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(axis_pass_lanes_k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set = true;
+  }
+  if (total > 0) axis_pass_lanes_k<<<total, kXThreads, smem, st>>>(b);
 }
 
 void launch_batch_y(AxisBatch& b, cudaStream_t st) {
@@ -470,7 +637,32 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
       Y.gscale = R.scale;
     }
   }
-  launch_batch_x(bx, tb, st);
+  // two-level passes for the jobs whose length factors well
+  AxisBatch b2{}, bd{};
+  b2.njobs = bd.njobs = 0;
+  long long cs_used = 0;
+  for (int i = 0; i < bx.njobs; ++i) {
+    AxisJob J = bx.job[i];
+    J.A = J.B = 0;
+    J.cs = nullptr;
+    const bool c1s1 = (J.aj == 2 && J.bj == 0 && J.ak == 1 && J.bk == 0);
+    if (c1s1 && tb.cs) {
+      int A = 0, B = 0;
+      pick_factors(J.D, std::min(J.nin, J.N), J.nout, &A, &B);
+      const long long need = (long long)J.nlines * B * (A + 1) * 2;
+      if (A > 0 && cs_used + need <= tb.cs_cap) {
+        J.A = A;
+        J.B = B;
+        J.cs = tb.cs + cs_used;
+        cs_used += need;
+        b2.job[b2.njobs++] = J;
+        continue;
+      }
+    }
+    bd.job[bd.njobs++] = J;
+  }
+  if (b2.njobs) launch_two_level(b2, st);
+  if (bd.njobs) launch_batch_x(bd, tb, st);
   if (by.njobs) launch_batch_y(by, st);
 }
 
