@@ -443,7 +443,7 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
   if (nm.p1 > nm.mHOS || nm.p2 > nm.mHOS) return fail(c, HOSNWT_ERR_ARG, "p1/p2 higher than M");
   if (nm.n1 < 5 || nm.n2 < 1 || (nm.n2 > 1 && nm.n2 < 5) || nm.n3 < 5)
     return fail(c, HOSNWT_ERR_ARG, "grid too small (n1, n3 >= 5; n2 = 1 or >= 5)");
-  if (nm.mHOS > 15) return fail(c, HOSNWT_ERR_ARG, "mHOS > 15");
+  if (nm.mHOS > 11) return fail(c, HOSNWT_ERR_ARG, "mHOS > 11 is not supported");
   if (nm.n3 > 257) return fail(c, HOSNWT_ERR_ARG, "n3 > 257 (n3_add is limited to 512)");
   P.n1 = nm.n1; P.n2 = nm.n2; P.n3 = nm.n3; P.M = nm.mHOS; P.p1 = nm.p1; P.p2 = nm.p2;
   P.l_add = 2;
@@ -679,6 +679,7 @@ int alloc_device(Ctx& c) {
                      &d.tbig, &d.tbig2, &d.tbig3, &d.pxe, &d.pye, &d.pze, &d.A1, &d.A3, &d.t1,
                      &d.geta2phiz, &d.geta2phiz2})
     *p = dalloc<double>(c, std::max(nB, nN));
+  for (int g = 0; g < 24; ++g) d.grp[g] = dalloc<double>(c, std::max(nB, nN));
   d.bc1 = dalloc<double>(c, nA);
   d.bcr = dalloc<double>(c, nA);
   if (P.n2 != 1) {

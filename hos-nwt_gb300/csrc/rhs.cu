@@ -124,6 +124,66 @@ __global__ void k_pow(const double* __restrict__ prev, const double* __restrict_
   if (i < n) out[i] = prev[i] / jp1 * e1[i];
 }
 
+// eta^j / j! for a run of orders without dealiasing in between:
+// e_{j+1} = e_j / (j+1) * e_1 for j = j0 .. j1-1 (resol_HOS.f90:979-987)
+struct PowArgs {
+  double* e[16];
+  int j0, j1;
+};
+__global__ void k_pow_run(PowArgs a, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double e1 = a.e[0][i];
+  double v = a.e[a.j0 - 1][i];
+  for (int j = a.j0; j < a.j1; ++j) {
+    v = v / (double)(j + 1) * e1;
+    a.e[j][i] = v;
+  }
+}
+
+// Products of HOSphis_modes' quadratic terms accumulated per dealiasing
+// group: out[g] = sum over the group's terms of s * x * y (x, y big-grid
+// fields); the terms of each group keep the reference's order.
+struct GroupTerms {
+  const double* x[48];
+  const double* y[48];
+  double s[48];
+  int group[48];
+  int nterm;
+  double* out[16];
+  int ngroup;
+};
+__global__ void k_group_products(GroupTerms g, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double acc[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) acc[q] = 0.0;
+  for (int t = 0; t < g.nterm; ++t) {
+    const double v = (g.s[t] * g.x[t][i]) * g.y[t][i];
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+      if (q == g.group[t]) acc[q] += v;
+  }
+  for (int q = 0; q < g.ngroup; ++q) g.out[q][i] = acc[q];
+}
+
+// out = sum of listed fields, optionally times gradeta2 (scale field)
+struct SumArgs {
+  const double* in[16];
+  int nin;
+  const double* scale;
+  double* out;
+};
+__global__ void k_sum_fields(SumArgs a, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v = 0.0;
+  for (int t = 0; t < a.nin; ++t) v += a.in[t][i];
+  if (a.scale) v = a.scale[i] * v;
+  a.out[i] = v;
+}
+
 // out = s * x * y  (s applied first, as 2.0_rp * a * b in the reference)
 __global__ void k_mul(const double* __restrict__ x, const double* __restrict__ y, double s,
                       double* out, long long n) {
@@ -192,26 +252,42 @@ __global__ void k_fs_products(const double* __restrict__ etax, const double* __r
 
 // A1 = detext + geta2phiz + phizMm1 + phizm(M) - grad eta.grad phi_add
 // A3 = 0.5 * (dphext + geta2phiz2 + phiz2) - grad phis.grad phi_add - |grad phi_add|^2/2
-__global__ void k_assemble(const double* __restrict__ detext, const double* __restrict__ dphext,
-                           const double* __restrict__ geta2phiz, const double* __restrict__ geta2phiz2,
-                           const double* __restrict__ phiz2, const double* __restrict__ phizMm1,
-                           const double* __restrict__ phizmM, const double* __restrict__ etax,
-                           const double* __restrict__ etay, const double* __restrict__ phisx,
-                           const double* __restrict__ phisy, const double* __restrict__ pxe,
-                           const double* __restrict__ pye, const double* __restrict__ pze,
-                           double* A1, double* A3, long long n, int M) {
+// (resol_HOS.f90:382-399, 534-608 before filter_ext, which is linear).
+// detext / dphext are the order-2 products -grad phis.grad eta, -|grad phis|^2,
+// computed here unless the caller dealiased them (p = 2).
+struct AssembleArgs {
+  const double *etax, *etay, *phisx, *phisy, *pxe, *pye, *pze;
+  const double *detext, *dphext;
+  const double* phizm[16];  // phizm(1 .. M-1), summed to phizMm1
+  int nphizm;
+  const double* phizmM;
+  const double* g1[8];      // parts of geta2phiz
+  int ng1;
+  const double* g2[8];      // parts of geta2phiz2
+  int ng2;
+  const double* t1[16];     // parts of phiz2
+  int nt1;
+  int M;
+};
+__global__ void k_assemble(AssembleArgs a, double* A1, double* A3, long long n) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double ax = pxe[i], ay = pye[i], az = pze[i];
-  const double gg = etax[i] * ax + etay[i] * ay;
-  const double gpg = phisx[i] * ax + phisy[i] * ay + 0.5 * (ax * ax + ay * ay + az * az);
-  const double det = detext[i] + geta2phiz[i];
-  const double dph = dphext[i] + geta2phiz2[i] + phiz2[i];
-  if (M >= 2) {
-    A1[i] = det + phizMm1[i] + phizmM[i] - gg;
+  const double ex = a.etax[i], ey = a.etay[i], px = a.phisx[i], py = a.phisy[i];
+  const double ax = a.pxe[i], ay = a.pye[i], az = a.pze[i];
+  const double gg = ex * ax + ey * ay;
+  const double gpg = px * ax + py * ay + 0.5 * (ax * ax + ay * ay + az * az);
+  double det = a.detext ? a.detext[i] : (-px * ex - py * ey);
+  double dph = a.dphext ? a.dphext[i] : (-px * px - py * py);
+  for (int t = 0; t < a.ng1; ++t) det += a.g1[t][i];
+  for (int t = 0; t < a.ng2; ++t) dph += a.g2[t][i];
+  for (int t = 0; t < a.nt1; ++t) dph += a.t1[t][i];
+  if (a.M >= 2) {
+    double mm1 = 0.0;
+    for (int t = 0; t < a.nphizm; ++t) mm1 += a.phizm[t][i];
+    A1[i] = det + mm1 + a.phizmM[i] - gg;
     A3[i] = 0.5 * dph - gpg;
   } else {
-    A1[i] = phizmM[i];
+    A1[i] = a.phizmM[i];
     A3[i] = 0.0;
   }
 }
@@ -827,11 +903,18 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
       cudaMemsetAsync(d.phisy, 0, sizeof(double) * nB, st);
     }
   }
-  // 3. powers eta^j / j! with partial dealiasing
-  for (int j = 1; j < M; ++j) {
-    E.ew(k_pow, nB, (const double*)d.etapm[j - 1], (const double*)d.etapm[0], (double)(j + 1),
-         d.etapm[j], nB);
-    E.dealias(j + 1, d.etapm[j]);
+  // 3. powers eta^j / j! with partial dealiasing: one kernel per run of
+  //    orders up to the next order that is dealiased
+  for (int j = 1; j < M;) {
+    int jend = j + 1;
+    while (jend < M && !E.dealias_on(jend)) ++jend;
+    PowArgs pa{};
+    for (int t = 0; t < M; ++t) pa.e[t] = d.etapm[t];
+    pa.j0 = j;
+    pa.j1 = jend;
+    E.ew(k_pow_run, nB, pa, nB);
+    E.dealias(jend, d.etapm[jend - 1]);
+    j = jend;
   }
   E.ew(k_sq2, nB, (const double*)d.etax, (const double*)d.etay, d.gradeta2, nB);
   E.dealias(2, d.gradeta2);
@@ -867,44 +950,78 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
       E.xf(rq);
     }
   }
-  // phizMm1 = sum_{j<M} phizm(j)
-  cudaMemsetAsync(d.phizMm1, 0, sizeof(double) * nB, st);
-  if (M >= 2) {
-    for (int j = 1; j <= M - 2; ++j) E.ew(k_add, nB, d.phizMm1, (const double*)d.phizm[j], nB);
-    E.ew(k_add, nB, d.phizMm1, (const double*)d.phizm[M - 1], nB);
-  }
-  // gradeta2 * phiz at order M (geta2phiz) and phiz^2, gradeta2 * phiz^2
-  cudaMemsetAsync(d.geta2phiz, 0, sizeof(double) * nB, st);
-  for (int j = 1; j <= M - 3; ++j) {
-    E.ew(k_mul, nB, (const double*)d.gradeta2, (const double*)d.phizm[j], 1.0, d.tbig, nB);
-    E.dealias(j + 2, d.tbig);
-    E.ew(k_add, nB, d.geta2phiz, (const double*)d.tbig, nB);
-  }
-  if (M >= 3) {
-    E.ew(k_mul, nB, (const double*)d.gradeta2, (const double*)d.phizm[std::max(M - 2, 1)], 1.0,
-         d.tbig, nB);
-    E.dealias(M, d.tbig);
-    E.ew(k_add, nB, d.geta2phiz, (const double*)d.tbig, nB);
-  }
-  cudaMemsetAsync(d.t1, 0, sizeof(double) * nB, st);
-  cudaMemsetAsync(d.geta2phiz2, 0, sizeof(double) * nB, st);
-  auto sq_term = [&](int j, int q, double s, int order, bool with_geta) {
-    E.ew(k_mul, nB, (const double*)d.phizm[j], (const double*)d.phizm[q], s, d.tbig, nB);
-    E.dealias(order, d.tbig);
-    E.ew(k_add, nB, d.t1, (const double*)d.tbig, nB);
-    if (with_geta) {
-      E.ew(k_mul, nB, (const double*)d.gradeta2, (const double*)d.tbig, 1.0, d.tbig2, nB);
-      E.dealias(order + 2, d.tbig2);
-      E.ew(k_add, nB, d.geta2phiz2, (const double*)d.tbig2, nB);
-    }
-  };
-  for (int j = 1; j <= (M - 2) / 2; ++j) sq_term(j, j, 1.0, 2 * j, true);
+  // Quadratic terms of HOSphis_modes (resol_HOS.f90:797-905): every term is
+  // dealiased at its order; dealiasing is linear, so terms are summed per
+  // dealiasing class first (class = which directions the order truncates).
+  struct Term { const double* x; const double* y; double s; int order; int kind; };
+  // kind 0: geta2phiz term, 1: phiz2 term, 2: phiz2 term whose gradeta2
+  // product also enters geta2phiz2 at order + 2
+  std::vector<Term> terms;
+  for (int j = 1; j <= M - 3; ++j) terms.push_back({d.gradeta2, d.phizm[j], 1.0, j + 2, 0});
+  if (M >= 3) terms.push_back({d.gradeta2, d.phizm[std::max(M - 2, 1)], 1.0, M, 0});
+  for (int j = 1; j <= (M - 2) / 2; ++j) terms.push_back({d.phizm[j], d.phizm[j], 1.0, 2 * j, 2});
   for (int j = 2; j <= M - 3; ++j)
-    for (int q = 1; q <= std::min(M - 2 - j, j - 1); ++q) sq_term(j, q, 2.0, j + q, true);
-  if (M >= 2) sq_term(M / 2, M / 2, 1.0, 2 * (M / 2), false);
+    for (int q = 1; q <= std::min(M - 2 - j, j - 1); ++q)
+      terms.push_back({d.phizm[j], d.phizm[q], 2.0, j + q, 2});
+  if (M >= 2) terms.push_back({d.phizm[M / 2], d.phizm[M / 2], 1.0, 2 * (M / 2), 1});
   for (int j = 2; j <= M - 1; ++j)
     for (int q = std::max(0, std::min(M - 2 - j, j - 1)) + 1; q <= std::min(M - j, j - 1); ++q)
-      sq_term(j, q, 2.0, j + q, false);
+      terms.push_back({d.phizm[j], d.phizm[q], 2.0, j + q, 1});
+  auto cls = [&](int order) { return (E.act_x(order) ? 1 : 0) | (E.act_y(order) ? 2 : 0); };
+  // groups keyed by (kind, class(order), class(order+2) for kind 2)
+  std::vector<int> gkind, gc1, gc2;
+  GroupTerms gt{};
+  gt.nterm = 0;
+  for (const Term& t : terms) {
+    const int c1 = cls(t.order), c2 = t.kind == 2 ? cls(t.order + 2) : 0;
+    int g = -1;
+    for (size_t q = 0; q < gkind.size(); ++q)
+      if (gkind[q] == t.kind && gc1[q] == c1 && gc2[q] == c2) g = (int)q;
+    if (g < 0) {
+      g = (int)gkind.size();
+      gkind.push_back(t.kind);
+      gc1.push_back(c1);
+      gc2.push_back(c2);
+    }
+    gt.x[gt.nterm] = t.x;
+    gt.y[gt.nterm] = t.y;
+    gt.s[gt.nterm] = t.s;
+    gt.group[gt.nterm] = g;
+    gt.nterm++;
+  }
+  gt.ngroup = (int)gkind.size();
+  for (int g = 0; g < gt.ngroup; ++g) gt.out[g] = d.grp[g];
+  AssembleArgs aa{};
+  aa.ng1 = aa.ng2 = aa.nt1 = 0;
+  if (gt.ngroup > 0) {
+    E.ew(k_group_products, nB, gt, nB);
+    auto dealias_class = [&](int c, double* buf) {
+      if (c == 0) return;
+      const int e1 = (c & 1) ? n1 : nd1, e2 = (c & 2) ? n2 : nd2;
+      E.xf({E.R(GRID_BIG, 1, 0, 0, buf, nd1, nd1, nd2, d.tbig3, nd1, e1, e2)});
+      E.xf({E.F2S_B(d.tbig3, nd1, e1, e2, buf)});
+    };
+    for (int g = 0; g < gt.ngroup; ++g) dealias_class(gc1[g], d.grp[g]);
+    for (int g = 0; g < gt.ngroup; ++g) {
+      if (gkind[g] == 0) aa.g1[aa.ng1++] = d.grp[g];
+      else aa.t1[aa.nt1++] = d.grp[g];
+    }
+    // geta2phiz2: gradeta2 times the kind-2 groups, dealiased by outer class
+    int nu_ = 0;
+    for (int c2 = 0; c2 < 4; ++c2) {
+      SumArgs sa{};
+      sa.nin = 0;
+      for (int g = 0; g < gt.ngroup; ++g)
+        if (gkind[g] == 2 && gc2[g] == c2) sa.in[sa.nin++] = d.grp[g];
+      if (sa.nin == 0) continue;
+      sa.scale = d.gradeta2;
+      sa.out = d.grp[gt.ngroup + nu_];
+      E.ew(k_sum_fields, nB, sa, nB);
+      dealias_class(c2, sa.out);
+      aa.g2[aa.ng2++] = sa.out;
+      nu_++;
+    }
+  }
 
   // 5. wavemaker: SWEET_1 and phiadd_SL
   double* kA1 = k + L.off[S_AADD1];
@@ -983,15 +1100,22 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   E.xf({E.F2S_B(d.pmode[0], n1, n1, n2, d.pxe), E.F2S_B(d.pmode[1], n1, n1, n2, d.pye),
         E.F2S_B(d.pmode[2], n1, n1, n2, d.pze)});
   // 7. free-surface terms, filters to the n grid, final RHS
-  E.ew(k_fs_products, nB, (const double*)d.etax, (const double*)d.etay, (const double*)d.phisx,
-       (const double*)d.phisy, d.tbig, d.tbig2, nB);
-  E.dealias(2, d.tbig);
-  E.dealias(2, d.tbig2);
-  E.ew(k_assemble, nB, (const double*)d.tbig, (const double*)d.tbig2, (const double*)d.geta2phiz,
-       (const double*)d.geta2phiz2, (const double*)d.t1, (const double*)d.phizMm1,
-       (const double*)d.phizm[M], (const double*)d.etax, (const double*)d.etay,
-       (const double*)d.phisx, (const double*)d.phisy, (const double*)d.pxe, (const double*)d.pye,
-       (const double*)d.pze, d.A1, d.A3, nB, M);
+  aa.etax = d.etax; aa.etay = d.etay; aa.phisx = d.phisx; aa.phisy = d.phisy;
+  aa.pxe = d.pxe; aa.pye = d.pye; aa.pze = d.pze;
+  aa.detext = aa.dphext = nullptr;
+  if (E.dealias_on(2)) {
+    E.ew(k_fs_products, nB, (const double*)d.etax, (const double*)d.etay, (const double*)d.phisx,
+         (const double*)d.phisy, d.tbig, d.tbig2, nB);
+    E.dealias(2, d.tbig);
+    E.dealias(2, d.tbig2);
+    aa.detext = d.tbig;
+    aa.dphext = d.tbig2;
+  }
+  aa.nphizm = 0;
+  for (int j = 1; j <= M - 1; ++j) aa.phizm[aa.nphizm++] = d.phizm[j];
+  aa.phizmM = d.phizm[M];
+  aa.M = M;
+  E.ew(k_assemble, nB, aa, d.A1, d.A3, nB);
   // filter_ext: S2F_big truncated to n1 x n2, then F2S on the n grid
   E.xf({E.R(GRID_BIG, 1, 0, 0, d.A1, nd1, nd1, nd2, d.pmode[0], n1, n1, n2),
         E.R(GRID_BIG, 1, 0, 0, d.phizm[1], nd1, nd1, nd2, d.pmode[1], n1, n1, n2),

@@ -77,6 +77,7 @@ struct Dev {
   double *phimext = nullptr, *phizMm1 = nullptr, *tbig = nullptr, *tbig2 = nullptr, *tbig3 = nullptr;
   double *pxe = nullptr, *pye = nullptr, *pze = nullptr, *A1 = nullptr, *A3 = nullptr;
   double *t1 = nullptr, *geta2phiz = nullptr, *geta2phiz2 = nullptr;
+  double* grp[24] = {};         // dealiasing groups of the quadratic terms
   // wavemaker grid
   double *bc1 = nullptr, *bcr = nullptr;
   // 3-D phiadd_SL workspace (n1 * n3a * n2 each)

@@ -295,36 +295,41 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
 // k' = 0..A; pass 2 combines them.  Work: 2 (A+1) nin + 2 B nout FMAs
 // instead of about nin * nout / 2 for the direct sum.
 constexpr int kTThreads = 256;
-constexpr int kTSplit = 8;                    // lanes sharing one output's sum
-constexpr int kTOut = kTThreads / kTSplit;    // outputs per CTA
 
+template <int SPLIT>
 __device__ __forceinline__ double group_sum(double v) {
 #pragma unroll
-  for (int o = kTSplit / 2; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o, kTSplit);
+  for (int o = SPLIT / 2; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o, SPLIT);
   return v;
 }
 
+// SPLIT lanes share one output's sum (8 when there are many outputs, 32 for
+// small launches so that enough warps hide the load latency)
+template <int SPLIT>
 __global__ void __launch_bounds__(kTThreads) two_level_pass1(const AxisBatch b) {
+  constexpr int kOut = kTThreads / SPLIT;
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const AxisJob& J = b.job[jb];
   const int nout1 = J.B * (J.A + 1);
-  const int per_line = (nout1 + kTOut - 1) / kTOut;
+  const int per_line = (nout1 + kOut - 1) / kOut;
   const int local = blockIdx.x - b.start[jb];
   const int line = local / per_line;
-  const int sub = threadIdx.x % kTSplit;
-  const int t = (local - line * per_line) * kTOut + threadIdx.x / kTSplit;
+  const int sub = threadIdx.x % SPLIT;
+  const int t = (local - line * per_line) * kOut + threadIdx.x / SPLIT;
   const bool on = t < nout1;
   const int j2 = on ? t / (J.A + 1) : 0, kp = on ? t - j2 * (J.A + 1) : 0;
   const int D = J.D, D4 = 4 * D;
   const double* __restrict__ x = J.in + (long long)line * J.in_sl;
   const int j_end = on ? min(J.jhi, J.nin) : 0;  // terms j in [jlo, j_end)
   // cos(pi j1 kp / A) = cos(pi * 2 B j1 kp / (2D)): table step 2 B kp per j1
-  const long long step1 = (2LL * J.B * kp) % D4;
-  const int inc = (int)((step1 * kTSplit) % D4);
-  int m = (int)((step1 * sub) % D4);
+  const unsigned d4 = (unsigned)D4;
+  const unsigned step1 = (2u * (unsigned)J.B * (unsigned)kp) % d4;
+  const int inc = (int)((step1 * (unsigned)SPLIT) % d4);
+  int m = (int)((step1 * (unsigned)sub) % d4);
   double c = 0.0, s = 0.0;
-  for (int j = j2 + sub * J.B; j < j_end; j += kTSplit * J.B) {
+#pragma unroll 2
+  for (int j = j2 + sub * J.B; j < j_end; j += SPLIT * J.B) {
     if (j >= J.jlo) {
       const double w = (j == 0) ? J.w0 : ((j == J.N - 1) ? J.wl : J.wm);
       const double v = w * __ldg(x + (long long)j * J.in_sk);
@@ -336,8 +341,8 @@ __global__ void __launch_bounds__(kTThreads) two_level_pass1(const AxisBatch b) 
     m += inc;
     if (m >= D4) m -= D4;
   }
-  c = group_sum(c);
-  s = group_sum(s);
+  c = group_sum<SPLIT>(c);
+  s = group_sum<SPLIT>(s);
   if (on && sub == 0) {
     double* cs = J.cs + (((long long)line * J.B + j2) * (J.A + 1) + kp) * 2;
     cs[0] = c;
@@ -345,15 +350,17 @@ __global__ void __launch_bounds__(kTThreads) two_level_pass1(const AxisBatch b) 
   }
 }
 
+template <int SPLIT>
 __global__ void __launch_bounds__(kTThreads) two_level_pass2(const AxisBatch b) {
+  constexpr int kOut = kTThreads / SPLIT;
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const AxisJob& J = b.job[jb];
-  const int per_line = (J.nout + kTOut - 1) / kTOut;
+  const int per_line = (J.nout + kOut - 1) / kOut;
   const int local = blockIdx.x - b.start[jb];
   const int line = local / per_line;
-  const int sub = threadIdx.x % kTSplit;
-  const int k = (local - line * per_line) * kTOut + threadIdx.x / kTSplit;
+  const int sub = threadIdx.x % SPLIT;
+  const int k = (local - line * per_line) * kOut + threadIdx.x / SPLIT;
   const bool on = k < J.nout && k >= J.klo && k < J.khi;
   const int D = J.D, D4 = 4 * D, A = J.A;
   int kp = on ? k % (2 * A) : 0;
@@ -364,12 +371,14 @@ __global__ void __launch_bounds__(kTThreads) two_level_pass2(const AxisBatch b) 
   }
   const bool is_sin = (J.off != 0);
   const double* cs = J.cs + ((long long)line * J.B * (A + 1) + kp) * 2;
-  const long long step2 = on ? (2LL * k) % D4 : 0;
-  const int inc = (int)((step2 * kTSplit) % D4);
-  int m = (int)((step2 * sub) % D4);
+  const unsigned d4 = (unsigned)D4;
+  const unsigned step2 = on ? (2u * (unsigned)k) % d4 : 0u;
+  const int inc = (int)((step2 * (unsigned)SPLIT) % d4);
+  int m = (int)((step2 * (unsigned)sub) % d4);
   double acc = 0.0;
   const int jz = on ? J.B : 0;
-  for (int j2 = sub; j2 < jz; j2 += kTSplit) {
+#pragma unroll 2
+  for (int j2 = sub; j2 < jz; j2 += SPLIT) {
     const double C = __ldg(cs + (long long)j2 * (A + 1) * 2);
     const double S = ssign * __ldg(cs + (long long)j2 * (A + 1) * 2 + 1);
     const double cw = twiddle(J.q, D, m);
@@ -381,7 +390,7 @@ __global__ void __launch_bounds__(kTThreads) two_level_pass2(const AxisBatch b) 
     m += inc;
     if (m >= D4) m -= D4;
   }
-  acc = group_sum(acc);
+  acc = group_sum<SPLIT>(acc);
   if (sub != 0 || k >= J.nout) return;
   double* out = J.out + (long long)line * J.out_sl + (long long)k * J.out_sk;
   if (!on) {
@@ -472,21 +481,30 @@ void pick_factors(int D, int nin, int nout, int* Aout, int* Bout) {
   }
 }
 
-void launch_two_level(AxisBatch& b, cudaStream_t st) {
+template <int SPLIT>
+void launch_two_level_split(AxisBatch& b, cudaStream_t st) {
+  constexpr int kOut = kTThreads / SPLIT;
   int total = 0;
   for (int i = 0; i < b.njobs; ++i) {
     b.start[i] = total;
-    total += b.job[i].nlines * ((b.job[i].B * (b.job[i].A + 1) + kTOut - 1) / kTOut);
+    total += b.job[i].nlines * ((b.job[i].B * (b.job[i].A + 1) + kOut - 1) / kOut);
   }
   b.start[b.njobs] = total;
-  if (total > 0) two_level_pass1<<<total, kTThreads, 0, st>>>(b);
+  if (total > 0) two_level_pass1<SPLIT><<<total, kTThreads, 0, st>>>(b);
   total = 0;
   for (int i = 0; i < b.njobs; ++i) {
     b.start[i] = total;
-    total += b.job[i].nlines * ((b.job[i].nout + kTOut - 1) / kTOut);
+    total += b.job[i].nlines * ((b.job[i].nout + kOut - 1) / kOut);
   }
   b.start[b.njobs] = total;
-  if (total > 0) two_level_pass2<<<total, kTThreads, 0, st>>>(b);
+  if (total > 0) two_level_pass2<SPLIT><<<total, kTThreads, 0, st>>>(b);
+}
+
+void launch_two_level(AxisBatch& b, cudaStream_t st) {
+  long long outputs = 0;
+  for (int i = 0; i < b.njobs; ++i) outputs += (long long)b.job[i].nlines * b.job[i].nout;
+  if (outputs < 65536) launch_two_level_split<32>(b, st);
+  else launch_two_level_split<8>(b, st);
 }
 
 // Decide the symmetry mode and the split of every x-pass job, then launch.
