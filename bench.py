@@ -304,13 +304,91 @@ def run_cuda(args, w):
         dist.destroy_process_group()
 
 
+def run_ensemble(args):
+    """Pattern 2: 64 independent 2-D tanks of uneven n1 / M, advanced by the
+    same simulated time one after another and then all together
+    (hosnwt_advance_many, one stream per tank).  Reports aggregate simulated
+    tank-seconds per wall-second of both and their ratio."""
+    import torch
+    import hosnwt
+    specs = workloads.ensemble()
+    tanks = [hosnwt.Tank(s["inp"], s["n1"], 1, s["n3"], s["mHOS"], s["p1"], 1, probes=s["probes"])
+             for s in specs]
+    sim_s = args.sim_seconds
+    infos = [t.info() for t in tanks]
+    # warm-up: every tank a short stretch alone
+    h = [i["delt"] for i in infos]
+    for k, t in enumerate(tanks):
+        h[k], _, _ = t.advance(0.05 / infos[k]["Tscale"], h[k])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    steps0 = sum(t.info()["n_rhs"] for t in tanks)
+    for k, t in enumerate(tanks):
+        inf = t.info()
+        h[k], _, _ = t.advance(inf["time_cur"] + sim_s / inf["Tscale"], h[k])
+    torch.cuda.synchronize()
+    seq = time.perf_counter() - t0
+    steps_seq = sum(t.info()["n_rhs"] for t in tanks) - steps0
+    t0 = time.perf_counter()
+    tn = [t.info()["time_cur"] + sim_s / t.info()["Tscale"] for t in tanks]
+    h = list(hosnwt.advance_many(tanks, tn, h))
+    torch.cuda.synchronize()
+    bat = time.perf_counter() - t0
+    steps_bat = sum(t.info()["n_rhs"] for t in tanks) - steps0 - steps_seq
+    line = {"metric": "ensemble tank-sim-s/wall-s (64 independent 2-D tanks)", "value": len(tanks) * sim_s / bat,
+            "unit": "tank-sim-s/wall-s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": "ensemble: 64 x 2-D JONSWAP tanks, n1 in {129..2049}, M in {3,5,7}, p1=M, "
+                                   "tol 1e-7, per-tank adaptive dt", "sim_seconds_per_tank": sim_s},
+            "sequential_value": len(tanks) * sim_s / seq, "batched_over_sequential": seq / bat,
+            "rk_steps": {"sequential": steps_seq // 5, "batched": steps_bat // 5},
+            "wall_s": {"sequential": seq, "batched": bat}}
+    print(json.dumps(line), flush=True)
+
+
+def run_3d(args):
+    """The 3-D directional tank (513 x 257, M = 5, p = 4): RK4(5) steps/s."""
+    import torch
+    import hosnwt
+    with tempfile.TemporaryDirectory() as tmp:
+        w = workloads.directional_3d(tmp)
+        tank = hosnwt.Tank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
+                           probes=w["probes"], wave_dir=w["wave_dir"])
+    inf = tank.info()
+    h = inf["delt"]
+    for _ in range(args.warmup):
+        tank.step(h)
+        tank.accept(h)
+    torch.cuda.synchronize()
+    ms0 = tank.info()["device_ms"]
+    for _ in range(args.steps):
+        tank.step(h)
+        tank.accept(h)
+    dev_ms = tank.info()["device_ms"] - ms0
+    line = {"metric": "RK4(5) steps/s, 3-D directional tank", "value": args.steps / (dev_ms * 1e-3),
+            "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "directional_3d: 50x30 m, n1=513 n2=257 n3=33 M=5 p1=p2=4",
+                       "nd1": inf["nd1"], "nd2": inf["nd2"], "dt_s": h * inf["Tscale"]},
+            "sim_s_per_wall_s": args.steps * h * inf["Tscale"] / (dev_ms * 1e-3)}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cuda", choices=("cuda", "reference"))
+    ap.add_argument("--workload", default="irregular_2d", choices=("irregular_2d", "ensemble", "directional_3d"))
+    ap.add_argument("--sim-seconds", type=float, default=1.0, help="ensemble: simulated seconds per tank")
     args = ap.parse_args()
+    if args.workload == "ensemble":
+        run_ensemble(args)
+        return
+    if args.workload == "directional_3d":
+        run_3d(args)
+        return
     with tempfile.TemporaryDirectory() as tmp:
         w = workloads.irregular_2d(tmp)
         if args.impl == "reference":

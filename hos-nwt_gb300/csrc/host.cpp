@@ -1082,12 +1082,82 @@ extern "C" int hosnwt_transform(hosnwt_ctx* h, int grid, int dir, int csx, int c
 
 extern "C" int hosnwt_advance_many(hosnwt_ctx* const* ctxs, int n, const double* time_next, double* h_rk) {
   if (!ctxs || n <= 0 || !time_next || !h_rk) return HOSNWT_ERR_ARG;
-  // independent tanks, each with its own stream and step control
+  // Independent tanks, each on its own stream with its own step graph and
+  // the step control of HOS-NWT.f90:498-571.  Each tank is relaunched as
+  // soon as its own step has finished (polled with an event), so tanks of
+  // different sizes overlap on the GPU without waiting for each other.
+  std::vector<double> h_loc(n, 0.0);
+  std::vector<char> inflight(n, 0);
+  std::vector<cudaEvent_t> done(n, nullptr);
+  int rc = HOSNWT_OK;
   for (int i = 0; i < n; ++i) {
-    int rc = hosnwt_advance(ctxs[i], time_next[i], &h_rk[i], nullptr, nullptr);
-    if (rc) return rc;
+    if (!ctxs[i] || !ctxs[i]->c.step_graph) return HOSNWT_ERR_ARG;
+    cudaEventCreateWithFlags(&done[i], cudaEventDisableTiming);
   }
-  return HOSNWT_OK;
+  auto launch = [&](int i) -> int {
+    Ctx& c = ctxs[i]->c;
+    h_loc[i] = h_rk[i];
+    if (time_next[i] - c.time_cur < h_rk[i]) h_loc[i] = time_next[i] - c.time_cur;
+    c.d.host_sc[SC_T0] = c.time_cur;
+    c.d.host_sc[SC_H] = h_loc[i];
+    if (cudaGraphLaunch(c.step_graph, c.st) != cudaSuccess) return cuda_check(c, "graph launch");
+    cudaMemcpyAsync(c.d.host_sc + SC_ERR, c.d.sc + SC_ERR, sizeof(double), cudaMemcpyDeviceToHost, c.st);
+    cudaEventRecord(done[i], c.st);
+    inflight[i] = 1;
+    return HOSNWT_OK;
+  };
+  int running = 0;
+  for (int i = 0; i < n && rc == HOSNWT_OK; ++i)
+    if (ctxs[i]->c.time_cur < time_next[i]) {
+      rc = launch(i);
+      ++running;
+    }
+  while (running > 0 && rc == HOSNWT_OK) {
+    for (int i = 0; i < n && rc == HOSNWT_OK; ++i) {
+      if (!inflight[i]) continue;
+      const cudaError_t q = cudaEventQuery(done[i]);
+      if (q == cudaErrorNotReady) continue;
+      Ctx& c = ctxs[i]->c;
+      const Params& P = c.P;
+      inflight[i] = 0;
+      if (q != cudaSuccess) { rc = cuda_check(c, "step"); break; }
+      c.n_rhs += 5;
+      const double error = c.d.host_sc[SC_ERR];
+      if (!std::isfinite(error)) {
+        c.err = "non-finite error estimate";
+        rc = HOSNWT_ERR_NAN;
+        break;
+      }
+      double dt_correc;
+      if (error > P.toler && h_rk[i] > 0.001 * 0.95 * P.dt_stab) {
+        dt_correc = (double)0.9f * std::pow(error / P.toler, -(double)(1.0f / 4.0f));
+        if (std::fabs(P.Tramp - (c.time_cur + h_loc[i])) <= TINY && P.Tramp > c.time_cur) c.endramp = 0;
+      } else {
+        bool end_ramp = false;
+        if (P.iramp == 1 && P.Tramp - (c.time_cur + h_loc[i]) <= TINY && P.Tramp > c.time_cur &&
+            c.endramp != 1) {
+          end_ramp = true;
+          c.endramp = 1;
+        }
+        enqueue_accept(c, end_ramp, c.st);
+        c.time_cur = c.time_cur + h_loc[i];
+        dt_correc = std::fabs(error) < TINY ? 2.0 : 0.9 * std::pow(error / P.toler, -(1.0 / 4.0));
+      }
+      double hr = h_rk[i] * dt_correc;
+      hr = std::min(std::min(hr, 0.95 * P.dt_stab), P.delt_out);
+      hr = std::max(std::max(hr, 0.0001 * 0.95 * P.dt_stab), 0.0001 * P.delt_out);
+      h_rk[i] = hr;
+      if (c.time_cur < time_next[i]) rc = launch(i);
+      else --running;
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    Ctx& c = ctxs[i]->c;
+    cudaStreamSynchronize(c.st);
+    if (done[i]) cudaEventDestroy(done[i]);
+    if (rc == HOSNWT_OK) rc = cuda_check(c, "advance_many");
+  }
+  return rc;
 }
 
 extern "C" int hosnwt_time_transform(hosnwt_ctx* h, int grid, int dir, int csx, int csy, int nin1,

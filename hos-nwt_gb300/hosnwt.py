@@ -156,6 +156,20 @@ def transform_noalloc(direction, cs, n, nlines, in_ptr, out_ptr, stream=0):
         raise HosError(f"hosnwt_transform_noalloc failed ({ERRORS.get(rc, rc)})")
 
 
+def advance_many(tanks, time_next, h_rk):
+    """Advance independent tanks together (hosnwt_advance_many): each tank
+    keeps its own adaptive step; their launches overlap on the GPU.
+    time_next, h_rk: sequences (nondimensional); returns the new h_rk."""
+    n = len(tanks)
+    arr = (ctypes.c_void_p * n)(*[t._h.value for t in tanks])
+    tn = np.ascontiguousarray(np.asarray(time_next, dtype=np.float64))
+    hr = np.ascontiguousarray(np.asarray(h_rk, dtype=np.float64)).copy()
+    rc = load_library().hosnwt_advance_many(arr, n, _dptr(tn), _dptr(hr))
+    if rc != HOSNWT_OK:
+        raise HosError(f"hosnwt_advance_many failed ({ERRORS.get(rc, rc)})")
+    return hr
+
+
 GRID = {"n": 0, "big": 1, "add": 2}
 CS = {"cos": 0, "sin": 1}
 

@@ -108,3 +108,22 @@ def directional_3d(directory, seed=2025, n1=513, n2=257, n3=33, mHOS=5, p1=4, p2
     probes = [(5.0, 15.0), (10.0, 15.0), (20.0, 15.0), (20.0, 7.5), (30.0, 15.0)]
     return dict(inp=inp, n1=n1, n2=n2, n3=n3, mHOS=mHOS, p1=p1, p2=p2, probes=probes, wave_dir=directory,
                 Hs=0.08, name="directional_3d")
+
+
+def ensemble(n_tanks=64, seed=7, T_stop=60.0, n3=33):
+    """64 independent 2-D JONSWAP tanks of uneven size and order: n1 from
+    {129, 257, 513, 1025, 2049}, M from {3, 5, 7} with p1 = M, Hs from
+    U[0.04, 0.12] m, Tp from U[1.0, 2.0] s, gamma = 3.3, phases from the
+    reference's SRAND/RAND with seed 1000 + k; all draws from PCG64(seed)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for k in range(n_tanks):
+        n1 = int(rng.choice([129, 257, 513, 1025, 2049]))
+        M = int(rng.choice([3, 5, 7]))
+        Hs = float(rng.uniform(0.04, 0.12))
+        Tp = float(rng.uniform(1.0, 2.0))
+        inp = base_input(icase=4, Hs=Hs, Tp=Tp, gamma=3.3, iseed=1000 + k, T_stop=T_stop, toler=1e-7,
+                         f_out=10.0)
+        out.append(dict(inp=inp, n1=n1, n2=1, n3=n3, mHOS=M, p1=M, p2=1, probes=[(10.0, 0.0)],
+                        wave_dir=".", Hs=Hs, name=f"tank{k}"))
+    return out
