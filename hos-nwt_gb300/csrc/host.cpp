@@ -662,7 +662,7 @@ int alloc_device(Ctx& c) {
   d.ynew = dalloc<double>(c, S);
   for (double** p : {&d.eta, &d.phis, &d.deta, &d.eta_c, &d.phis_c, &d.deta_c, &d.etam, &d.phim,
                      &d.eta_sp, &d.w_eta_x, &d.w_eta_y, &d.w_phi_x, &d.w_phi_y, &d.phix_add,
-                     &d.phiy_add, &d.phiz_add, &d.phit_add, &d.phit_add1, &d.phiz_add1, &d.a1k,
+                     &d.phiy_add, &d.phiz_add, &d.phit_add, &d.phi_add, &d.phit_add1, &d.phiz_add1, &d.a1k,
                      &d.phiz1st, &d.rhs1, &d.X1, &d.X2, &d.X3, &d.det, &d.dph, &d.NL1, &d.NL2,
                      &d.pmode[0], &d.pmode[1], &d.pmode[2]})
     *p = dalloc<double>(c, nN);
@@ -680,11 +680,12 @@ int alloc_device(Ctx& c) {
                      &d.geta2phiz, &d.geta2phiz2})
     *p = dalloc<double>(c, std::max(nB, nN));
   for (int g = 0; g < 24; ++g) d.grp[g] = dalloc<double>(c, std::max(nB, nN));
+  d.diag = dalloc<double>(c, 8);
   d.bc1 = dalloc<double>(c, nA);
   d.bcr = dalloc<double>(c, nA);
   if (P.n2 != 1) {
     const size_t nQ = (size_t)P.n1 * P.n3a * P.n2;
-    for (int q = 0; q < 4; ++q) { d.Q[q] = dalloc<double>(c, nQ); d.B[q] = dalloc<double>(c, nQ); }
+    for (int q = 0; q < 5; ++q) { d.Q[q] = dalloc<double>(c, nQ); d.B[q] = dalloc<double>(c, nQ); }
   }
   const size_t ntmp = (size_t)std::max(std::max(P.nd1, P.n3a), P.n1) * std::max(P.nd2, P.n2);
   for (int i = 0; i < kMaxJobs; ++i) d.xtmp[i] = dalloc<double>(c, ntmp);
@@ -951,38 +952,215 @@ extern "C" int hosnwt_probes(hosnwt_ctx* h, double* out) {
   return cuda_check(c, "probes");
 }
 
+// ---------------------------------------------------------------------------
+// output files (output.f90:37-229, 232-482) and diagnostics
+// ---------------------------------------------------------------------------
+// Fortran Ew.d / Dw.d: 0.ddddd x 10^e, right-justified in w
+static std::string fortran_E(double v, int w, int d, char letter) {
+  char buf[64];
+  std::string body;
+  if (v == 0.0 || !std::isfinite(v)) {
+    body = "0." + std::string(d, '0') + letter + "+00";
+    if (!std::isfinite(v)) body = std::string(w, '*');
+  } else {
+    std::snprintf(buf, sizeof buf, "%.*E", d - 1, std::fabs(v));
+    std::string t(buf);  // x.xxxxE+yy
+    const size_t ep = t.find('E');
+    std::string digits = t.substr(0, 1) + t.substr(2, ep - 2);
+    int e = std::atoi(t.c_str() + ep + 1) + 1;
+    std::snprintf(buf, sizeof buf, "%c%02d", e < 0 ? '-' : '+', std::abs(e));
+    body = std::string(v < 0 ? "-" : "") + "0." + digits + letter + buf;
+  }
+  if ((int)body.size() < w) body = std::string(w - body.size(), ' ') + body;
+  return body;
+}
+
+static std::string fortran_ES(double v, int w, int d) {
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%*.*E", w, d, v);
+  return buf;
+}
+
+static std::string rjust(const std::string& s, size_t w) {
+  if (s.size() >= w) return s.substr(0, w);
+  return std::string(w - s.size(), ' ') + s;
+}
+
+// write_input (input.f90:318-395): the input echo at the top of each result file
+static void write_input(FILE* f, const Ctx& c) {
+  const hosnwt_input& in = c.in;
+  auto blank = [&](const char* t) { std::fprintf(f, "#%s\n", t); };
+  auto R = [&](double v, const char* var, const char* txt) {
+    std::fprintf(f, "#%s:: %s:: %s\n", rjust(txt, 33).c_str(), rjust(var, 13).c_str(), fortran_ES(v, 25, 16).c_str());
+  };
+  auto I = [&](int v, const char* var, const char* txt) {
+    std::fprintf(f, "#%s:: %s:: %5d\n", rjust(txt, 33).c_str(), rjust(var, 13).c_str(), v);
+  };
+  auto A = [&](const char* v, const char* var, const char* txt) {
+    std::fprintf(f, "#%s:: %s:: %s\n", rjust(txt, 33).c_str(), rjust(var, 13).c_str(), v);
+  };
+  blank("----------------------- Tank dimensions -----------------------");
+  R(in.xlen, "xlen", "Length(m) of the wavetank");
+  R(in.ylen, "ylen", "Beam(m) of the wavetank");
+  R(in.h, "h", "Depth(m) of the wavetank");
+  blank("------------------------ Select case --------------------------");
+  I(in.icase, "icase", "Choice of computed case");
+  blank("------------------ Sloshing case (icase = 1) ------------------");
+  I(in.islosh + 1, "islosh", "Number of the natural mode");
+  R(in.aslosh, "aslosh", "Amplitude (m) of the mode");
+  blank("--------------- Monochromatic case (icase = 2) ----------------");
+  R(in.amp_mono, "amp_mono", "Amplitude (m) of wave train");
+  R(in.nu_mono, "nu_mono", "Frequency (Hz) of wave train");
+  R(c.P.theta_mono, "theta_mono", "Angle (deg) from x-axis");
+  R(in.ph_mono, "ph_mono", "Phasis (rad) of wave train");
+  I(in.ibat, "ibat", "Directional wmk type");
+  R(in.xd_mono, "xd_mono", "Wave target distance (ibat=3)");
+  blank("-------------------- File case (icase = 3) --------------------");
+  A(in.file_name, "file_name", "Name of frequency file");
+  I(in.i_cut, "i_cut", "Frequency cut-off");
+  R(in.nuc_low, "nuc_low", "Low cut_off frequency (Hz)");
+  R(in.nuc_high, "nuc_high", "High cut_off frequency (Hz) ");
+  blank("------------------ Irregular wave (icase=4) -------------------");
+  R(in.Hs, "Hs", "Significant wave height (m)");
+  R(in.Tp, "Tp", "Peak period (s)");
+  R(in.gamma, "gamma", "Shape factor (Jonswap)");
+  I(in.iseed, "iseed", "Seed number for random numb. ");
+  blank("-------------------- Wavemaker definition ---------------------");
+  I(in.i_wmk, "i_wmk", "Nonlinear order of wavemaker");
+  I(in.igeom, "igeom", "Type (1: piston, 2: hinged)");
+  R(in.d_hinge, "d_hinge", "Rotation axis distance");
+  I(in.iramp, "iramp", "Time ramp");
+  R(in.iramp == 0 ? 0.0 : in.Tramp, "Tramp", "Time ramp duration");
+  blank("----------------------- Numerical beach -----------------------");
+  I(in.iabsnb, "iabsnb", "Absorption numerical beach");
+  R(in.xabsf, "xabsf", "Beginning front num. beach");
+  R(in.coeffabsf, "coeffabsf", "Absorption strength front");
+  blank("------------- Elevation/Velocity-Pressure probes --------------");
+  I(in.iprobes, "iprobes", "Use of probes");
+  A(in.pro_file, "pro_file", "Filename of probe positions");
+  blank("---------------------- Time-integration -----------------------");
+  R(in.T_stop, "T_stop", "Duration of the simulation");
+  R(in.toler, "toler", "Time tolerance: RK 4(5)");
+  R(in.f_out, "f_out", "Output frequency");
+  blank("--------------------------- Output ----------------------------");
+  I(in.idim, "idim", "Output: 1-dim. ; 0-nondim.");
+  I(in.i3d, "i3d", "Free surface plot");
+  I(in.imodes, "imodes", "Modes plot");
+  I(in.iwmk, "iwmk", "Wavemaker motion plot");
+  I(in.i_sw, "i_sw", "Swense output 1='yes',0='no'");
+  blank("--------------------- Numerical parameters ---------------------");
+  I(c.P.n1, "n1", "Number of nodes/modes in x");
+  I(c.P.n2, "n2", "Number of nodes/modes in y");
+  I(c.P.n3, "n3", "Number of nodes/modes on wmk");
+  I(c.P.M, "mHOS", "HOS order");
+  I(c.P.p1, "p1", "Dealiasing in x-direction");
+  I(c.P.p2, "p2", "Dealiasing in y-direction");
+  R(1.0, "coeffilt(1)", "Filtering ratio in x-modes");
+  R(1.0, "coeffilt(2)", "Filtering ratio in y-modes");
+  R(1.0, "coeffilt(3)", "Filtering ratio in z-modes");
+}
+
+// volume, energies and slopes of the current state (vol_energy.f90:36-119)
+static int diagnostics(Ctx& c, double out[5]) {
+  enqueue_diagnostics(c, c.d.diag, c.st);
+  double raw[5];
+  cudaMemcpyAsync(raw, c.d.diag, 5 * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) return cuda_check(c, "diagnostics");
+  const Params& P = c.P;
+  double vol = raw[0] * P.delx / P.xlen, ep = raw[1] * P.delx / 2.0, ek = raw[2] * P.delx / 2.0;
+  if (P.n2 != 1) {
+    vol = vol / P.ylen * P.dely;
+    ep *= P.dely;
+    ek *= P.dely;
+  }
+  out[0] = vol;
+  out[1] = ep;
+  out[2] = ek;
+  out[3] = raw[3];
+  out[4] = raw[4];
+  return HOSNWT_OK;
+}
+
+// check_slope (initial_condition.f90:687-716): filter eta and phis when the
+// slope of the last right-hand side exceeds 8
+static int check_slope(Ctx& c, int* filtered) {
+  double dg[5];
+  int rc = diagnostics(c, dg);
+  if (rc) return rc;
+  int f = 0;
+  if (dg[3] > 8.0) { enqueue_slope_filter(c, 0, c.st); f |= 1; }
+  if (dg[4] > 8.0 && c.P.n2 != 1) { enqueue_slope_filter(c, 1, c.st); f |= 2; }
+  if (filtered) *filtered = f;
+  cudaStreamSynchronize(c.st);
+  return cuda_check(c, "check_slope");
+}
+
+extern "C" int hosnwt_diagnostics(hosnwt_ctx* h, double* out5) {
+  if (!h || !out5) return HOSNWT_ERR_ARG;
+  return diagnostics(h->c, out5);
+}
+
+extern "C" int hosnwt_check_slope(hosnwt_ctx* h, int* filtered) {
+  if (!h) return HOSNWT_ERR_ARG;
+  return check_slope(h->c, filtered);
+}
+
 extern "C" int hosnwt_run(hosnwt_ctx* h, const char* results_dir) {
   if (!h) return HOSNWT_ERR_ARG;
   Ctx& c = h->c;
   const Params& P = c.P;
+  const bool dimensional = c.in.idim == 1;
+  const double t_adim = dimensional ? P.Tscale : 1.0, x_adim = dimensional ? P.h : 1.0;
   FILE* fp = nullptr;
+  FILE* fv = nullptr;
   if (results_dir) {
     std::string path = std::string(results_dir) + "/probes.dat";
-    fp = std::fopen(path.c_str(), "w");
-    if (!fp) return fail(c, HOSNWT_ERR_IO, "cannot open %s", path.c_str());
-    // output.f90:144-151 (idim = 1 header)
-    std::fprintf(fp, "TITLE=\"Probes elevation records versus time\"\n");
-    std::fprintf(fp, "VARIABLES = \"time\" ");
-    for (int p = 0; p < c.nprobes; ++p) std::fprintf(fp, "\"p%d\" ", p + 1);
-    std::fprintf(fp, "\n");
+    if (c.nprobes > 0) {
+      fp = std::fopen(path.c_str(), "w");
+      if (!fp) return fail(c, HOSNWT_ERR_IO, "cannot open %s", path.c_str());
+      write_input(fp, c);
+      std::fprintf(fp, "TITLE=\"Probes elevation records versus time\"\n");
+      std::fprintf(fp, dimensional ? "VARIABLES = \"time\" " : "VARIABLES = \"time*sqrt(g/h)\" ");
+      for (int p = 0; p < c.nprobes; ++p) std::fprintf(fp, dimensional ? "\"p%d\" " : "\"p%d/h\" ", p + 1);
+      std::fprintf(fp, "\n");
+    }
+    path = std::string(results_dir) + "/vol_energy.dat";
+    fv = std::fopen(path.c_str(), "w");
+    if (!fv) {
+      if (fp) std::fclose(fp);
+      return fail(c, HOSNWT_ERR_IO, "cannot open %s", path.c_str());
+    }
+    write_input(fv, c);
+    std::fprintf(fv, "TITLE=\" volume and energy evolution \"\n");
+    std::fprintf(fv, dimensional ? "VARIABLES=\"time\", \"voltot\", \"enepot\", \"enekin\", \"enetot\"\n"
+                                 : "VARIABLES=\"time*sqrt(g/h)\", \"voltot\", \"enepot\", \"enekin\", \"enetot\"\n");
   }
   std::vector<double> pv(std::max(c.nprobes, 1));
   double delt = P.delt;
   int rc = HOSNWT_OK;
   while (c.time_cur < P.T_stop + P.delt_out) {
+    if (fv) {
+      // output_time_step (output.f90:232-282)
+      double dg[5];
+      rc = diagnostics(c, dg);
+      if (rc) break;
+      double sc[SC_COUNT];
+      cudaMemcpy(sc, c.d.sc, sizeof sc, cudaMemcpyDeviceToHost);
+      double eta11 = 0.0;
+      cudaMemcpy(&eta11, c.d.eta, sizeof(double), cudaMemcpyDeviceToHost);
+      double vol = dg[0];
+      const double a = sc[SC_ALPHA], pt = sc[SC_POSTOP];
+      if (P.igeom == 2) vol = vol - 0.5 * a * (1 - P.d_hinge) * pt / P.xlen - eta11 * a * pt / P.xlen;
+      else if (P.igeom == 1) vol = vol - a * pt / P.xlen - eta11 * a * pt / P.xlen;
+      std::fprintf(fv, "%s %s %s %s %s \n", fortran_ES(c.time_cur * t_adim, 12, 5).c_str(),
+                   fortran_ES(vol, 12, 5).c_str(), fortran_ES(dg[1], 12, 5).c_str(),
+                   fortran_ES(dg[2], 12, 5).c_str(), fortran_ES(dg[1] + dg[2], 12, 5).c_str());
+    }
     if (fp) {
       rc = hosnwt_probes(h, pv.data());
       if (rc) break;
-      // format 61d13.5 (output.f90:281): Fortran D exponent
-      char buf[64];
-      auto dfmt = [&](double v) {
-        std::snprintf(buf, sizeof buf, "%13.5E", v);
-        for (char* q = buf; *q; ++q)
-          if (*q == 'E') *q = 'D';
-        return std::string(buf);
-      };
-      std::string line = dfmt(c.time_cur * P.Tscale);
-      for (int p = 0; p < c.nprobes; ++p) line += dfmt(pv[p] * P.h);
+      std::string line = fortran_E(c.time_cur * t_adim, 13, 5, 'D');
+      for (int p = 0; p < c.nprobes; ++p) line += fortran_E(pv[p] * x_adim, 13, 5, 'D');
       std::fprintf(fp, "%s\n", line.c_str());
     }
     if (std::fabs(c.time_cur - P.T_stop) <= TINY) break;
@@ -992,8 +1170,11 @@ extern "C" int hosnwt_run(hosnwt_ctx* h, const char* results_dir) {
     rc = advance(c, time_next, &h_rk, nullptr, nullptr);
     if (rc) break;
     delt = h_rk;
+    rc = check_slope(c, nullptr);
+    if (rc) break;
   }
   if (fp) std::fclose(fp);
+  if (fv) std::fclose(fv);
   return rc;
 }
 

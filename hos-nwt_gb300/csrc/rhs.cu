@@ -542,9 +542,9 @@ __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
     const double* __restrict__ eta, const double* __restrict__ a1, const double* __restrict__ a2,
     const double* __restrict__ a3, const double* __restrict__ da, const double* __restrict__ kx_add,
     const double* __restrict__ csh, const double* __restrict__ ksh, const double* __restrict__ kxcsh,
-    int n1, int n3a, double* phix, double* phiy, double* phiz, double* phit) {
+    int n1, int n3a, double* phix, double* phiy, double* phiz, double* phit, double* phi) {
   __shared__ double sa[512], sd[512];
-  __shared__ double r[3][kCy][kCx];
+  __shared__ double r[4][kCy][kCx];
   const int tx = threadIdx.x % kCx, ty = threadIdx.x / kCx;
   const int i1 = blockIdx.x * kCx + tx;
   for (int t = threadIdx.x; t < n3a; t += blockDim.x) {
@@ -553,7 +553,7 @@ __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
   }
   __syncthreads();
   const int ch = (n3a + kCy - 1) / kCy;
-  double st = 0.0, sx = 0.0, sz = 0.0;
+  double st = 0.0, sx = 0.0, sz = 0.0, sp = 0.0;
   if (i1 < n1) {
     const double e1 = eta[i1] + 1.0;
     const int i3a = ty * ch, i3b = min(n3a, (ty + 1) * ch);
@@ -564,6 +564,7 @@ __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
       for (int i3 = i3a; i3 < i3b; ++i3) {
         const long long o = i1 + (long long)n1 * i3;
         st = fma(sd[i3] * c, csh[o], st);
+        sp = fma(sa[i3] * c, csh[o], sp);
         sx = fma(-sa[i3] * c, ksh[o], sx);
         sz = fma(-sa[i3] * s, kxcsh[o], sz);
         const double cn = c * c2 - s * s2;
@@ -575,14 +576,16 @@ __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
   r[0][ty][tx] = st;
   r[1][ty][tx] = sx;
   r[2][ty][tx] = sz;
+  r[3][ty][tx] = sp;
   __syncthreads();
   if (ty == 0 && i1 < n1) {
-    double t = 0.0, x = 0.0, z = 0.0;
-    for (int q = 0; q < kCy; ++q) { t += r[0][q][tx]; x += r[1][q][tx]; z += r[2][q][tx]; }
+    double t = 0.0, x = 0.0, z = 0.0, f = 0.0;
+    for (int q = 0; q < kCy; ++q) { t += r[0][q][tx]; x += r[1][q][tx]; z += r[2][q][tx]; f += r[3][q][tx]; }
     phix[i1] = x;
     phiy[i1] = 0.0;
     phiz[i1] = z;
     phit[i1] = t;
+    phi[i1] = f;
   }
 }
 
@@ -591,7 +594,8 @@ __global__ void k_phiadd_q(const double* __restrict__ a1, const double* __restri
                            const double* __restrict__ a3, const double* __restrict__ da,
                            const double* __restrict__ csh, const double* __restrict__ ksh,
                            const double* __restrict__ kycsh, const double* __restrict__ kxcsh,
-                           int n1, int n2, int n3a, double* Qt, double* Qx, double* Qy, double* Qz) {
+                           int n1, int n2, int n3a, double* Qt, double* Qx, double* Qy, double* Qz,
+                           double* Qp) {
   const long long n = (long long)n1 * n3a * n2;
   const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (o >= n) return;
@@ -601,19 +605,20 @@ __global__ void k_phiadd_q(const double* __restrict__ a1, const double* __restri
   Qx[o] = a * ksh[o];
   Qy[o] = a * kycsh[o];
   Qz[o] = a * kxcsh[o];
+  Qp[o] = a * csh[o];
 }
 
 // phiadd_SL (3-D): contraction over i3 at z = eta of the y-transformed B_q
 __global__ void k_phiadd_contract(const double* __restrict__ eta, const double* __restrict__ kx_add,
                                   const double* __restrict__ Bt, const double* __restrict__ Bx,
                                   const double* __restrict__ By, const double* __restrict__ Bz,
-                                  int n1, int n2, int n3a, double* phix, double* phiy, double* phiz,
-                                  double* phit) {
+                                  const double* __restrict__ Bp, int n1, int n2, int n3a,
+                                  double* phix, double* phiy, double* phiz, double* phit, double* phi) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= (long long)n1 * n2) return;
   const int i1 = (int)(i % n1), i2 = (int)(i / n1);
   const double e1 = eta[i] + 1.0;
-  double st = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+  double st = 0.0, sx = 0.0, sy = 0.0, sz = 0.0, sp = 0.0;
   for (int i3 = 0; i3 < n3a; ++i3) {
     double s, c;
     sincos(kx_add[i3] * e1, &s, &c);
@@ -622,11 +627,13 @@ __global__ void k_phiadd_contract(const double* __restrict__ eta, const double* 
     sx -= c * Bx[o];
     sy -= c * By[o];
     sz -= s * Bz[o];
+    sp += c * Bp[o];
   }
   phix[i] = sx;
   phiy[i] = sy;
   phiz[i] = sz;
   phit[i] = st;
+  phi[i] = sp;
 }
 
 // ---------------------------------------------------------------------------
@@ -776,6 +783,50 @@ __global__ void k_probe_dot(const double* __restrict__ modes, const double* __re
   for (long long i = threadIdx.x; i < n; i += blockDim.x) s += modes[i] * mat[n * p + i];
   s = block_reduce<0>(s);
   if (threadIdx.x == 0) out[p] = s;
+}
+
+// Diagnostics of one output time (single block, fixed order):
+// out[0] = trapezoid sum of eta, out[1] of eta^2, out[2] of (phis + phi_add) deta
+// (vol_energy.f90:36-119 before the mesh factors); out[3], out[4] = max |eta_x|,
+// max |eta_y| on the dealiased grid (check_slope, initial_condition.f90:687-716).
+__global__ void k_diagnostics(const double* __restrict__ eta, const double* __restrict__ phis,
+                              const double* __restrict__ phi_add, const double* __restrict__ deta,
+                              const double* __restrict__ etax, const double* __restrict__ etay, int n1,
+                              int n2, long long nB, double* out) {
+  double v = 0.0, ep = 0.0, ek = 0.0, mx = 0.0, my = 0.0;
+  const long long n = (long long)n1 * n2;
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+    const int i1 = (int)(i % n1), i2 = (int)(i / n1);
+    double w = (i1 == 0 || i1 == n1 - 1) ? 0.5 : 1.0;
+    if (n2 != 1) w *= (i2 == 0 || i2 == n2 - 1) ? 0.5 : 1.0;
+    const double e = eta[i];
+    v += w * e;
+    ep += w * (e * e);
+    ek += w * ((phis[i] + phi_add[i]) * deta[i]);
+  }
+  for (long long i = threadIdx.x; i < nB; i += blockDim.x) {
+    mx = fmax(mx, fabs(etax[i]));
+    my = fmax(my, fabs(etay[i]));
+  }
+  v = block_reduce<0>(v);
+  if (threadIdx.x == 0) out[0] = v;
+  ep = block_reduce<0>(ep);
+  if (threadIdx.x == 0) out[1] = ep;
+  ek = block_reduce<0>(ek);
+  if (threadIdx.x == 0) out[2] = ek;
+  mx = block_reduce<1>(mx);
+  if (threadIdx.x == 0) out[3] = mx;
+  my = block_reduce<1>(my);
+  if (threadIdx.x == 0) out[4] = my;
+}
+
+// zero the modes beyond nf along x (dir 0) or y (dir 1): the cut filter of
+// filtering_base (filtering.f90:334-360)
+__global__ void k_cut_modes(double* m, int n1, int n2, int nf, int dir) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)n1 * n2) return;
+  const int i1 = (int)(i % n1), i2 = (int)(i / n1);
+  if ((dir == 0 && i1 >= nf) || (dir == 1 && i2 >= nf)) m[i] = 0.0;
 }
 
 }  // namespace
@@ -1063,20 +1114,22 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     if (n2 == 1) {
       k_phiadd_sl_1d<<<(n1 + kCx - 1) / kCx, kCx * kCy, 0, st>>>(d.eta_sp, aA1, aA2, aA3, kA1, d.kx_add, d.csh,
                                                      d.ksh, d.kxcsh, n1, P.n3a, d.phix_add,
-                                                     d.phiy_add, d.phiz_add, d.phit_add);
+                                                     d.phiy_add, d.phiz_add, d.phit_add, d.phi_add);
     } else {
       const long long nq = (long long)n1 * P.n3a * n2;
       E.ew(k_phiadd_q, nq, aA1, aA2, aA3, (const double*)kA1, (const double*)d.csh,
            (const double*)d.ksh, (const double*)d.kycsh, (const double*)d.kxcsh, n1, n2, P.n3a,
-           d.Q[0], d.Q[1], d.Q[2], d.Q[3]);
+           d.Q[0], d.Q[1], d.Q[2], d.Q[3], d.Q[4]);
       const int lines = n1 * P.n3a;
       launch_y_f2s(c.tb, d.Q[0], lines, lines, d.B[0], lines, 0, st);
       launch_y_f2s(c.tb, d.Q[1], lines, lines, d.B[1], lines, 0, st);
       launch_y_f2s(c.tb, d.Q[2], lines, lines, d.B[2], lines, 1, st);
       launch_y_f2s(c.tb, d.Q[3], lines, lines, d.B[3], lines, 0, st);
+      launch_y_f2s(c.tb, d.Q[4], lines, lines, d.B[4], lines, 0, st);
       E.ew(k_phiadd_contract, nN, (const double*)d.eta_sp, (const double*)d.kx_add,
            (const double*)d.B[0], (const double*)d.B[1], (const double*)d.B[2],
-           (const double*)d.B[3], n1, n2, P.n3a, d.phix_add, d.phiy_add, d.phiz_add, d.phit_add);
+           (const double*)d.B[3], (const double*)d.B[4], n1, n2, P.n3a, d.phix_add, d.phiy_add,
+           d.phiz_add, d.phit_add, d.phi_add);
     }
   } else {
     cudaMemsetAsync(kA1, 0, sizeof(double) * nA, st);
@@ -1087,6 +1140,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     cudaMemsetAsync(d.phiy_add, 0, sizeof(double) * nN, st);
     cudaMemsetAsync(d.phiz_add, 0, sizeof(double) * nN, st);
     cudaMemsetAsync(d.phit_add, 0, sizeof(double) * nN, st);
+    cudaMemsetAsync(d.phi_add, 0, sizeof(double) * nN, st);
   }
   // second- and third-order wavemaker slopes stay zero (i_wmk = 1)
   cudaMemsetAsync(k + L.off[S_AADD2], 0, sizeof(double) * nA, st);
@@ -1218,6 +1272,24 @@ void enqueue_initialize(Ctx& c, cudaStream_t st) {
   E.xf({E.R(GRID_ADD, 1, 0, 0, d.bc1, P.n3a, P.n3a, P.n2, a1, P.n3a, P.n3a, P.n2)});
   E.ew(k_div, nA, a1, (double*)nullptr, (const double*)d.k_add_thk, nA);
   cudaMemcpyAsync(d.y0 + L.off[S_AADDR], a1, sizeof(double) * nA, cudaMemcpyDeviceToDevice, st);
+}
+
+void enqueue_diagnostics(Ctx& c, double* out, cudaStream_t st) {
+  const Params& P = c.P;
+  k_diagnostics<<<1, 1024, 0, st>>>(c.d.eta, c.d.phis, c.d.phi_add, c.d.deta, c.d.etax, c.d.etay, P.n1, P.n2,
+                                     (long long)P.nd1 * P.nd2, out);
+}
+
+// filtering_x / filtering_y with coeff_cut = 0.7 of phis and eta (check_slope)
+void enqueue_slope_filter(Ctx& c, int dir, cudaStream_t st) {
+  Enq E(c, st);
+  const Params& P = c.P;
+  const int nf = dir == 0 ? std::abs((int)(P.n1 * 0.7)) : std::abs((int)(P.n2 * 0.7));
+  for (double* f : {c.d.phis, c.d.eta}) {
+    E.xf({E.S2F_N(f, c.d.NL1)});
+    k_cut_modes<<<nblk(E.nN()), kEW, 0, st>>>(c.d.NL1, P.n1, P.n2, nf, dir);
+    E.xf({E.F2S_N(c.d.NL1, f)});
+  }
 }
 
 void enqueue_probes(Ctx& c, cudaStream_t st) {

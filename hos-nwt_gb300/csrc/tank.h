@@ -66,6 +66,7 @@ struct Dev {
   double *etam = nullptr, *phim = nullptr, *eta_sp = nullptr;
   double *w_eta_x = nullptr, *w_eta_y = nullptr, *w_phi_x = nullptr, *w_phi_y = nullptr;
   double *phix_add = nullptr, *phiy_add = nullptr, *phiz_add = nullptr, *phit_add = nullptr;
+  double *phi_add = nullptr, *diag = nullptr;
   double *phit_add1 = nullptr, *phiz_add1 = nullptr, *a1k = nullptr, *phiz1st = nullptr, *rhs1 = nullptr;
   double *pmode[3] = {};        // S2F of phix/phiy/phiz_add
   double *X1 = nullptr, *X2 = nullptr, *X3 = nullptr, *det = nullptr, *dph = nullptr;
@@ -129,6 +130,8 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
 void enqueue_step(Ctx& c, cudaStream_t st);
 void enqueue_initialize(Ctx& c, cudaStream_t st);
 void enqueue_probes(Ctx& c, cudaStream_t st);
+void enqueue_diagnostics(Ctx& c, double* out, cudaStream_t st);
+void enqueue_slope_filter(Ctx& c, int dir, cudaStream_t st);
 void enqueue_accept(Ctx& c, bool end_ramp, cudaStream_t st);
 void enqueue_set_scalar(Ctx& c, int slot, double v, cudaStream_t st);
 

@@ -27,7 +27,7 @@ C_FUNCTIONS = ("hosnwt_read_input", "hosnwt_create", "hosnwt_destroy", "hosnwt_l
                "hosnwt_advance", "hosnwt_run", "hosnwt_get_state", "hosnwt_set_state",
                "hosnwt_probes", "hosnwt_solveHOS2", "hosnwt_transform", "hosnwt_advance_many",
                "hosnwt_time_transform", "hosnwt_fp64_peak", "hosnwt_get_rk_state",
-               "hosnwt_transform_noalloc")
+               "hosnwt_transform_noalloc", "hosnwt_diagnostics", "hosnwt_check_slope")
 
 
 class HosInput(ctypes.Structure):
@@ -98,6 +98,8 @@ def load_library(path=LIB_PATH):
     lib.hosnwt_time_transform.argtypes = [vp] + [ctypes.c_int] * 10 + [dp]
     lib.hosnwt_fp64_peak.argtypes = [dp]
     lib.hosnwt_get_rk_state.argtypes = [vp] + [dp] * 10
+    lib.hosnwt_diagnostics.argtypes = [vp, dp]
+    lib.hosnwt_check_slope.argtypes = [vp, P(ctypes.c_int)]
     lib.hosnwt_transform_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     _lib = lib
@@ -316,6 +318,17 @@ class Tank:
         p = np.array(phis, dtype=np.float64, order="F", copy=True)
         self._check(self.lib.hosnwt_set_state(self._h, _dptr(e), _dptr(p)), "set_state")
 
+    def diagnostics(self):
+        """(volume, potential energy, kinetic energy, max|eta_x|, max|eta_y|)."""
+        out = np.zeros(5)
+        self._check(self.lib.hosnwt_diagnostics(self._h, _dptr(out)), "diagnostics")
+        return out
+
+    def check_slope(self):
+        f = ctypes.c_int()
+        self._check(self.lib.hosnwt_check_slope(self._h, ctypes.byref(f)), "check_slope")
+        return f.value
+
     def probes(self):
         out = np.zeros(max(self.nprobes, 1))
         self._check(self.lib.hosnwt_probes(self._h, _dptr(out)), "probes")
@@ -336,4 +349,5 @@ class Tank:
                 break
             time_next = min(t + delt_out, T_stop + delt_out)
             delt, _, _ = self.advance(time_next, delt)
+            self.check_slope()
         return recs

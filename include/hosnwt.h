@@ -116,8 +116,20 @@ int hosnwt_accept(hosnwt_ctx* ctx, double h_loc);
 int hosnwt_advance(hosnwt_ctx* ctx, double time_next, double* h_rk, int* n_acc, int* n_rej);
 
 /* Whole time loop (HOS-NWT.f90:446-581) writing Results/probes.dat and
- * Results/vol_energy.dat into results_dir (NULL: no files). */
+ * Results/vol_energy.dat into results_dir (NULL: no files), in the formats of
+ * output.f90 (input echo, 61d13.5 probe records, 5(ES12.5,X) energies),
+ * with check_slope after each output interval. */
 int hosnwt_run(hosnwt_ctx* ctx, const char* results_dir);
+
+/* Diagnostics of the current state (vol_energy.f90:36-119 and
+ * check_slope's slopes): out[0] volume, out[1] potential and out[2] kinetic
+ * energy (phis + phi_add of the last right-hand side times deta), out[3] and
+ * out[4] max |eta_x| and max |eta_y| of the last right-hand side. */
+int hosnwt_diagnostics(hosnwt_ctx* ctx, double* out5);
+/* check_slope (initial_condition.f90:687-716): filter eta and phis (cut at
+ * 0.7 of the modes) in each direction whose slope exceeds 8; *filtered gets
+ * bit 0 (x) and bit 1 (y) of what was filtered. */
+int hosnwt_check_slope(hosnwt_ctx* ctx, int* filtered);
 
 /* Copy the physical state to host arrays (n1 x n2 each; NULL to skip). */
 int hosnwt_get_state(hosnwt_ctx* ctx, double* eta, double* phis, double* deta);

@@ -1283,6 +1283,22 @@ class Tank:
             v = v / self.ylen * self.dely
         return v
 
+    def energy(self):
+        """energy (vol_energy.f90:69-119) with phis + phi_add and deta."""
+        def integ(f):
+            if self.n2 == 1:
+                sy = 0.5 * (f[:, 0] + f[:, 0])
+            else:
+                sy = 0.5 * (f[:, 0] + f[:, -1]) + f[:, 1:-1].sum(axis=1)
+            v = (0.5 * (sy[0] + sy[-1]) + sy[1:-1].sum()) * self.delx
+            return v
+        ep = integ(self.eta * self.eta) / 2.0
+        ek = integ((self.phis + self.phi_add) * self.deta) / 2.0
+        if self.n2 != 1:
+            ep *= self.dely
+            ek *= self.dely
+        return ep, ek
+
     def run(self, T_end=None, on_output=None):
         """Whole time loop (HOS-NWT.f90:446-581); returns probe records."""
         T_stop = self.T_stop if T_end is None else T_end / self.Tscale
