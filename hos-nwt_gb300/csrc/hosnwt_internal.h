@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include <complex>
 #include <cstdint>
 #include <string>
@@ -11,6 +13,33 @@
 #include "hosnwt.h"
 
 namespace hos {
+
+// Programmatic dependent launch: kernels are launched with programmatic
+// stream serialization so that a kernel's launch overlaps the end of the
+// previous one; every kernel waits for its predecessor's completion and
+// memory at its start (griddepcontrol.wait is a no-op without a
+// programmatic predecessor).
+__device__ __forceinline__ void pdl_wait() {
+#if defined(__CUDA_ARCH__)
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                              cudaStream_t st, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
 
 // ---------------------------------------------------------------------------
 // Spectral transforms along one axis.

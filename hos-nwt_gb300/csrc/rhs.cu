@@ -88,6 +88,7 @@ __global__ void k_gtof(const double* __restrict__ G1, const double* __restrict__
                        const double* __restrict__ ky, double* sc_, int n1, int n2, int igeom,
                        double d_hinge, double xlen, double* etam, double* phim, double* wex,
                        double* wey, double* wpx, double* wpy, double* part, unsigned int* counter) {
+  pdl_wait();
   const double* sc = sc_;
   const double dt = sc[SC_DT];
   const long long n = (long long)n1 * n2;
@@ -120,6 +121,7 @@ __global__ void k_gtof(const double* __restrict__ G1, const double* __restrict__
 
 __global__ void k_pow(const double* __restrict__ prev, const double* __restrict__ e1, double jp1,
                       double* out, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n) out[i] = prev[i] / jp1 * e1[i];
 }
@@ -131,6 +133,7 @@ struct PowArgs {
   int j0, j1;
 };
 __global__ void k_pow_run(PowArgs a, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double e1 = a.e[0][i];
@@ -154,6 +157,7 @@ struct GroupTerms {
   int ngroup;
 };
 __global__ void k_group_products(GroupTerms g, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double acc[16];
@@ -176,6 +180,7 @@ struct SumArgs {
   double* out;
 };
 __global__ void k_sum_fields(SumArgs a, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double v = 0.0;
@@ -187,17 +192,20 @@ __global__ void k_sum_fields(SumArgs a, long long n) {
 // out = s * x * y  (s applied first, as 2.0_rp * a * b in the reference)
 __global__ void k_mul(const double* __restrict__ x, const double* __restrict__ y, double s,
                       double* out, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n) out[i] = (s * x[i]) * y[i];
 }
 
 __global__ void k_add(double* out, const double* __restrict__ x, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n) out[i] += x[i];
 }
 
 __global__ void k_sq2(const double* __restrict__ a, const double* __restrict__ b, double* out,
                       long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n) out[i] = a[i] * a[i] + b[i] * b[i];
 }
@@ -210,6 +218,7 @@ struct ProdArgs {
 };
 __global__ void k_prod_kth(const double* __restrict__ a, int a_ld, int e1, int e2,
                            const double* __restrict__ kth_ext, int nd1, int nd2, ProdArgs pa) {
+  pdl_wait();
   const long long n = (long long)e1 * e2;
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -227,6 +236,7 @@ struct AccArgs {
   int iHOS;
 };
 __global__ void k_hos_accum(AccArgs a, double* phimext, double* phizm, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   double pm = 0.0, pz = 0.0;
@@ -243,6 +253,7 @@ __global__ void k_hos_accum(AccArgs a, double* phimext, double* phizm, long long
 __global__ void k_fs_products(const double* __restrict__ etax, const double* __restrict__ etay,
                               const double* __restrict__ phisx, const double* __restrict__ phisy,
                               double* detext, double* dphext, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double px = phisx[i], py = phisy[i];
@@ -270,6 +281,7 @@ struct AssembleArgs {
   int M;
 };
 __global__ void k_assemble(AssembleArgs a, double* A1, double* A3, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double ex = a.etax[i], ey = a.etay[i], px = a.phisx[i], py = a.phisy[i];
@@ -297,6 +309,7 @@ __global__ void k_final(const double* __restrict__ X1, const double* __restrict_
                         const double* __restrict__ X3, const double* __restrict__ phiz_add,
                         const double* __restrict__ phit_add, const double* __restrict__ nu,
                         double* det, double* dph, long long n, int M) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double dphin = X1[i] + phiz_add[i];
@@ -311,6 +324,7 @@ __global__ void k_final(const double* __restrict__ X1, const double* __restrict_
 __global__ void k_expon(const double* __restrict__ NL1, const double* __restrict__ NL2,
                         const double* __restrict__ om, const double* __restrict__ sc, double* kG1,
                         double* kG2, long long n, int rk_mode) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double dt = sc[SC_DT];
@@ -393,6 +407,7 @@ __device__ void ramp_law(const RampP& r, double time, double* a, double* at, dou
 }
 
 __global__ void k_eiwt(const double* __restrict__ freq, double* sc, double* eiwt, int nf, RampP rp) {
+  pdl_wait();
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n == 0) {
     // the wavemaker law of this stage (single writer of the ramp slots)
@@ -418,6 +433,7 @@ __global__ void k_pos_bc(const double* __restrict__ pos_re, const double* __rest
                          const double* __restrict__ freq, const double* __restrict__ eiwt,
                          const double* __restrict__ gzed, double* sc, int nf, int n2,
                          int n3, int n3a, double* bc1, double* bcr, int mode) {
+  pdl_wait();
   const int i2 = blockIdx.x;
   const double a = sc[SC_ALPHA], at = sc[SC_ALPHAT], att = sc[SC_ALPHATT];
   double p0 = 0.0, p1 = 0.0, p2 = 0.0;
@@ -459,6 +475,7 @@ __global__ void k_pos_bc(const double* __restrict__ pos_re, const double* __rest
 // linear in f, df, d2f).
 __global__ void k_extend(double* a, double* b, const double* __restrict__ ext, int n2, int n3,
                          int n3a) {
+  pdl_wait();
   const int nrow = n3a - n3;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int tot = nrow * n2;
@@ -473,6 +490,7 @@ __global__ void k_extend(double* a, double* b, const double* __restrict__ ext, i
 }
 
 __global__ void k_div(double* a, double* b, const double* __restrict__ d, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   a[i] = a[i] / d[i];
@@ -488,6 +506,7 @@ __global__ void __launch_bounds__(kCx * kCy) k_sweet_contract(
     const double* __restrict__ a, const double* __restrict__ da, const double* __restrict__ cosk,
     const double* __restrict__ sink, const double* __restrict__ csh, const double* __restrict__ kxcsh,
     int n1, int n2, int n3a, double* At, double* Az) {
+  pdl_wait();
   __shared__ double sa[512], sd[512];
   __shared__ double rt[kCy][kCx], rz[kCy][kCx];
   const int j2 = blockIdx.y;
@@ -523,6 +542,7 @@ __global__ void k_sweet_rhs(const double* __restrict__ eta1st, const double* __r
                             const double* __restrict__ phiz1st_spec, const double* __restrict__ phiz1,
                             const double* __restrict__ nu, double iabsnb, double* rhs, double* keta1,
                             long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double pz = phiz1st_spec[i] + phiz1[i];
@@ -531,6 +551,7 @@ __global__ void k_sweet_rhs(const double* __restrict__ eta1st, const double* __r
 }
 
 __global__ void k_sum3(const double* a, const double* b, const double* c, double* out, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n) out[i] = a[i] + b[i] + c[i];
 }
@@ -543,6 +564,7 @@ __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
     const double* __restrict__ a3, const double* __restrict__ da, const double* __restrict__ kx_add,
     const double* __restrict__ csh, const double* __restrict__ ksh, const double* __restrict__ kxcsh,
     int n1, int n3a, double* phix, double* phiy, double* phiz, double* phit, double* phi) {
+  pdl_wait();
   __shared__ double sa[512], sd[512];
   __shared__ double r[4][kCy][kCx];
   const int tx = threadIdx.x % kCx, ty = threadIdx.x / kCx;
@@ -596,6 +618,7 @@ __global__ void k_phiadd_q(const double* __restrict__ a1, const double* __restri
                            const double* __restrict__ kycsh, const double* __restrict__ kxcsh,
                            int n1, int n2, int n3a, double* Qt, double* Qx, double* Qy, double* Qz,
                            double* Qp) {
+  pdl_wait();
   const long long n = (long long)n1 * n3a * n2;
   const long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (o >= n) return;
@@ -614,6 +637,7 @@ __global__ void k_phiadd_contract(const double* __restrict__ eta, const double* 
                                   const double* __restrict__ By, const double* __restrict__ Bz,
                                   const double* __restrict__ Bp, int n1, int n2, int n3a,
                                   double* phix, double* phiy, double* phiz, double* phit, double* phi) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= (long long)n1 * n2) return;
   const int i1 = (int)(i % n1), i2 = (int)(i / n1);
@@ -647,6 +671,7 @@ struct StageArgs {
 };
 __global__ void k_rk_stage(const double* __restrict__ y0, StageArgs sa, double* sc, double* ys,
                            long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const double h = sc[SC_H];
   if (i < n) {
@@ -668,6 +693,7 @@ struct FinalArgs {
 // max |y_new| and max |erm| per array for the error norm (runge_kutta.f90:225-279)
 __global__ void k_rk_final(const double* __restrict__ y0, FinalArgs fa, const double* __restrict__ sc,
                            double* ynew, double* part, long long n) {
+  pdl_wait();
   const double h = sc[SC_H];
   const double b[5] = {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0, 0.0};
   const double e[5] = {1.0 / 6.0, 2.0 / 3.0, 0.0, 0.0, 1.0 / 6.0};
@@ -705,6 +731,7 @@ __global__ void k_rk_final(const double* __restrict__ y0, FinalArgs fa, const do
 }
 
 __global__ void k_rk_err(const double* __restrict__ part, int nblocks, double* sc) {
+  pdl_wait();
   // one block of 32 threads: max over blocks per slot, then the norm
   __shared__ double mx[10];
   if (threadIdx.x < 10) {
@@ -728,6 +755,7 @@ __global__ void k_rk_out(const double* __restrict__ G1, const double* __restrict
                          const double* __restrict__ om, double* sc_, int n, int igeom,
                          double d_hinge, double xlen, double* etam, double* phim, double* detam,
                          double* part, unsigned int* counter) {
+  pdl_wait();
   const double* sc = sc_;
   const double h = sc[SC_H];
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -761,6 +789,7 @@ __global__ void k_rk_out(const double* __restrict__ G1, const double* __restrict
 
 // G2 = S2F(phis) * omega, phisrk0 = S2F(phis)(1,1) (runge_kutta.f90:125-141)
 __global__ void k_scale_omega(double* G2, const double* __restrict__ om, double* sc, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double g = G2[i];
@@ -768,9 +797,11 @@ __global__ void k_scale_omega(double* G2, const double* __restrict__ om, double*
   G2[i] = g * om[i];
 }
 
-__global__ void k_set_scalar(double* sc, int slot, double v) { sc[slot] = v; }
+__global__ void k_set_scalar(double* sc, int slot, double v) {
+  pdl_wait(); sc[slot] = v; }
 
 __global__ void k_sub(double* a, const double* __restrict__ b, long long n) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n) a[i] -= b[i];
 }
@@ -778,6 +809,7 @@ __global__ void k_sub(double* a, const double* __restrict__ b, long long n) {
 // probes: eta_p = sum S2F(eta) * mat_coscos (output.f90:265-282); one block per probe
 __global__ void k_probe_dot(const double* __restrict__ modes, const double* __restrict__ mat,
                             long long n, double* out) {
+  pdl_wait();
   const int p = blockIdx.x;
   double s = 0.0;
   for (long long i = threadIdx.x; i < n; i += blockDim.x) s += modes[i] * mat[n * p + i];
@@ -793,6 +825,7 @@ __global__ void k_diagnostics(const double* __restrict__ eta, const double* __re
                               const double* __restrict__ phi_add, const double* __restrict__ deta,
                               const double* __restrict__ etax, const double* __restrict__ etay, int n1,
                               int n2, long long nB, double* out) {
+  pdl_wait();
   double v = 0.0, ep = 0.0, ek = 0.0, mx = 0.0, my = 0.0;
   const long long n = (long long)n1 * n2;
   for (long long i = threadIdx.x; i < n; i += blockDim.x) {
@@ -823,6 +856,7 @@ __global__ void k_diagnostics(const double* __restrict__ eta, const double* __re
 // zero the modes beyond nf along x (dir 0) or y (dir 1): the cut filter of
 // filtering_base (filtering.f90:334-360)
 __global__ void k_cut_modes(double* m, int n1, int n2, int nf, int dir) {
+  pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= (long long)n1 * n2) return;
   const int i1 = (int)(i % n1), i2 = (int)(i / n1);
@@ -887,14 +921,14 @@ struct Enq {
   template <typename K, typename... A>
   void ew(K kern, long long n, A... a) {
     if (n <= 0) return;
-    kern<<<nblk(n), kEW, 0, st>>>(a...);
+    launch_pdl(kern, dim3(nblk(n)), dim3(kEW), 0, st, a...);
   }
 };
 
 }  // namespace
 
 void enqueue_set_scalar(Ctx& c, int slot, double v, cudaStream_t st) {
-  k_set_scalar<<<1, 1, 0, st>>>(c.d.sc, slot, v);
+  launch_pdl(k_set_scalar, dim3(1), dim3(1), 0, st, c.d.sc, slot, v);
 }
 
 static RampP ramp_params(const Params& P) {
@@ -926,7 +960,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   // 1. GtoF + volume correction of the mean mode
   {
     const int nb = nblk(nN);
-    k_gtof<<<nb, kEW, 0, st>>>(G1, G2, d.omega, d.kx, d.ky, d.sc, n1, n2, P.igeom, P.d_hinge,
+    launch_pdl(k_gtof, dim3(nb), dim3(kEW), 0, st, G1, G2, d.omega, d.kx, d.ky, d.sc, n1, n2, P.igeom, P.d_hinge,
                                P.xlen, d.etam, d.phim, d.w_eta_x, d.w_eta_y, d.w_phi_x, d.w_phi_y,
                                d.part, d.counter);
   }
@@ -936,7 +970,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     ProdArgs pa{};
     pa.count = M;
     for (int j = 1; j <= M; ++j) { pa.out[j - 1] = d.prod[j - 1]; pa.jidx[j - 1] = j - 1; }
-    k_prod_kth<<<nblk(nN), kEW, 0, st>>>(d.phim, n1, n1, n2, d.kth_ext, nd1, nd2, pa);
+    launch_pdl(k_prod_kth, dim3(nblk(nN)), dim3(kEW), 0, st, d.phim, n1, n1, n2, d.kth_ext, nd1, nd2, pa);
     std::vector<XfReq> rq;
     rq.push_back(E.F2S_N(d.etam, d.eta_sp));
     rq.push_back(E.F2S_B(d.etam, n1, n1, n2, d.etapm[0]));
@@ -993,7 +1027,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
       ProdArgs pa{};
       pa.count = M + 1 - o;
       for (int j = 1; j <= pa.count; ++j) { pa.out[j - 1] = d.prod[j - 1]; pa.jidx[j - 1] = j - 1; }
-      k_prod_kth<<<nblk((long long)e1 * e2), kEW, 0, st>>>(d.aHOS[o], nd1, e1, e2, d.kth_ext, nd1,
+      launch_pdl(k_prod_kth, dim3(nblk((long long)e1 * e2)), dim3(kEW), 0, st, d.aHOS[o], nd1, e1, e2, d.kth_ext, nd1,
                                                           nd2, pa);
       std::vector<XfReq> rq;
       for (int j = 1; j <= pa.count; ++j)
@@ -1081,19 +1115,19 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   double* kEta1 = k + L.off[S_ETA1ST];
   if (has_wavemaker(P)) {
     const RampP rp = ramp_params(P);
-    k_eiwt<<<nblk(c.nf > 0 ? c.nf : 1), kEW, 0, st>>>(d.freq_w, d.sc, d.eiwt, c.nf, rp);
-    k_pos_bc<<<n2, 128, 0, st>>>(d.pos_re, d.pos_im, d.freq_w, d.eiwt, d.gzed, d.sc, c.nf, n2,
+    launch_pdl(k_eiwt, dim3(nblk(c.nf > 0 ? c.nf : 1)), dim3(kEW), 0, st, d.freq_w, d.sc, d.eiwt, c.nf, rp);
+    launch_pdl(k_pos_bc, dim3(n2), dim3(128), 0, st, d.pos_re, d.pos_im, d.freq_w, d.eiwt, d.gzed, d.sc, c.nf, n2,
                                  P.n3, P.n3a, d.bc1, d.bcr, 0);
     {
       const int tot = 2 * (P.n3a - P.n3) * n2;
-      k_extend<<<nblk(tot), kEW, 0, st>>>(d.bc1, d.bcr, d.ext, n2, P.n3, P.n3a);
+      launch_pdl(k_extend, dim3(nblk(tot)), dim3(kEW), 0, st, d.bc1, d.bcr, d.ext, n2, P.n3, P.n3a);
     }
     E.xf({E.R(GRID_ADD, 1, 0, 0, d.bc1, P.n3a, P.n3a, n2, kA1, P.n3a, P.n3a, n2),
           E.R(GRID_ADD, 1, 0, 0, d.bcr, P.n3a, P.n3a, n2, kAR, P.n3a, P.n3a, n2)});
     E.ew(k_div, nA, kA1, kAR, (const double*)d.k_add_thk, nA);
     // reconstruction at z = 0 (phiadd_1st_SWEET) for phit_add_1, phiz_add_1
     const double* aA1 = y + L.off[S_AADD1];
-    k_sweet_contract<<<dim3((n1 + kCx - 1) / kCx, n2), kCx * kCy, 0, st>>>(
+    launch_pdl(k_sweet_contract, dim3(dim3((n1 + kCx - 1) / kCx, n2)), dim3(kCx * kCy), 0, st, 
         aA1, kA1, d.cosk, d.sink, d.csh, d.kxcsh, n1, n2, P.n3a, n2 == 1 ? d.phit_add1 : d.tbig,
         n2 == 1 ? d.phiz_add1 : d.tbig2);
     if (n2 != 1) {
@@ -1112,7 +1146,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     const double* aA2 = y + L.off[S_AADD2];
     const double* aA3 = y + L.off[S_AADD3];
     if (n2 == 1) {
-      k_phiadd_sl_1d<<<(n1 + kCx - 1) / kCx, kCx * kCy, 0, st>>>(d.eta_sp, aA1, aA2, aA3, kA1, d.kx_add, d.csh,
+      launch_pdl(k_phiadd_sl_1d, dim3((n1 + kCx - 1) / kCx), dim3(kCx * kCy), 0, st, d.eta_sp, aA1, aA2, aA3, kA1, d.kx_add, d.csh,
                                                      d.ksh, d.kxcsh, n1, P.n3a, d.phix_add,
                                                      d.phiy_add, d.phiz_add, d.phit_add, d.phi_add);
     } else {
@@ -1198,7 +1232,7 @@ void enqueue_step(Ctx& c, cudaStream_t st) {
     StageArgs sa{};
     sa.nk = 0;
     sa.c = 0.0;
-    k_rk_stage<<<nblk(S), kEW, 0, st>>>(d.y0, sa, d.sc, d.ys, S);
+    launch_pdl(k_rk_stage, dim3(nblk(S)), dim3(kEW), 0, st, d.y0, sa, d.sc, d.ys, S);
   }
   enqueue_rhs(c, d.ys, d.k[0], true, st);
   static const double A[5][5] = {{0, 0, 0, 0, 0}, {0.5, 0, 0, 0, 0}, {0, 0.5, 0, 0, 0},
@@ -1213,7 +1247,7 @@ void enqueue_step(Ctx& c, cudaStream_t st) {
       sa.nk++;
     }
     sa.c = Cc[s];
-    k_rk_stage<<<nblk(S), kEW, 0, st>>>(d.y0, sa, d.sc, d.ys, S);
+    launch_pdl(k_rk_stage, dim3(nblk(S)), dim3(kEW), 0, st, d.y0, sa, d.sc, d.ys, S);
     enqueue_rhs(c, d.ys, d.k[s], true, st);
   }
   FinalArgs fa{};
@@ -1221,9 +1255,9 @@ void enqueue_step(Ctx& c, cudaStream_t st) {
   for (int a = 0; a < 10; ++a) fa.off[a] = L.off[a];
   fa.off[10] = S;
   const int nb = nblk(S);
-  k_rk_final<<<nb, kEW, 0, st>>>(d.y0, fa, d.sc, d.ynew, d.part, S);
-  k_rk_err<<<1, 32, 0, st>>>(d.part, nb, d.sc);
-  k_rk_out<<<nblk(nN), kEW, 0, st>>>(d.ynew + L.off[S_G1], d.ynew + L.off[S_G2],
+  launch_pdl(k_rk_final, dim3(nb), dim3(kEW), 0, st, d.y0, fa, d.sc, d.ynew, d.part, S);
+  launch_pdl(k_rk_err, dim3(1), dim3(32), 0, st, d.part, nb, d.sc);
+  launch_pdl(k_rk_out, dim3(nblk(nN)), dim3(kEW), 0, st, d.ynew + L.off[S_G1], d.ynew + L.off[S_G2],
                                      d.k[4] + L.off[S_G1], d.k[4] + L.off[S_G2], d.omega, d.sc,
                                      (int)nN, P.igeom, P.d_hinge, P.xlen, d.etam, d.phim, d.NL1,
                                      d.part + 10 * (long long)nb, d.counter);
@@ -1240,7 +1274,7 @@ void enqueue_accept(Ctx& c, bool end_ramp, cudaStream_t st) {
   cudaMemcpyAsync(d.deta, d.deta_c, sizeof(double) * nN, cudaMemcpyDeviceToDevice, st);
   if (end_ramp) {
     const long long nA = (long long)c.P.n3a * c.P.n2;
-    k_sub<<<nblk(nA), kEW, 0, st>>>(d.y0 + L.off[S_AADD1], d.y0 + L.off[S_AADDR], nA);
+    launch_pdl(k_sub, dim3(nblk(nA)), dim3(kEW), 0, st, d.y0 + L.off[S_AADD1], d.y0 + L.off[S_AADDR], nA);
   }
 }
 
@@ -1261,12 +1295,12 @@ void enqueue_initialize(Ctx& c, cudaStream_t st) {
   if (!has_wavemaker(P)) return;
   const RampP rp = ramp_params(P);
   const long long nA = E.nA();
-  k_eiwt<<<nblk(c.nf > 0 ? c.nf : 1), kEW, 0, st>>>(d.freq_w, d.sc, d.eiwt, c.nf, rp);
-  k_pos_bc<<<P.n2, 128, 0, st>>>(d.pos_re, d.pos_im, d.freq_w, d.eiwt, d.gzed, d.sc, c.nf,
+  launch_pdl(k_eiwt, dim3(nblk(c.nf > 0 ? c.nf : 1)), dim3(kEW), 0, st, d.freq_w, d.sc, d.eiwt, c.nf, rp);
+  launch_pdl(k_pos_bc, dim3(P.n2), dim3(128), 0, st, d.pos_re, d.pos_im, d.freq_w, d.eiwt, d.gzed, d.sc, c.nf,
                                  P.n2, P.n3, P.n3a, d.bc1, d.bcr, 1);
   {
     const int tot = (P.n3a - P.n3) * P.n2;
-    k_extend<<<nblk(tot), kEW, 0, st>>>(d.bc1, nullptr, d.ext, P.n2, P.n3, P.n3a);
+    launch_pdl(k_extend, dim3(nblk(tot)), dim3(kEW), 0, st, d.bc1, nullptr, d.ext, P.n2, P.n3, P.n3a);
   }
   double* a1 = d.y0 + L.off[S_AADD1];
   E.xf({E.R(GRID_ADD, 1, 0, 0, d.bc1, P.n3a, P.n3a, P.n2, a1, P.n3a, P.n3a, P.n2)});
@@ -1276,7 +1310,7 @@ void enqueue_initialize(Ctx& c, cudaStream_t st) {
 
 void enqueue_diagnostics(Ctx& c, double* out, cudaStream_t st) {
   const Params& P = c.P;
-  k_diagnostics<<<1, 1024, 0, st>>>(c.d.eta, c.d.phis, c.d.phi_add, c.d.deta, c.d.etax, c.d.etay, P.n1, P.n2,
+  launch_pdl(k_diagnostics, dim3(1), dim3(1024), 0, st, c.d.eta, c.d.phis, c.d.phi_add, c.d.deta, c.d.etax, c.d.etay, P.n1, P.n2,
                                      (long long)P.nd1 * P.nd2, out);
 }
 
@@ -1287,7 +1321,7 @@ void enqueue_slope_filter(Ctx& c, int dir, cudaStream_t st) {
   const int nf = dir == 0 ? std::abs((int)(P.n1 * 0.7)) : std::abs((int)(P.n2 * 0.7));
   for (double* f : {c.d.phis, c.d.eta}) {
     E.xf({E.S2F_N(f, c.d.NL1)});
-    k_cut_modes<<<nblk(E.nN()), kEW, 0, st>>>(c.d.NL1, P.n1, P.n2, nf, dir);
+    launch_pdl(k_cut_modes, dim3(nblk(E.nN())), dim3(kEW), 0, st, c.d.NL1, P.n1, P.n2, nf, dir);
     E.xf({E.F2S_N(c.d.NL1, f)});
   }
 }
@@ -1296,7 +1330,7 @@ void enqueue_probes(Ctx& c, cudaStream_t st) {
   if (c.nprobes <= 0) return;
   Enq E(c, st);
   E.xf({E.S2F_N(c.d.eta, c.d.NL2)});
-  k_probe_dot<<<c.nprobes, 256, 0, st>>>(c.d.NL2, c.d.mat_coscos, E.nN(), c.d.probe_out);
+  launch_pdl(k_probe_dot, dim3(c.nprobes), dim3(256), 0, st, c.d.NL2, c.d.mat_coscos, E.nN(), c.d.probe_out);
 }
 
 }  // namespace hos

@@ -51,6 +51,7 @@ __device__ __forceinline__ double twiddle_s(const double* q, int D, int m) {
 //   mode 2: input symmetry: terms are pairs (j, D-j) staged as
 //           u = x_j + x_{D-j}, v = x_j - x_{D-j} (outputs k <= D/2)
 __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b) {
+  pdl_wait();
   extern __shared__ double smem[];
   __shared__ double red[kXWarps][32][2];
   __shared__ bool amlast;
@@ -231,6 +232,7 @@ constexpr int kYR = 8;  // outputs per thread
 // y pass: one thread = one line (consecutive lines are contiguous in memory)
 // and kYR outputs; twiddles are warp-uniform.
 __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatch b) {
+  pdl_wait();
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const AxisJob& J = b.job[jb];
@@ -307,6 +309,7 @@ __device__ __forceinline__ double group_sum(double v) {
 // small launches so that enough warps hide the load latency)
 template <int SPLIT>
 __global__ void __launch_bounds__(kTThreads) two_level_pass1(const AxisBatch b) {
+  pdl_wait();
   constexpr int kOut = kTThreads / SPLIT;
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
@@ -352,6 +355,7 @@ __global__ void __launch_bounds__(kTThreads) two_level_pass1(const AxisBatch b) 
 
 template <int SPLIT>
 __global__ void __launch_bounds__(kTThreads) two_level_pass2(const AxisBatch b) {
+  pdl_wait();
   constexpr int kOut = kTThreads / SPLIT;
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
@@ -490,14 +494,14 @@ void launch_two_level_split(AxisBatch& b, cudaStream_t st) {
     total += b.job[i].nlines * ((b.job[i].B * (b.job[i].A + 1) + kOut - 1) / kOut);
   }
   b.start[b.njobs] = total;
-  if (total > 0) two_level_pass1<SPLIT><<<total, kTThreads, 0, st>>>(b);
+  if (total > 0) launch_pdl(two_level_pass1<SPLIT>, dim3(total), dim3(kTThreads), 0, st, b);
   total = 0;
   for (int i = 0; i < b.njobs; ++i) {
     b.start[i] = total;
     total += b.job[i].nlines * ((b.job[i].nout + kOut - 1) / kOut);
   }
   b.start[b.njobs] = total;
-  if (total > 0) two_level_pass2<SPLIT><<<total, kTThreads, 0, st>>>(b);
+  if (total > 0) launch_pdl(two_level_pass2<SPLIT>, dim3(total), dim3(kTThreads), 0, st, b);
 }
 
 void launch_two_level(AxisBatch& b, cudaStream_t st) {
@@ -577,7 +581,7 @@ void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
     cudaFuncSetAttribute(axis_pass_lanes_k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr_set = true;
   }
-  if (total > 0) axis_pass_lanes_k<<<total, kXThreads, smem, st>>>(b);
+  if (total > 0) launch_pdl(axis_pass_lanes_k, dim3(total), dim3(kXThreads), smem, st, b);
 }
 
 void launch_batch_y(AxisBatch& b, cudaStream_t st) {
@@ -588,7 +592,7 @@ void launch_batch_y(AxisBatch& b, cudaStream_t st) {
     total += nlb * ((b.job[i].nout + kYR - 1) / kYR);
   }
   b.start[b.njobs] = total;
-  if (total > 0) axis_pass_lanes_line<<<total, kYThreads, 0, st>>>(b);
+  if (total > 0) launch_pdl(axis_pass_lanes_line, dim3(total), dim3(kYThreads), 0, st, b);
 }
 
 }  // namespace
@@ -686,6 +690,7 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
 
 namespace {
 __global__ void k_dfma_peak(double* out, int iters, double a, double b) {
+  pdl_wait();
   double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
   double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
   for (int i = 0; i < iters; ++i) {
