@@ -116,10 +116,26 @@ def _measured_peaks():
     return 6800.0, "of fallback"
 
 
+def _two_level_fmas(D, nin, nout):
+    """FMAs of the two-level pass pair the library picks for a REDFT00
+    length with D = A * B (the choice of pick_factors in xform.cu), or of
+    the direct symmetric sum when no factor pair is cheaper."""
+    direct = 0.5 * nin * nout
+    best = 0.6 * direct
+    for A in range(2, D // 2 + 1):
+        if D % A:
+            continue
+        B = D // A
+        if B < 2:
+            continue
+        best = min(best, 2.0 * (A + 1) * nin + 2.0 * B * nout)
+    return best if best < 0.6 * direct else direct
+
+
 def _profile_traffic():
-    """Per-launch DRAM traffic of the dominant kernel from the committed ncu
-    summary (profiles/xform_x_pass_irregular_2d.md), if present."""
-    p = os.path.join(ROOT, "profiles", "xform_x_pass_irregular_2d.md")
+    """Per-launch DRAM traffic of the dominant kernels from the committed ncu
+    summary (profiles/two_level_passes_irregular_2d.md), if present."""
+    p = os.path.join(ROOT, "profiles", "two_level_passes_irregular_2d.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -263,15 +279,16 @@ def run_cuda(args, w):
     e2e_value = world * args.steps / e2e_s
     io_bytes = 8 * sum(s[0] * s[1] for s in shapes)
 
-    # roofline of the dominant kernel: the x pass of the big-grid transforms
-    # (a batch of four FOURIER_2_SPACE_BIG of extended n1 modes), timed alone
+    # roofline of the dominant kernels: the two passes of the big-grid
+    # transforms (a batch of four FOURIER_2_SPACE_BIG of extended n1 modes,
+    # the shape of the HOS order loop), timed alone after the step loop
     nd1 = info["nd1"]
     ms = tank.time_transform("big", -1, "cos", "cos", (n1, 1), (nd1, 1), batch=4, nrep=50)
     alg_bytes = 16.0 * nd1 * 4          # 8-byte read + 8-byte write per output element
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     peak, peak_src = _measured_peaks()
     fp64_peak = hosnwt.fp64_peak_gflops()
-    fp64_flops = 2.0 * n1 * nd1 * 4     # one FMA per (input, output) pair of the direct sum
+    fp64_flops = 2.0 * _two_level_fmas(nd1 - 1, n1, nd1) * 4
     fp64_achieved = fp64_flops / (ms * 1e-3) / 1e9
     traffic = _profile_traffic()
 
@@ -289,12 +306,13 @@ def run_cuda(args, w):
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_src,
-                             "kernel": "axis_pass_lanes_k (x pass, 4 x F2S_big of n1 modes)",
+                             "kernel": "two_level_pass1 + two_level_pass2 (4 x FOURIER_2_SPACE_BIG of n1 modes)",
                              "ms_per_launch": ms,
                              "fp64": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64_peak,
                                       "frac": fp64_achieved / fp64_peak,
-                                      "note": "the pass is FP64-pipe bound on GB300; peak measured "
-                                              "live with a DFMA loop"}},
+                                      "note": "FMAs of the two-level algorithm actually run; the "
+                                              "passes are latency-bound; FP64 peak measured live "
+                                              "with a DFMA loop"}},
                 }
         if world == 1:
             line["cpu_baseline"] = cpu_baseline(w)
