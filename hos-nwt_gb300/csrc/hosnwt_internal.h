@@ -94,7 +94,7 @@ struct AxisJob {
   double* cs;                // nlines * B * (A + 1) * 2 partial cos/sin sums
 };
 
-constexpr int kMaxJobs = 8;
+constexpr int kMaxJobs = 16;
 
 struct AxisBatch {
   AxisJob job[kMaxJobs];

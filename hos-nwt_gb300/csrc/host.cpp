@@ -641,8 +641,14 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
     // B (A+1) 2 <= 2 (D+2) doubles per line for any factor pair
     c.tb.cs_cap = (long long)kMaxJobs * std::max(nd2, n2) * 4LL * (std::max(nd1, n1) + 2);
     c.tb.cs = dalloc<double>(c, (size_t)c.tb.cs_cap);
+    // the wavemaker branch runs on its own stream with its own scratch
+    c.tb2 = c.tb;
+    c.tb2.part = dalloc<double>(c, (size_t)c.tb.part_cap);
+    c.tb2.cnt = dalloc<unsigned int>(c, (size_t)c.tb.cnt_cap);
+    c.tb2.cs = dalloc<double>(c, (size_t)c.tb.cs_cap);
   }
   c.tb.q_n1 = d.q_n1; c.tb.q_n2 = d.q_n2; c.tb.q_nd1 = d.q_nd1; c.tb.q_nd2 = d.q_nd2; c.tb.q_add = d.q_add;
+  c.tb2.q_n1 = d.q_n1; c.tb2.q_n2 = d.q_n2; c.tb2.q_nd1 = d.q_nd1; c.tb2.q_nd2 = d.q_nd2; c.tb2.q_add = d.q_add;
   for (void* p : c.allocs)
     if (!p) return fail(c, HOSNWT_ERR_CUDA, "device allocation failed");
   if (cudaGetLastError() != cudaSuccess) return fail(c, HOSNWT_ERR_CUDA, "upload failed");
@@ -688,7 +694,13 @@ int alloc_device(Ctx& c) {
     for (int q = 0; q < 5; ++q) { d.Q[q] = dalloc<double>(c, nQ); d.B[q] = dalloc<double>(c, nQ); }
   }
   const size_t ntmp = (size_t)std::max(std::max(P.nd1, P.n3a), P.n1) * std::max(P.nd2, P.n2);
-  for (int i = 0; i < kMaxJobs; ++i) d.xtmp[i] = dalloc<double>(c, ntmp);
+  for (int i = 0; i < kMaxJobs; ++i) {
+    d.xtmp[i] = dalloc<double>(c, ntmp);
+    d.xtmp2[i] = dalloc<double>(c, ntmp);
+  }
+  if (cudaStreamCreateWithFlags(&c.st2, cudaStreamNonBlocking) != cudaSuccess) return 1;
+  for (cudaEvent_t* e : {&c.ev_fork, &c.ev_eta, &c.ev_join})
+    if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return 1;
   d.sc = dalloc<double>(c, SC_COUNT);
   const size_t nparts = 10 * ((S + 255) / 256) + (std::max(nB, nN) + 255) / 256 + 1024;
   d.part = dalloc<double>(c, nparts);
@@ -711,6 +723,11 @@ void free_device(Ctx& c) {
   c.allocs.clear();
   if (c.d.host_sc) cudaFreeHost(c.d.host_sc);
   c.d.host_sc = nullptr;
+  for (cudaEvent_t e : {c.ev_fork, c.ev_eta, c.ev_join})
+    if (e) cudaEventDestroy(e);
+  c.ev_fork = c.ev_eta = c.ev_join = nullptr;
+  if (c.st2) cudaStreamDestroy(c.st2);
+  c.st2 = nullptr;
   if (c.st) cudaStreamDestroy(c.st);
   c.st = nullptr;
 }

@@ -875,7 +875,11 @@ struct Enq {
   cudaStream_t st;
   const Params& P;
   const Dev& d;
-  Enq(Ctx& cc, cudaStream_t s) : c(cc), st(s), P(cc.P), d(cc.d) {}
+  const Tables& tb;
+  double* const* tmp;
+  Enq(Ctx& cc, cudaStream_t s) : c(cc), st(s), P(cc.P), d(cc.d), tb(cc.tb), tmp(cc.d.xtmp) {}
+  Enq(Ctx& cc, cudaStream_t s, const Tables& t, double* const* tp)
+      : c(cc), st(s), P(cc.P), d(cc.d), tb(t), tmp(tp) {}
 
   long long nN() const { return (long long)P.n1 * P.n2; }
   long long nB() const { return (long long)P.nd1 * P.nd2; }
@@ -884,7 +888,7 @@ struct Enq {
   void xf(std::vector<XfReq> reqs) {
     for (size_t s = 0; s < reqs.size(); s += kMaxJobs) {
       const int cnt = (int)std::min<size_t>(kMaxJobs, reqs.size() - s);
-      launch_transforms(reqs.data() + s, cnt, c.tb, d.xtmp, st);
+      launch_transforms(reqs.data() + s, cnt, tb, tmp, st);
     }
   }
   XfReq R(int grid, int dir, int csx, int csy, const double* in, int in_ld, int nin1, int nin2,
@@ -964,6 +968,59 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
                                P.xlen, d.etam, d.phim, d.w_eta_x, d.w_eta_y, d.w_phi_x, d.w_phi_y,
                                d.part, d.counter);
   }
+  // 5. wavemaker: SWEET_1, phiadd_SL and the gradients of phi_add.  This
+  //    branch reads the free surface only through eta in space, so it runs
+  //    on the second stream with its own transform scratch and joins the
+  //    main stream before assembly.
+  cudaStream_t sw = c.st2;
+  Enq W(c, sw, c.tb2, d.xtmp2);
+  cudaEventRecord(c.ev_fork, st);
+  cudaStreamWaitEvent(sw, c.ev_fork, 0);
+  double* kA1 = k + L.off[S_AADD1];
+  double* kAR = k + L.off[S_AADDR];
+  double* kA1st = k + L.off[S_A1ST];
+  double* kEta1 = k + L.off[S_ETA1ST];
+  if (has_wavemaker(P)) {
+    const RampP rp = ramp_params(P);
+    launch_pdl(k_eiwt, dim3(nblk(c.nf > 0 ? c.nf : 1)), dim3(kEW), 0, sw, d.freq_w, d.sc, d.eiwt, c.nf, rp);
+    launch_pdl(k_pos_bc, dim3(n2), dim3(128), 0, sw, d.pos_re, d.pos_im, d.freq_w, d.eiwt, d.gzed, d.sc, c.nf, n2,
+                                 P.n3, P.n3a, d.bc1, d.bcr, 0);
+    {
+      const int tot = 2 * (P.n3a - P.n3) * n2;
+      launch_pdl(k_extend, dim3(nblk(tot)), dim3(kEW), 0, sw, d.bc1, d.bcr, d.ext, n2, P.n3, P.n3a);
+    }
+    W.xf({W.R(GRID_ADD, 1, 0, 0, d.bc1, P.n3a, P.n3a, n2, kA1, P.n3a, P.n3a, n2),
+          W.R(GRID_ADD, 1, 0, 0, d.bcr, P.n3a, P.n3a, n2, kAR, P.n3a, P.n3a, n2)});
+    W.ew(k_div, nA, kA1, kAR, (const double*)d.k_add_thk, nA);
+    // reconstruction at z = 0 (phiadd_1st_SWEET) for phit_add_1, phiz_add_1
+    const double* aA1 = y + L.off[S_AADD1];
+    launch_pdl(k_sweet_contract, dim3(dim3((n1 + kCx - 1) / kCx, n2)), dim3(kCx * kCy), 0, sw, 
+        aA1, kA1, d.cosk, d.sink, d.csh, d.kxcsh, n1, n2, P.n3a, n2 == 1 ? d.phit_add1 : d.Q[0],
+        n2 == 1 ? d.phiz_add1 : d.Q[1]);
+    if (n2 != 1) {
+      // y sums: sum_j2 A(i1, j2) cos(ky(j2) y(i2)) = FOURIER_2_SPACE_y
+      launch_y_f2s(W.tb, d.Q[0], n1, n1, d.phit_add1, n1, 0, sw);
+      launch_y_f2s(W.tb, d.Q[1], n1, n1, d.phiz_add1, n1, 0, sw);
+    }
+    // phidphiz + SWEET_1 RHS
+    W.ew(k_mul, nN, y + L.off[S_A1ST], (const double*)d.kth1, 1.0, d.a1k, nN);
+    W.xf({W.F2S_N(d.a1k, d.phiz1st)});
+    W.ew(k_sweet_rhs, nN, y + L.off[S_ETA1ST], (const double*)d.phit_add1,
+         (const double*)d.phiz1st, (const double*)d.phiz_add1, (const double*)d.nu,
+         (double)P.iabsnb, d.rhs1, kEta1, nN);
+    W.xf({W.S2F_N(d.rhs1, kA1st)});
+  } else {
+    cudaMemsetAsync(kA1, 0, sizeof(double) * nA, sw);
+    cudaMemsetAsync(kAR, 0, sizeof(double) * nA, sw);
+    cudaMemsetAsync(kA1st, 0, sizeof(double) * nN, sw);
+    cudaMemsetAsync(kEta1, 0, sizeof(double) * nN, sw);
+  }
+  // second- and third-order wavemaker slopes stay zero (i_wmk = 1)
+  cudaMemsetAsync(k + L.off[S_AADD2], 0, sizeof(double) * nA, sw);
+  cudaMemsetAsync(k + L.off[S_AADD3], 0, sizeof(double) * nA, sw);
+  cudaMemsetAsync(k + L.off[S_A2ND], 0, sizeof(double) * nN, sw);
+  cudaMemsetAsync(k + L.off[S_ETA2ND], 0, sizeof(double) * nN, sw);
+
   // 2. transform batch A: eta in space, eta / eta_x / eta_y / phis_x / phis_y on
   //    the big grid (phisxy_etaxy) and the order-1 HOS terms F2S_big(a1 kth_ext(j))
   {
@@ -983,11 +1040,52 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     for (int j = 1; j <= M; ++j)
       rq.push_back(E.F2S_B(d.prod[j - 1], nd1, n1, n2, d.phizi[(0) * M + (j - 1)]));
     E.xf(rq);
+    cudaEventRecord(c.ev_eta, st);
     if (n2 == 1) {
       cudaMemsetAsync(d.etay, 0, sizeof(double) * nB, st);
       cudaMemsetAsync(d.phisy, 0, sizeof(double) * nB, st);
     }
   }
+  // 5b. wavemaker branch, second part: phiadd_SL with the total additional
+  //     amplitudes at z = eta (needs eta in space from batch A) and the
+  //     gradients of phi_add on the big grid (resol_HOS.f90:534-555)
+  if (has_wavemaker(P)) {
+    cudaStreamWaitEvent(sw, c.ev_eta, 0);
+    const double* aA1 = y + L.off[S_AADD1];
+    const double* aA2 = y + L.off[S_AADD2];
+    const double* aA3 = y + L.off[S_AADD3];
+    if (n2 == 1) {
+      launch_pdl(k_phiadd_sl_1d, dim3((n1 + kCx - 1) / kCx), dim3(kCx * kCy), 0, sw, d.eta_sp, aA1, aA2,
+                 aA3, kA1, d.kx_add, d.csh, d.ksh, d.kxcsh, n1, P.n3a, d.phix_add, d.phiy_add, d.phiz_add,
+                 d.phit_add, d.phi_add);
+    } else {
+      const long long nq = (long long)n1 * P.n3a * n2;
+      W.ew(k_phiadd_q, nq, aA1, aA2, aA3, (const double*)kA1, (const double*)d.csh,
+           (const double*)d.ksh, (const double*)d.kycsh, (const double*)d.kxcsh, n1, n2, P.n3a,
+           d.Q[0], d.Q[1], d.Q[2], d.Q[3], d.Q[4]);
+      const int lines = n1 * P.n3a;
+      launch_y_f2s(W.tb, d.Q[0], lines, lines, d.B[0], lines, 0, sw);
+      launch_y_f2s(W.tb, d.Q[1], lines, lines, d.B[1], lines, 0, sw);
+      launch_y_f2s(W.tb, d.Q[2], lines, lines, d.B[2], lines, 1, sw);
+      launch_y_f2s(W.tb, d.Q[3], lines, lines, d.B[3], lines, 0, sw);
+      launch_y_f2s(W.tb, d.Q[4], lines, lines, d.B[4], lines, 0, sw);
+      W.ew(k_phiadd_contract, nN, (const double*)d.eta_sp, (const double*)d.kx_add,
+           (const double*)d.B[0], (const double*)d.B[1], (const double*)d.B[2],
+           (const double*)d.B[3], (const double*)d.B[4], n1, n2, P.n3a, d.phix_add, d.phiy_add,
+           d.phiz_add, d.phit_add, d.phi_add);
+    }
+  } else {
+    cudaMemsetAsync(d.phix_add, 0, sizeof(double) * nN, sw);
+    cudaMemsetAsync(d.phiy_add, 0, sizeof(double) * nN, sw);
+    cudaMemsetAsync(d.phiz_add, 0, sizeof(double) * nN, sw);
+    cudaMemsetAsync(d.phit_add, 0, sizeof(double) * nN, sw);
+    cudaMemsetAsync(d.phi_add, 0, sizeof(double) * nN, sw);
+  }
+  W.xf({W.S2F_N(d.phix_add, d.pmode[0]), W.S2F_N(d.phiy_add, d.pmode[1]),
+        W.S2F_N(d.phiz_add, d.pmode[2])});
+  W.xf({W.F2S_B(d.pmode[0], n1, n1, n2, d.pxe), W.F2S_B(d.pmode[1], n1, n1, n2, d.pye),
+        W.F2S_B(d.pmode[2], n1, n1, n2, d.pze)});
+  cudaEventRecord(c.ev_join, sw);
   // 3. powers eta^j / j! with partial dealiasing: one kernel per run of
   //    orders up to the next order that is dealiased
   for (int j = 1; j < M;) {
@@ -1108,85 +1206,6 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     }
   }
 
-  // 5. wavemaker: SWEET_1 and phiadd_SL
-  double* kA1 = k + L.off[S_AADD1];
-  double* kAR = k + L.off[S_AADDR];
-  double* kA1st = k + L.off[S_A1ST];
-  double* kEta1 = k + L.off[S_ETA1ST];
-  if (has_wavemaker(P)) {
-    const RampP rp = ramp_params(P);
-    launch_pdl(k_eiwt, dim3(nblk(c.nf > 0 ? c.nf : 1)), dim3(kEW), 0, st, d.freq_w, d.sc, d.eiwt, c.nf, rp);
-    launch_pdl(k_pos_bc, dim3(n2), dim3(128), 0, st, d.pos_re, d.pos_im, d.freq_w, d.eiwt, d.gzed, d.sc, c.nf, n2,
-                                 P.n3, P.n3a, d.bc1, d.bcr, 0);
-    {
-      const int tot = 2 * (P.n3a - P.n3) * n2;
-      launch_pdl(k_extend, dim3(nblk(tot)), dim3(kEW), 0, st, d.bc1, d.bcr, d.ext, n2, P.n3, P.n3a);
-    }
-    E.xf({E.R(GRID_ADD, 1, 0, 0, d.bc1, P.n3a, P.n3a, n2, kA1, P.n3a, P.n3a, n2),
-          E.R(GRID_ADD, 1, 0, 0, d.bcr, P.n3a, P.n3a, n2, kAR, P.n3a, P.n3a, n2)});
-    E.ew(k_div, nA, kA1, kAR, (const double*)d.k_add_thk, nA);
-    // reconstruction at z = 0 (phiadd_1st_SWEET) for phit_add_1, phiz_add_1
-    const double* aA1 = y + L.off[S_AADD1];
-    launch_pdl(k_sweet_contract, dim3(dim3((n1 + kCx - 1) / kCx, n2)), dim3(kCx * kCy), 0, st, 
-        aA1, kA1, d.cosk, d.sink, d.csh, d.kxcsh, n1, n2, P.n3a, n2 == 1 ? d.phit_add1 : d.tbig,
-        n2 == 1 ? d.phiz_add1 : d.tbig2);
-    if (n2 != 1) {
-      // y sums: sum_j2 A(i1, j2) cos(ky(j2) y(i2)) = FOURIER_2_SPACE_y
-      launch_y_f2s(c.tb, d.tbig, n1, n1, d.phit_add1, n1, 0, st);
-      launch_y_f2s(c.tb, d.tbig2, n1, n1, d.phiz_add1, n1, 0, st);
-    }
-    // phidphiz + SWEET_1 RHS
-    E.ew(k_mul, nN, y + L.off[S_A1ST], (const double*)d.kth1, 1.0, d.a1k, nN);
-    E.xf({E.F2S_N(d.a1k, d.phiz1st)});
-    E.ew(k_sweet_rhs, nN, y + L.off[S_ETA1ST], (const double*)d.phit_add1,
-         (const double*)d.phiz1st, (const double*)d.phiz_add1, (const double*)d.nu,
-         (double)P.iabsnb, d.rhs1, kEta1, nN);
-    E.xf({E.S2F_N(d.rhs1, kA1st)});
-    // phiadd_SL with the total additional amplitudes at z = eta
-    const double* aA2 = y + L.off[S_AADD2];
-    const double* aA3 = y + L.off[S_AADD3];
-    if (n2 == 1) {
-      launch_pdl(k_phiadd_sl_1d, dim3((n1 + kCx - 1) / kCx), dim3(kCx * kCy), 0, st, d.eta_sp, aA1, aA2, aA3, kA1, d.kx_add, d.csh,
-                                                     d.ksh, d.kxcsh, n1, P.n3a, d.phix_add,
-                                                     d.phiy_add, d.phiz_add, d.phit_add, d.phi_add);
-    } else {
-      const long long nq = (long long)n1 * P.n3a * n2;
-      E.ew(k_phiadd_q, nq, aA1, aA2, aA3, (const double*)kA1, (const double*)d.csh,
-           (const double*)d.ksh, (const double*)d.kycsh, (const double*)d.kxcsh, n1, n2, P.n3a,
-           d.Q[0], d.Q[1], d.Q[2], d.Q[3], d.Q[4]);
-      const int lines = n1 * P.n3a;
-      launch_y_f2s(c.tb, d.Q[0], lines, lines, d.B[0], lines, 0, st);
-      launch_y_f2s(c.tb, d.Q[1], lines, lines, d.B[1], lines, 0, st);
-      launch_y_f2s(c.tb, d.Q[2], lines, lines, d.B[2], lines, 1, st);
-      launch_y_f2s(c.tb, d.Q[3], lines, lines, d.B[3], lines, 0, st);
-      launch_y_f2s(c.tb, d.Q[4], lines, lines, d.B[4], lines, 0, st);
-      E.ew(k_phiadd_contract, nN, (const double*)d.eta_sp, (const double*)d.kx_add,
-           (const double*)d.B[0], (const double*)d.B[1], (const double*)d.B[2],
-           (const double*)d.B[3], (const double*)d.B[4], n1, n2, P.n3a, d.phix_add, d.phiy_add,
-           d.phiz_add, d.phit_add, d.phi_add);
-    }
-  } else {
-    cudaMemsetAsync(kA1, 0, sizeof(double) * nA, st);
-    cudaMemsetAsync(kAR, 0, sizeof(double) * nA, st);
-    cudaMemsetAsync(kA1st, 0, sizeof(double) * nN, st);
-    cudaMemsetAsync(kEta1, 0, sizeof(double) * nN, st);
-    cudaMemsetAsync(d.phix_add, 0, sizeof(double) * nN, st);
-    cudaMemsetAsync(d.phiy_add, 0, sizeof(double) * nN, st);
-    cudaMemsetAsync(d.phiz_add, 0, sizeof(double) * nN, st);
-    cudaMemsetAsync(d.phit_add, 0, sizeof(double) * nN, st);
-    cudaMemsetAsync(d.phi_add, 0, sizeof(double) * nN, st);
-  }
-  // second- and third-order wavemaker slopes stay zero (i_wmk = 1)
-  cudaMemsetAsync(k + L.off[S_AADD2], 0, sizeof(double) * nA, st);
-  cudaMemsetAsync(k + L.off[S_AADD3], 0, sizeof(double) * nA, st);
-  cudaMemsetAsync(k + L.off[S_A2ND], 0, sizeof(double) * nN, st);
-  cudaMemsetAsync(k + L.off[S_ETA2ND], 0, sizeof(double) * nN, st);
-
-  // 6. gradients of phi_add on the big grid (resol_HOS.f90:534-555)
-  E.xf({E.S2F_N(d.phix_add, d.pmode[0]), E.S2F_N(d.phiy_add, d.pmode[1]),
-        E.S2F_N(d.phiz_add, d.pmode[2])});
-  E.xf({E.F2S_B(d.pmode[0], n1, n1, n2, d.pxe), E.F2S_B(d.pmode[1], n1, n1, n2, d.pye),
-        E.F2S_B(d.pmode[2], n1, n1, n2, d.pze)});
   // 7. free-surface terms, filters to the n grid, final RHS
   aa.etax = d.etax; aa.etay = d.etay; aa.phisx = d.phisx; aa.phisy = d.phisy;
   aa.pxe = d.pxe; aa.pye = d.pye; aa.pze = d.pze;
@@ -1203,6 +1222,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   for (int j = 1; j <= M - 1; ++j) aa.phizm[aa.nphizm++] = d.phizm[j];
   aa.phizmM = d.phizm[M];
   aa.M = M;
+  cudaStreamWaitEvent(st, c.ev_join, 0);
   E.ew(k_assemble, nB, aa, d.A1, d.A3, nB);
   // filter_ext: S2F_big truncated to n1 x n2, then F2S on the n grid
   E.xf({E.R(GRID_BIG, 1, 0, 0, d.A1, nd1, nd1, nd2, d.pmode[0], n1, n1, n2),

@@ -85,6 +85,7 @@ struct Dev {
   double *Q[5] = {}, *B[5] = {};
   // transform temporaries
   double *xtmp[kMaxJobs] = {};
+  double *xtmp2[kMaxJobs] = {};  // temporaries of the wavemaker branch
   // scalars and reductions
   double *sc = nullptr;
   double *part = nullptr;       // partial sums / maxima
@@ -108,7 +109,10 @@ struct Ctx {
   StateLayout L{};
   Dev d{};
   Tables tb{};
+  Tables tb2{};                   // transform scratch of the wavemaker branch
   cudaStream_t st = nullptr;
+  cudaStream_t st2 = nullptr;     // wavemaker branch of each right-hand side
+  cudaEvent_t ev_fork = nullptr, ev_eta = nullptr, ev_join = nullptr;
   cudaGraphExec_t step_graph = nullptr;
   double time_cur = 0.0;
   int endramp = 0;
