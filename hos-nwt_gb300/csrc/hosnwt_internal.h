@@ -80,6 +80,8 @@ struct AxisJob {
   double w0, wm, wl;         // weights for j == 0, interior j, j == N-1
   double s0, sm, sl;         // scales for k == 0, interior k, k == N-1
   double gscale;
+  const double* win;         // optional input weights (first pass only):
+  long long win_sl;          //   input j of line l is multiplied by win[j + l * win_sl]
   const double* q;           // quarter-wave table cos(pi*m/(2D)), m = 0..D
   // work decomposition of the x pass (set by the launcher)
   int mode;                  // 0 direct, 1 output symmetry k <-> D-k, 2 input symmetry j <-> D-j
@@ -115,6 +117,8 @@ struct XfReq {
   double* out;
   int out_ld, nout1, nout2;  // output leading dim and written extent
   double scale;
+  const double* win = nullptr;  // optional weights: input (i1, i2) times win[i1 + win_ld * i2]
+  int win_ld = 0;
 };
 
 struct Tables;

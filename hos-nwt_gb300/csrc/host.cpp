@@ -646,9 +646,16 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
     c.tb2.part = dalloc<double>(c, (size_t)c.tb.part_cap);
     c.tb2.cnt = dalloc<unsigned int>(c, (size_t)c.tb.cnt_cap);
     c.tb2.cs = dalloc<double>(c, (size_t)c.tb.cs_cap);
+    // and so does the eta-power branch
+    c.tb3 = c.tb;
+    c.tb3.part = dalloc<double>(c, (size_t)c.tb.part_cap);
+    c.tb3.cnt = dalloc<unsigned int>(c, (size_t)c.tb.cnt_cap);
+    c.tb3.cs = dalloc<double>(c, (size_t)c.tb.cs_cap);
   }
   c.tb.q_n1 = d.q_n1; c.tb.q_n2 = d.q_n2; c.tb.q_nd1 = d.q_nd1; c.tb.q_nd2 = d.q_nd2; c.tb.q_add = d.q_add;
-  c.tb2.q_n1 = d.q_n1; c.tb2.q_n2 = d.q_n2; c.tb2.q_nd1 = d.q_nd1; c.tb2.q_nd2 = d.q_nd2; c.tb2.q_add = d.q_add;
+  for (Tables* t : {&c.tb2, &c.tb3}) {
+    t->q_n1 = d.q_n1; t->q_n2 = d.q_n2; t->q_nd1 = d.q_nd1; t->q_nd2 = d.q_nd2; t->q_add = d.q_add;
+  }
   for (void* p : c.allocs)
     if (!p) return fail(c, HOSNWT_ERR_CUDA, "device allocation failed");
   if (cudaGetLastError() != cudaSuccess) return fail(c, HOSNWT_ERR_CUDA, "upload failed");
@@ -673,19 +680,19 @@ int alloc_device(Ctx& c) {
                      &d.pmode[0], &d.pmode[1], &d.pmode[2]})
     *p = dalloc<double>(c, nN);
   d.etapm.resize(M);
-  d.prod.resize(M);
   d.phizm.assign(M + 2, nullptr);
   d.aHOS.assign(M + 2, nullptr);
-  for (int j = 0; j < M; ++j) { d.etapm[j] = dalloc<double>(c, nB); d.prod[j] = dalloc<double>(c, nB); }
+  for (int j = 0; j < M; ++j) d.etapm[j] = dalloc<double>(c, nB);
   for (int j = 1; j <= M; ++j) { d.phizm[j] = dalloc<double>(c, nB); d.aHOS[j] = dalloc<double>(c, nB); }
   d.phizi.assign((size_t)M * M, nullptr);
   for (int m = 1; m <= M; ++m)
     for (int j = 1; j <= M + 1 - m; ++j) d.phizi[(m - 1) * M + (j - 1)] = dalloc<double>(c, nB);
   for (double** p : {&d.etax, &d.etay, &d.phisx, &d.phisy, &d.gradeta2, &d.phimext, &d.phizMm1,
-                     &d.tbig, &d.tbig2, &d.tbig3, &d.pxe, &d.pye, &d.pze, &d.A1, &d.A3, &d.t1,
+                     &d.tbig, &d.tbig2, &d.ptmp, &d.pxe, &d.pye, &d.pze, &d.A1, &d.A3, &d.t1,
                      &d.geta2phiz, &d.geta2phiz2})
     *p = dalloc<double>(c, std::max(nB, nN));
   for (int g = 0; g < 24; ++g) d.grp[g] = dalloc<double>(c, std::max(nB, nN));
+  for (int i = 0; i < Dev::kDealiasTmp; ++i) d.dtmp[i] = dalloc<double>(c, std::max(nB, nN));
   d.diag = dalloc<double>(c, 8);
   d.bc1 = dalloc<double>(c, nA);
   d.bcr = dalloc<double>(c, nA);
@@ -697,12 +704,14 @@ int alloc_device(Ctx& c) {
   for (int i = 0; i < kMaxJobs; ++i) {
     d.xtmp[i] = dalloc<double>(c, ntmp);
     d.xtmp2[i] = dalloc<double>(c, ntmp);
+    d.xtmp3[i] = dalloc<double>(c, ntmp);
   }
   if (cudaStreamCreateWithFlags(&c.st2, cudaStreamNonBlocking) != cudaSuccess) return 1;
-  for (cudaEvent_t* e : {&c.ev_fork, &c.ev_eta, &c.ev_join})
+  if (cudaStreamCreateWithFlags(&c.st3, cudaStreamNonBlocking) != cudaSuccess) return 1;
+  for (cudaEvent_t* e : {&c.ev_fork, &c.ev_eta, &c.ev_join, &c.ev_pow})
     if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return 1;
   d.sc = dalloc<double>(c, SC_COUNT);
-  const size_t nparts = 10 * ((S + 255) / 256) + (std::max(nB, nN) + 255) / 256 + 1024;
+  const size_t nparts = 10 * ((S + 255) / 256) + (std::max(nB, nN) + 63) / 64 + 1024;
   d.part = dalloc<double>(c, nparts);
   d.counter = dalloc<unsigned int>(c, 16);
   if (cudaMallocHost((void**)&d.host_sc, SC_COUNT * sizeof(double)) != cudaSuccess) return 1;
@@ -723,11 +732,13 @@ void free_device(Ctx& c) {
   c.allocs.clear();
   if (c.d.host_sc) cudaFreeHost(c.d.host_sc);
   c.d.host_sc = nullptr;
-  for (cudaEvent_t e : {c.ev_fork, c.ev_eta, c.ev_join})
+  for (cudaEvent_t e : {c.ev_fork, c.ev_eta, c.ev_join, c.ev_pow})
     if (e) cudaEventDestroy(e);
-  c.ev_fork = c.ev_eta = c.ev_join = nullptr;
-  if (c.st2) cudaStreamDestroy(c.st2);
-  c.st2 = nullptr;
+  c.ev_fork = c.ev_eta = c.ev_join = c.ev_pow = nullptr;
+  for (cudaStream_t* s : {&c.st2, &c.st3}) {
+    if (*s) cudaStreamDestroy(*s);
+    *s = nullptr;
+  }
   if (c.st) cudaStreamDestroy(c.st);
   c.st = nullptr;
 }

@@ -17,6 +17,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <utility>
+#include <vector>
 
 #include "tank.h"
 
@@ -25,6 +27,9 @@ namespace hos {
 namespace {
 
 constexpr int kEW = 256;
+// FP64 sincos per element is slow on this part: kernels that evaluate one per
+// element use small blocks so that the work spreads over more SMs.
+constexpr int kTrig = 64;
 inline int nblk(long long n, int t = kEW) { return (int)((n + t - 1) / t); }
 
 // ---------------------------------------------------------------------------
@@ -96,7 +101,8 @@ __global__ void k_gtof(const double* __restrict__ G1, const double* __restrict__
   double e = 0.0;
   if (i < n) {
     const double w = om[i];
-    const double c = cos(-w * dt), s = sin(-w * dt);
+    double s, c;
+    sincos(-w * dt, &s, &c);
     const double g1 = G1[i], g2 = G2[i];
     e = g1 * c - g2 * s;
     double p = g2 * c + g1 * s;
@@ -211,24 +217,6 @@ __global__ void k_sq2(const double* __restrict__ a, const double* __restrict__ b
 }
 
 // products a(m) * kth_ext(:,:,j) on the nonzero extent of a(m)
-struct ProdArgs {
-  double* out[16];
-  int jidx[16];
-  int count;
-};
-__global__ void k_prod_kth(const double* __restrict__ a, int a_ld, int e1, int e2,
-                           const double* __restrict__ kth_ext, int nd1, int nd2, ProdArgs pa) {
-  pdl_wait();
-  const long long n = (long long)e1 * e2;
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int i1 = (int)(i % e1), i2 = (int)(i / e1);
-  const double v = a[i1 + (long long)a_ld * i2];
-  const long long o = i1 + (long long)nd1 * i2;
-  const long long plane = (long long)nd1 * nd2;
-  for (int t = 0; t < pa.count; ++t) pa.out[t][o] = v * kth_ext[plane * pa.jidx[t] + o];
-}
-
 // order iHOS of HOSphis_modes (resol_HOS.f90:716-764)
 struct AccArgs {
   const double* phizi[16];  // phizi(m = iHOS+1-j, j), indexed by j-1
@@ -329,7 +317,8 @@ __global__ void k_expon(const double* __restrict__ NL1, const double* __restrict
   if (i >= n) return;
   const double dt = sc[SC_DT];
   const double w = om[i];
-  const double c = cos(w * dt), s = sin(w * dt);
+  double s, c;
+  sincos(w * dt, &s, &c);
   const double a = NL1[i], b0 = NL2[i];
   const double b = b0 * w;
   kG1[i] = a * c - b * s;
@@ -762,7 +751,8 @@ __global__ void k_rk_out(const double* __restrict__ G1, const double* __restrict
   double e = 0.0;
   if (i < n) {
     const double w = om[i];
-    const double c = cos(-w * h), s = sin(-w * h);
+    double s, c;
+    sincos(-w * h, &s, &c);
     const double g1 = G1[i], g2 = G2[i];
     e = g1 * c - g2 * s;
     double p = g2 * c + g1 * s;
@@ -877,9 +867,12 @@ struct Enq {
   const Dev& d;
   const Tables& tb;
   double* const* tmp;
-  Enq(Ctx& cc, cudaStream_t s) : c(cc), st(s), P(cc.P), d(cc.d), tb(cc.tb), tmp(cc.d.xtmp) {}
-  Enq(Ctx& cc, cudaStream_t s, const Tables& t, double* const* tp)
-      : c(cc), st(s), P(cc.P), d(cc.d), tb(t), tmp(tp) {}
+  double* const* dt;  // temporaries of the truncated modes of dealiasing
+  int ndt;
+  Enq(Ctx& cc, cudaStream_t s)
+      : c(cc), st(s), P(cc.P), d(cc.d), tb(cc.tb), tmp(cc.d.xtmp), dt(cc.d.dtmp), ndt(Dev::kDealiasTmp) {}
+  Enq(Ctx& cc, cudaStream_t s, const Tables& t, double* const* tp, double* const* dtp, int nd)
+      : c(cc), st(s), P(cc.P), d(cc.d), tb(t), tmp(tp), dt(dtp), ndt(nd) {}
 
   long long nN() const { return (long long)P.n1 * P.n2; }
   long long nB() const { return (long long)P.nd1 * P.nd2; }
@@ -911,21 +904,48 @@ struct Enq {
   XfReq F2S_B(const double* in, int in_ld, int e1, int e2, double* out, int csx = 0, int csy = 0) const {
     return R(GRID_BIG, -1, csx, csy, in, in_ld, e1, e2, out, P.nd1, P.nd1, P.nd2);
   }
+  // the same request with its input multiplied by w[i1 + w_ld * i2]
+  static XfReq weighted(XfReq r, const double* w, int w_ld) {
+    r.win = w;
+    r.win_ld = w_ld;
+    return r;
+  }
   bool act_x(int order) const { return P.p1 != 1 && (order - 1) % (P.p1 - 1) == 0; }
   bool act_y(int order) const { return P.n2 != 1 && P.p2 != 1 && (order - 1) % (P.p2 - 1) == 0; }
   bool dealias_on(int order) const { return act_x(order) || act_y(order); }
-  // dealias (dealiasing.f90:39-92): S2F_big, truncate, F2S_big, in place
+  int dclass(int order) const { return (act_x(order) ? 1 : 0) | (act_y(order) ? 2 : 0); }
+  // dealias (dealiasing.f90:39-92): S2F_big, truncate, F2S_big, in place.
+  // cls bit 0 truncates x to n1 modes, bit 1 truncates y to n2 modes; the
+  // fields of one call are transformed together, ndt at a time.
+  void dealias_many(const std::vector<std::pair<int, double*>>& fields) {
+    std::vector<std::pair<int, double*>> f;
+    for (const auto& p : fields)
+      if (p.first != 0) f.push_back(p);
+    for (size_t s = 0; s < f.size(); s += ndt) {
+      const size_t e = std::min(f.size(), s + ndt);
+      std::vector<XfReq> fw, bw;
+      for (size_t i = s; i < e; ++i) {
+        const int e1 = (f[i].first & 1) ? P.n1 : P.nd1, e2 = (f[i].first & 2) ? P.n2 : P.nd2;
+        fw.push_back(R(GRID_BIG, 1, 0, 0, f[i].second, P.nd1, P.nd1, P.nd2, dt[i - s], P.nd1, e1, e2));
+        bw.push_back(F2S_B(dt[i - s], P.nd1, e1, e2, f[i].second));
+      }
+      xf(fw);
+      xf(bw);
+    }
+  }
   void dealias(int order, double* buf) {
     if (!dealias_on(order)) return;
-    const int e1 = act_x(order) ? P.n1 : P.nd1;
-    const int e2 = act_y(order) ? P.n2 : P.nd2;
-    xf({R(GRID_BIG, 1, 0, 0, buf, P.nd1, P.nd1, P.nd2, d.tbig3, P.nd1, e1, e2)});
-    xf({F2S_B(d.tbig3, P.nd1, e1, e2, buf)});
+    dealias_many({{dclass(order), buf}});
   }
   template <typename K, typename... A>
   void ew(K kern, long long n, A... a) {
     if (n <= 0) return;
     launch_pdl(kern, dim3(nblk(n)), dim3(kEW), 0, st, a...);
+  }
+  template <typename K, typename... A>
+  void ew_trig(K kern, long long n, A... a) {
+    if (n <= 0) return;
+    launch_pdl(kern, dim3(nblk(n, kTrig)), dim3(kTrig), 0, st, a...);
   }
 };
 
@@ -963,8 +983,8 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
 
   // 1. GtoF + volume correction of the mean mode
   {
-    const int nb = nblk(nN);
-    launch_pdl(k_gtof, dim3(nb), dim3(kEW), 0, st, G1, G2, d.omega, d.kx, d.ky, d.sc, n1, n2, P.igeom, P.d_hinge,
+    const int nb = nblk(nN, kTrig);
+    launch_pdl(k_gtof, dim3(nb), dim3(kTrig), 0, st, G1, G2, d.omega, d.kx, d.ky, d.sc, n1, n2, P.igeom, P.d_hinge,
                                P.xlen, d.etam, d.phim, d.w_eta_x, d.w_eta_y, d.w_phi_x, d.w_phi_y,
                                d.part, d.counter);
   }
@@ -973,7 +993,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   //    on the second stream with its own transform scratch and joins the
   //    main stream before assembly.
   cudaStream_t sw = c.st2;
-  Enq W(c, sw, c.tb2, d.xtmp2);
+  Enq W(c, sw, c.tb2, d.xtmp2, nullptr, 0);
   cudaEventRecord(c.ev_fork, st);
   cudaStreamWaitEvent(sw, c.ev_fork, 0);
   double* kA1 = k + L.off[S_AADD1];
@@ -1024,10 +1044,6 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   // 2. transform batch A: eta in space, eta / eta_x / eta_y / phis_x / phis_y on
   //    the big grid (phisxy_etaxy) and the order-1 HOS terms F2S_big(a1 kth_ext(j))
   {
-    ProdArgs pa{};
-    pa.count = M;
-    for (int j = 1; j <= M; ++j) { pa.out[j - 1] = d.prod[j - 1]; pa.jidx[j - 1] = j - 1; }
-    launch_pdl(k_prod_kth, dim3(nblk(nN)), dim3(kEW), 0, st, d.phim, n1, n1, n2, d.kth_ext, nd1, nd2, pa);
     std::vector<XfReq> rq;
     rq.push_back(E.F2S_N(d.etam, d.eta_sp));
     rq.push_back(E.F2S_B(d.etam, n1, n1, n2, d.etapm[0]));
@@ -1037,8 +1053,11 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
       rq.push_back(E.F2S_B(d.w_eta_y, n1, n1, n2, d.etay, 0, 1));
       rq.push_back(E.F2S_B(d.w_phi_y, n1, n1, n2, d.phisy, 0, 1));
     }
+    // F2S_big(phis_modes * kth_ext(j)): the products are taken as the
+    // transform reads its input
     for (int j = 1; j <= M; ++j)
-      rq.push_back(E.F2S_B(d.prod[j - 1], nd1, n1, n2, d.phizi[(0) * M + (j - 1)]));
+      rq.push_back(E.weighted(E.F2S_B(d.phim, n1, n1, n2, d.phizi[(0) * M + (j - 1)]),
+                              d.kth_ext + (long long)nd1 * nd2 * (j - 1), nd1));
     E.xf(rq);
     cudaEventRecord(c.ev_eta, st);
     if (n2 == 1) {
@@ -1086,25 +1105,38 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   W.xf({W.F2S_B(d.pmode[0], n1, n1, n2, d.pxe), W.F2S_B(d.pmode[1], n1, n1, n2, d.pye),
         W.F2S_B(d.pmode[2], n1, n1, n2, d.pze)});
   cudaEventRecord(c.ev_join, sw);
-  // 3. powers eta^j / j! with partial dealiasing: one kernel per run of
-  //    orders up to the next order that is dealiased
-  for (int j = 1; j < M;) {
-    int jend = j + 1;
-    while (jend < M && !E.dealias_on(jend)) ++jend;
-    PowArgs pa{};
-    for (int t = 0; t < M; ++t) pa.e[t] = d.etapm[t];
-    pa.j0 = j;
-    pa.j1 = jend;
-    E.ew(k_pow_run, nB, pa, nB);
-    E.dealias(jend, d.etapm[jend - 1]);
-    j = jend;
+  // 3. powers eta^j / j! with partial dealiasing (one kernel per run of
+  //    orders up to the next order that is dealiased) and |grad eta|^2.
+  //    Order 1 of the HOS recursion needs none of them, so they run on a
+  //    third stream and join before order 2.
+  {
+    cudaStream_t sp = c.st3;
+    Enq Pw(c, sp, c.tb3, d.xtmp3, &d.ptmp, 1);
+    cudaStreamWaitEvent(sp, c.ev_eta, 0);
+    for (int j = 1; j < M;) {
+      int jend = j + 1;
+      while (jend < M && !E.dealias_on(jend)) ++jend;
+      PowArgs pa{};
+      for (int t = 0; t < M; ++t) pa.e[t] = d.etapm[t];
+      pa.j0 = j;
+      pa.j1 = jend;
+      Pw.ew(k_pow_run, nB, pa, nB);
+      Pw.dealias(jend, d.etapm[jend - 1]);
+      j = jend;
+    }
+    Pw.ew(k_sq2, nB, (const double*)d.etax, (const double*)d.etay, d.gradeta2, nB);
+    Pw.dealias(2, d.gradeta2);
+    cudaEventRecord(c.ev_pow, sp);
   }
-  E.ew(k_sq2, nB, (const double*)d.etax, (const double*)d.etay, d.gradeta2, nB);
-  E.dealias(2, d.gradeta2);
+  bool pow_joined = false;
 
   // 4. HOS recursion (HOSphis_modes)
   std::vector<int> ext1(M + 2, nd1), ext2(M + 2, nd2);
   for (int iHOS = 1; iHOS <= M; ++iHOS) {
+    if (iHOS == 2) {
+      cudaStreamWaitEvent(st, c.ev_pow, 0);
+      pow_joined = true;
+    }
     AccArgs aa{};
     aa.iHOS = iHOS;
     for (int j = 1; j <= iHOS; ++j) {
@@ -1121,18 +1153,15 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
       ext1[o] = e1;
       ext2[o] = e2;
       E.xf({E.R(GRID_BIG, 1, 0, 0, d.phimext, nd1, nd1, nd2, d.aHOS[o], nd1, e1, e2)});
-      // products with kth_ext(j), j = 1 .. M+1-o, then their F2S_big
-      ProdArgs pa{};
-      pa.count = M + 1 - o;
-      for (int j = 1; j <= pa.count; ++j) { pa.out[j - 1] = d.prod[j - 1]; pa.jidx[j - 1] = j - 1; }
-      launch_pdl(k_prod_kth, dim3(nblk((long long)e1 * e2)), dim3(kEW), 0, st, d.aHOS[o], nd1, e1, e2, d.kth_ext, nd1,
-                                                          nd2, pa);
+      // F2S_big of the products with kth_ext(j), j = 1 .. M+1-o
       std::vector<XfReq> rq;
-      for (int j = 1; j <= pa.count; ++j)
-        rq.push_back(E.F2S_B(d.prod[j - 1], nd1, e1, e2, d.phizi[(o - 1) * M + (j - 1)]));
+      for (int j = 1; j <= M + 1 - o; ++j)
+        rq.push_back(E.weighted(E.F2S_B(d.aHOS[o], nd1, e1, e2, d.phizi[(o - 1) * M + (j - 1)]),
+                                d.kth_ext + (long long)nd1 * nd2 * (j - 1), nd1));
       E.xf(rq);
     }
   }
+  if (!pow_joined) cudaStreamWaitEvent(st, c.ev_pow, 0);
   // Quadratic terms of HOSphis_modes (resol_HOS.f90:797-905): every term is
   // dealiased at its order; dealiasing is linear, so terms are summed per
   // dealiasing class first (class = which directions the order truncates).
@@ -1178,18 +1207,17 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   aa.ng1 = aa.ng2 = aa.nt1 = 0;
   if (gt.ngroup > 0) {
     E.ew(k_group_products, nB, gt, nB);
-    auto dealias_class = [&](int c, double* buf) {
-      if (c == 0) return;
-      const int e1 = (c & 1) ? n1 : nd1, e2 = (c & 2) ? n2 : nd2;
-      E.xf({E.R(GRID_BIG, 1, 0, 0, buf, nd1, nd1, nd2, d.tbig3, nd1, e1, e2)});
-      E.xf({E.F2S_B(d.tbig3, nd1, e1, e2, buf)});
-    };
-    for (int g = 0; g < gt.ngroup; ++g) dealias_class(gc1[g], d.grp[g]);
+    {
+      std::vector<std::pair<int, double*>> dl;
+      for (int g = 0; g < gt.ngroup; ++g) dl.push_back({gc1[g], d.grp[g]});
+      E.dealias_many(dl);
+    }
     for (int g = 0; g < gt.ngroup; ++g) {
       if (gkind[g] == 0) aa.g1[aa.ng1++] = d.grp[g];
       else aa.t1[aa.nt1++] = d.grp[g];
     }
     // geta2phiz2: gradeta2 times the kind-2 groups, dealiased by outer class
+    std::vector<std::pair<int, double*>> dl2;
     int nu_ = 0;
     for (int c2 = 0; c2 < 4; ++c2) {
       SumArgs sa{};
@@ -1200,10 +1228,11 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
       sa.scale = d.gradeta2;
       sa.out = d.grp[gt.ngroup + nu_];
       E.ew(k_sum_fields, nB, sa, nB);
-      dealias_class(c2, sa.out);
+      dl2.push_back({c2, sa.out});
       aa.g2[aa.ng2++] = sa.out;
       nu_++;
     }
+    E.dealias_many(dl2);
   }
 
   // 7. free-surface terms, filters to the n grid, final RHS
@@ -1213,8 +1242,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   if (E.dealias_on(2)) {
     E.ew(k_fs_products, nB, (const double*)d.etax, (const double*)d.etay, (const double*)d.phisx,
          (const double*)d.phisy, d.tbig, d.tbig2, nB);
-    E.dealias(2, d.tbig);
-    E.dealias(2, d.tbig2);
+    E.dealias_many({{E.dclass(2), d.tbig}, {E.dclass(2), d.tbig2}});
     aa.detext = d.tbig;
     aa.dphext = d.tbig2;
   }
@@ -1233,7 +1261,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
        (const double*)d.phiz_add, (const double*)d.phit_add, (const double*)d.nu, d.det, d.dph, nN,
        M);
   E.xf({E.S2F_N(d.det, d.NL1), E.S2F_N(d.dph, d.NL2)});
-  E.ew(k_expon, nN, (const double*)d.NL1, (const double*)d.NL2, (const double*)d.omega,
+  E.ew_trig(k_expon, nN, (const double*)d.NL1, (const double*)d.NL2, (const double*)d.omega,
        (const double*)d.sc, kG1, kG2, nN, rk_mode ? 1 : 0);
 }
 
@@ -1277,7 +1305,7 @@ void enqueue_step(Ctx& c, cudaStream_t st) {
   const int nb = nblk(S);
   launch_pdl(k_rk_final, dim3(nb), dim3(kEW), 0, st, d.y0, fa, d.sc, d.ynew, d.part, S);
   launch_pdl(k_rk_err, dim3(1), dim3(32), 0, st, d.part, nb, d.sc);
-  launch_pdl(k_rk_out, dim3(nblk(nN)), dim3(kEW), 0, st, d.ynew + L.off[S_G1], d.ynew + L.off[S_G2],
+  launch_pdl(k_rk_out, dim3(nblk(nN, kTrig)), dim3(kTrig), 0, st, d.ynew + L.off[S_G1], d.ynew + L.off[S_G2],
                                      d.k[4] + L.off[S_G1], d.k[4] + L.off[S_G2], d.omega, d.sc,
                                      (int)nN, P.igeom, P.d_hinge, P.xlen, d.etam, d.phim, d.NL1,
                                      d.part + 10 * (long long)nb, d.counter);

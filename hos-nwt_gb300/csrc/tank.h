@@ -72,10 +72,10 @@ struct Dev {
   double *X1 = nullptr, *X2 = nullptr, *X3 = nullptr, *det = nullptr, *dph = nullptr;
   double *NL1 = nullptr, *NL2 = nullptr;
   // big grid
-  std::vector<double*> etapm, phizm, aHOS, prod;
+  std::vector<double*> etapm, phizm, aHOS;
   std::vector<double*> phizi;   // (m, j) packed
   double *etax = nullptr, *etay = nullptr, *phisx = nullptr, *phisy = nullptr, *gradeta2 = nullptr;
-  double *phimext = nullptr, *phizMm1 = nullptr, *tbig = nullptr, *tbig2 = nullptr, *tbig3 = nullptr;
+  double *phimext = nullptr, *phizMm1 = nullptr, *tbig = nullptr, *tbig2 = nullptr;
   double *pxe = nullptr, *pye = nullptr, *pze = nullptr, *A1 = nullptr, *A3 = nullptr;
   double *t1 = nullptr, *geta2phiz = nullptr, *geta2phiz2 = nullptr;
   double* grp[24] = {};         // dealiasing groups of the quadratic terms
@@ -86,6 +86,10 @@ struct Dev {
   // transform temporaries
   double *xtmp[kMaxJobs] = {};
   double *xtmp2[kMaxJobs] = {};  // temporaries of the wavemaker branch
+  double *xtmp3[kMaxJobs] = {};  // temporaries of the eta-power branch
+  static constexpr int kDealiasTmp = 8;
+  double *dtmp[kDealiasTmp] = {};  // truncated modes of batched dealiasing (main stream)
+  double *ptmp = nullptr;          // truncated modes of the eta-power dealiasing
   // scalars and reductions
   double *sc = nullptr;
   double *part = nullptr;       // partial sums / maxima
@@ -110,9 +114,11 @@ struct Ctx {
   Dev d{};
   Tables tb{};
   Tables tb2{};                   // transform scratch of the wavemaker branch
+  Tables tb3{};                   // transform scratch of the eta-power branch
   cudaStream_t st = nullptr;
   cudaStream_t st2 = nullptr;     // wavemaker branch of each right-hand side
-  cudaEvent_t ev_fork = nullptr, ev_eta = nullptr, ev_join = nullptr;
+  cudaStream_t st3 = nullptr;     // eta powers and |grad eta|^2 with their dealiasing
+  cudaEvent_t ev_fork = nullptr, ev_eta = nullptr, ev_join = nullptr, ev_pow = nullptr;
   cudaGraphExec_t step_graph = nullptr;
   double time_cur = 0.0;
   int endramp = 0;

@@ -31,6 +31,13 @@ __device__ __forceinline__ int mod4d(long long v, int D4) {
   return (int)(r < 0 ? r + D4 : r);
 }
 
+// input j of a first-pass line, times the optional weight
+__device__ __forceinline__ double in_at(const double* __restrict__ x, long long sk,
+                                       const double* __restrict__ w, int j) {
+  const double v = __ldg(x + (long long)j * sk);
+  return w ? v * __ldg(w + j) : v;
+}
+
 constexpr int kXThreads = 256;   // 8 warps
 constexpr int kXWarps = kXThreads / 32;
 constexpr int kMaxPairChunk = 1024;  // staged terms per CTA
@@ -71,6 +78,7 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b
   const int inc = mod4d((long long)J.aj * kk, D4);
   const bool lane_on = k < J.nlane;
   const long long sk = J.in_sk;
+  const double* __restrict__ wr = J.win ? J.win + (long long)line * J.win_sl : nullptr;
 
   double* q = smem;                    // D + 1 table entries
   double* su = smem + (D + 1);         // staged inputs (or u)
@@ -87,13 +95,13 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b
     if (J.mode == 2) {
       for (int t = threadIdx.x; t < sb - sa; t += kXThreads) {
         const int j = sa + t;
-        const double xa = __ldg(x + (long long)j * sk);
-        const double xb = __ldg(x + (long long)(D - j) * sk);
+        const double xa = in_at(x, sk, wr, j);
+        const double xb = in_at(x, sk, wr, D - j);
         su[t] = xa + xb;
         sv[t] = xa - xb;
       }
     } else {
-      for (int t = threadIdx.x; t < sb - sa; t += kXThreads) su[t] = __ldg(x + (long long)(sa + t) * sk);
+      for (int t = threadIdx.x; t < sb - sa; t += kXThreads) su[t] = in_at(x, sk, wr, sa + t);
     }
     __syncthreads();
     const int len = sb - sa;
@@ -148,7 +156,7 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b
     const int j_end = min(J.jhi, J.nin);
     if (J.mode == 2) {
       if (J.jlo == 0) {  // pair (0, D) with the end weight
-        const double xa = __ldg(x), xb = __ldg(x + (long long)D * sk);
+        const double xa = in_at(x, sk, wr, 0), xb = in_at(x, sk, wr, D);
         const double t = ((k & 1) == 0) ? xa + xb : xa - xb;
         e = fma(J.w0 * t, twiddle_s(q, D, mod4d((long long)J.bj * kk + J.off, D4)), e);
       }
@@ -156,18 +164,18 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b
         const int jm = D / 2;
         if (jm >= J.jlo && jm < J.jhi && jm > 0) {
           const int mm = mod4d((long long)(J.aj * jm + J.bj) * kk + J.off, D4);
-          e = fma(J.wm * __ldg(x + (long long)jm * sk), twiddle_s(q, D, mm), e);
+          e = fma(J.wm * in_at(x, sk, wr, jm), twiddle_s(q, D, mm), e);
         }
       }
     } else {
       if (J.jlo == 0 && 0 < j_end) {
         const int mm = mod4d((long long)J.bj * kk + J.off, D4);
-        e = fma(J.w0 * __ldg(x), twiddle_s(q, D, mm), e);
+        e = fma(J.w0 * in_at(x, sk, wr, 0), twiddle_s(q, D, mm), e);
       }
       const int jl = J.N - 1;
       if (jl > 0 && jl >= J.jlo && jl < j_end) {
         const int mm = mod4d((long long)(J.aj * jl + J.bj) * kk + J.off, D4);
-        const double t = J.wl * __ldg(x + (long long)jl * sk) * twiddle_s(q, D, mm);
+        const double t = J.wl * in_at(x, sk, wr, jl) * twiddle_s(q, D, mm);
         if (J.mode == 1 && (jl & 1)) o += t;
         else e += t;
       }
@@ -324,6 +332,7 @@ __global__ void __launch_bounds__(kTThreads) two_level_pass1(const AxisBatch b) 
   const int j2 = on ? t / (J.A + 1) : 0, kp = on ? t - j2 * (J.A + 1) : 0;
   const int D = J.D, D4 = 4 * D;
   const double* __restrict__ x = J.in + (long long)line * J.in_sl;
+  const double* __restrict__ wr = J.win ? J.win + (long long)line * J.win_sl : nullptr;
   const int j_end = on ? min(J.jhi, J.nin) : 0;  // terms j in [jlo, j_end)
   // cos(pi j1 kp / A) = cos(pi * 2 B j1 kp / (2D)): table step 2 B kp per j1
   const unsigned d4 = (unsigned)D4;
@@ -335,7 +344,7 @@ __global__ void __launch_bounds__(kTThreads) two_level_pass1(const AxisBatch b) 
   for (int j = j2 + sub * J.B; j < j_end; j += SPLIT * J.B) {
     if (j >= J.jlo) {
       const double w = (j == 0) ? J.w0 : ((j == J.N - 1) ? J.wl : J.wm);
-      const double v = w * __ldg(x + (long long)j * J.in_sk);
+      const double v = w * in_at(x, J.in_sk, wr, j);
       c = fma(v, twiddle(J.q, D, m), c);
       int ms = m - D;
       if (ms < 0) ms += D4;
@@ -485,8 +494,17 @@ void pick_factors(int D, int nin, int nout, int* Aout, int* Bout) {
   }
 }
 
+// Lanes per output: enough threads to fill the GPU (about 1024 per SM), no
+// more lanes than terms, at most a warp.
+int pick_split(long long outputs, int terms, int nsm) {
+  const long long target = 1024LL * std::max(nsm, 1);
+  int split = 1;
+  while (split < 32 && outputs * split < target && 2 * split <= std::max(terms, 1)) split *= 2;
+  return split;
+}
+
 template <int SPLIT>
-void launch_two_level_split(AxisBatch& b, cudaStream_t st) {
+void launch_pass1(AxisBatch& b, cudaStream_t st) {
   constexpr int kOut = kTThreads / SPLIT;
   int total = 0;
   for (int i = 0; i < b.njobs; ++i) {
@@ -495,7 +513,12 @@ void launch_two_level_split(AxisBatch& b, cudaStream_t st) {
   }
   b.start[b.njobs] = total;
   if (total > 0) launch_pdl(two_level_pass1<SPLIT>, dim3(total), dim3(kTThreads), 0, st, b);
-  total = 0;
+}
+
+template <int SPLIT>
+void launch_pass2(AxisBatch& b, cudaStream_t st) {
+  constexpr int kOut = kTThreads / SPLIT;
+  int total = 0;
   for (int i = 0; i < b.njobs; ++i) {
     b.start[i] = total;
     total += b.job[i].nlines * ((b.job[i].nout + kOut - 1) / kOut);
@@ -504,11 +527,32 @@ void launch_two_level_split(AxisBatch& b, cudaStream_t st) {
   if (total > 0) launch_pdl(two_level_pass2<SPLIT>, dim3(total), dim3(kTThreads), 0, st, b);
 }
 
-void launch_two_level(AxisBatch& b, cudaStream_t st) {
-  long long outputs = 0;
-  for (int i = 0; i < b.njobs; ++i) outputs += (long long)b.job[i].nlines * b.job[i].nout;
-  if (outputs < 65536) launch_two_level_split<32>(b, st);
-  else launch_two_level_split<8>(b, st);
+template <template <int> class F>
+void with_split(int split, AxisBatch& b, cudaStream_t st) {
+  switch (split) {
+    case 1: F<1>::run(b, st); break;
+    case 2: F<2>::run(b, st); break;
+    case 4: F<4>::run(b, st); break;
+    case 8: F<8>::run(b, st); break;
+    case 16: F<16>::run(b, st); break;
+    default: F<32>::run(b, st); break;
+  }
+}
+template <int S> struct Pass1 { static void run(AxisBatch& b, cudaStream_t st) { launch_pass1<S>(b, st); } };
+template <int S> struct Pass2 { static void run(AxisBatch& b, cudaStream_t st) { launch_pass2<S>(b, st); } };
+
+void launch_two_level(AxisBatch& b, int nsm, cudaStream_t st) {
+  long long out1 = 0, out2 = 0;
+  int terms1 = 0, terms2 = 0;
+  for (int i = 0; i < b.njobs; ++i) {
+    const AxisJob& J = b.job[i];
+    out1 += (long long)J.nlines * J.B * (J.A + 1);
+    out2 += (long long)J.nlines * J.nout;
+    terms1 = std::max(terms1, (std::min(J.jhi, J.nin) + J.B - 1) / J.B);
+    terms2 = std::max(terms2, J.B);
+  }
+  with_split<Pass1>(pick_split(out1, terms1, nsm), b, st);
+  with_split<Pass2>(pick_split(out2, terms2, nsm), b, st);
 }
 
 // Decide the symmetry mode and the split of every x-pass job, then launch.
@@ -627,6 +671,8 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
     X.in = R.in;
     X.in_sk = 1;
     X.in_sl = R.in_ld;
+    X.win = R.win;
+    X.win_sl = R.win_ld;
     X.nin = R.nin1;
     X.gscale = twod ? 1.0 : R.scale;
     if (twod) {
@@ -683,7 +729,7 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
     }
     bd.job[bd.njobs++] = J;
   }
-  if (b2.njobs) launch_two_level(b2, st);
+  if (b2.njobs) launch_two_level(b2, tb.nsm, st);
   if (bd.njobs) launch_batch_x(bd, tb, st);
   if (by.njobs) launch_batch_y(by, st);
 }
