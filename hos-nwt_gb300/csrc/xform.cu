@@ -304,114 +304,219 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
 // through k mod 2A (C even, S odd about A).  Pass 1 computes C, S for
 // k' = 0..A; pass 2 combines them.  Work: 2 (A+1) nin + 2 B nout FMAs
 // instead of about nin * nout / 2 for the direct sum.
-constexpr int kTThreads = 256;
+//
+// Both passes first issue all of their global loads (inputs, partial sums
+// and twiddles staged in shared memory), then run FMA loops over shared
+// memory: one round trip to L2 per pass instead of a chain of dependent
+// scattered loads.
+constexpr int kP1Threads = 128;
+constexpr int kP2Threads = 128;  // 4 warps split the j2 sum of 32 outputs
+constexpr int kP2Warps = kP2Threads / 32;
 
-template <int SPLIT>
-__device__ __forceinline__ double group_sum(double v) {
-#pragma unroll
-  for (int o = SPLIT / 2; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o, SPLIT);
+// Thread-block clusters: a sum too long for one SM is split over the CTAs of
+// a cluster, whose partial results are combined through distributed shared
+// memory by rank 0 in rank order.
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" :::
+                   "memory");
+}
+__device__ __forceinline__ double ld_cluster(const double* local, unsigned rank) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(local);
+  unsigned ra;
+  double v;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(ra) : "memory");
   return v;
 }
 
-// SPLIT lanes share one output's sum (8 when there are many outputs, 32 for
-// small launches so that enough warps hide the load latency)
-template <int SPLIT>
-__global__ void __launch_bounds__(kTThreads) two_level_pass1(const AxisBatch b) {
+// pass 1: cluster = (job, line, group of kpc consecutive k'); CTA r of the
+// cluster sums j1 in its slice of [0, K).  Threads own (k', part, j2) items
+// with j2 fastest: staged inputs are read without bank conflicts and the j1
+// twiddles are broadcast.
+__global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatch b, int kpc, int ncl) {
   pdl_wait();
-  constexpr int kOut = kTThreads / SPLIT;
+  extern __shared__ double sm1[];
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const AxisJob& J = b.job[jb];
-  const int nout1 = J.B * (J.A + 1);
-  const int per_line = (nout1 + kOut - 1) / kOut;
-  const int local = blockIdx.x - b.start[jb];
-  const int line = local / per_line;
-  const int sub = threadIdx.x % SPLIT;
-  const int t = (local - line * per_line) * kOut + threadIdx.x / SPLIT;
-  const bool on = t < nout1;
-  const int j2 = on ? t / (J.A + 1) : 0, kp = on ? t - j2 * (J.A + 1) : 0;
-  const int D = J.D, D4 = 4 * D;
+  const int A = J.A, B = J.B, D = J.D, D4 = 4 * D;
+  const int ngrp = (A + 1 + kpc - 1) / kpc;
+  const int local = (blockIdx.x - b.start[jb]) / ncl;
+  const unsigned rank = ncl > 1 ? cluster_rank() : 0u;
+  const int line = local / ngrp;
+  const int kp0 = (local - line * ngrp) * kpc;
+  const int nkp = min(kpc, A + 1 - kp0);
+  const int j_end = min(J.jhi, J.nin);  // terms j in [jlo, j_end)
+  const int K = (j_end + B - 1) / B;
+  const int Kc = (K + ncl - 1) / ncl;
+  const int ja1 = min(K, (int)rank * Kc), Kl = min(K, ja1 + Kc) - ja1;
+  double* fin = sm1;                // kpc * B (C, S) of this CTA's slice
+  double* xs = fin + 2 * kpc * B;   // Kl * B weighted inputs, zero outside the sum
+  double* tc = xs + Kc * B;         // kpc * Kc cos(pi j1 k' / A)
+  double* ts = tc + kpc * Kc;       // kpc * Kc sin(pi j1 k' / A)
+  double* red = ts + kpc * Kc;      // partial sums of the items
   const double* __restrict__ x = J.in + (long long)line * J.in_sl;
   const double* __restrict__ wr = J.win ? J.win + (long long)line * J.win_sl : nullptr;
-  const int j_end = on ? min(J.jhi, J.nin) : 0;  // terms j in [jlo, j_end)
-  // cos(pi j1 kp / A) = cos(pi * 2 B j1 kp / (2D)): table step 2 B kp per j1
-  const unsigned d4 = (unsigned)D4;
-  const unsigned step1 = (2u * (unsigned)J.B * (unsigned)kp) % d4;
-  const int inc = (int)((step1 * (unsigned)SPLIT) % d4);
-  int m = (int)((step1 * (unsigned)sub) % d4);
-  double c = 0.0, s = 0.0;
-#pragma unroll 2
-  for (int j = j2 + sub * J.B; j < j_end; j += SPLIT * J.B) {
-    if (j >= J.jlo) {
+  for (int t = threadIdx.x; t < Kl * B; t += kP1Threads) {
+    const int j = ja1 * B + t;
+    double v = 0.0;
+    if (j >= J.jlo && j < j_end) {
       const double w = (j == 0) ? J.w0 : ((j == J.N - 1) ? J.wl : J.wm);
-      const double v = w * in_at(x, J.in_sk, wr, j);
-      c = fma(v, twiddle(J.q, D, m), c);
-      int ms = m - D;
-      if (ms < 0) ms += D4;
-      s = fma(v, twiddle(J.q, D, ms), s);
+      v = w * in_at(x, J.in_sk, wr, j);
     }
-    m += inc;
-    if (m >= D4) m -= D4;
+    xs[t] = v;
   }
-  c = group_sum<SPLIT>(c);
-  s = group_sum<SPLIT>(s);
-  if (on && sub == 0) {
-    double* cs = J.cs + (((long long)line * J.B + j2) * (J.A + 1) + kp) * 2;
-    cs[0] = c;
-    cs[1] = s;
+  for (int t = threadIdx.x; t < nkp * Kl; t += kP1Threads) {
+    const int kpl = t / Kl, j1 = ja1 + t - kpl * Kl;
+    // pi j1 k' / A = pi (2 B j1 k') / (2 D); both factors below 4D
+    const unsigned step = (2u * (unsigned)B * (unsigned)(kp0 + kpl)) % (unsigned)D4;
+    const int m = (int)((step * (unsigned)j1) % (unsigned)D4);
+    tc[kpl * Kc + j1 - ja1] = twiddle(J.q, D, m);
+    ts[kpl * Kc + j1 - ja1] = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
   }
+  __syncthreads();
+  const int P = max(1, kP1Threads / (nkp * B));  // parts splitting the j1 sum
+  const int nitem = nkp * P * B;
+  for (int it = threadIdx.x; it < nitem; it += kP1Threads) {
+    const int j2 = it % B, r = it / B;
+    const int part = r % P, kpl = r / P;
+    const double* tcp = tc + kpl * Kc;
+    const double* tsp = ts + kpl * Kc;
+    double c = 0.0, s = 0.0;
+#pragma unroll 4
+    for (int j1 = part; j1 < Kl; j1 += P) {
+      const double v = xs[j1 * B + j2];
+      c = fma(v, tcp[j1], c);
+      s = fma(v, tsp[j1], s);
+    }
+    red[2 * it] = c;
+    red[2 * it + 1] = s;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nkp * B; t += kP1Threads) {
+    const int j2 = t % B, kpl = t / B;
+    double c = 0.0, s = 0.0;
+    for (int part = 0; part < P; ++part) {
+      const int it = (kpl * P + part) * B + j2;
+      c += red[2 * it];
+      s += red[2 * it + 1];
+    }
+    fin[2 * t] = c;
+    fin[2 * t + 1] = s;
+  }
+  if (ncl > 1) cluster_sync_all();
+  else __syncthreads();
+  if (rank == 0) {
+    for (int t = threadIdx.x; t < nkp * B; t += kP1Threads) {
+      double c = fin[2 * t], s = fin[2 * t + 1];
+      for (int r = 1; r < ncl; ++r) {
+        c += ld_cluster(fin + 2 * t, (unsigned)r);
+        s += ld_cluster(fin + 2 * t + 1, (unsigned)r);
+      }
+      const int j2 = t % B, kpl = t / B;
+      double* cs = J.cs + (((long long)line * B + j2) * (A + 1) + kp0 + kpl) * 2;
+      cs[0] = c;
+      cs[1] = s;
+    }
+  }
+  if (ncl > 1) cluster_sync_all();  // remote reads done before any CTA exits
 }
 
-template <int SPLIT>
-__global__ void __launch_bounds__(kTThreads) two_level_pass2(const AxisBatch b) {
+// pass 2: cluster = (job, line, 32 outputs); CTA r of the cluster sums j2 in
+// its slice of [0, B).  The slice's twiddles cos/sin(pi j2 k / D) are staged
+// first; lanes own outputs (their C, S loads are contiguous), warps split
+// the slice and are combined in a fixed order.
+__global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatch b, int ncl) {
   pdl_wait();
-  constexpr int kOut = kTThreads / SPLIT;
+  extern __shared__ double sm2[];
+  __shared__ double red[kP2Warps][32];
+  __shared__ double fin[32];
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const AxisJob& J = b.job[jb];
-  const int per_line = (J.nout + kOut - 1) / kOut;
-  const int local = blockIdx.x - b.start[jb];
-  const int line = local / per_line;
-  const int sub = threadIdx.x % SPLIT;
-  const int k = (local - line * per_line) * kOut + threadIdx.x / SPLIT;
+  const int A = J.A, B = J.B, D = J.D, D4 = 4 * D;
+  const int nkb = (J.nout + 31) / 32;
+  const int local = (blockIdx.x - b.start[jb]) / ncl;
+  const unsigned rank = ncl > 1 ? cluster_rank() : 0u;
+  const int line = local / nkb;
+  const int k0 = (local - line * nkb) * 32;
+  const int Bc = (B + ncl - 1) / ncl;
+  const int ja2 = min(B, (int)rank * Bc), Bl = min(B, ja2 + Bc) - ja2;
+  for (int t = threadIdx.x; t < Bl * 32; t += kP2Threads) {
+    const int j2 = ja2 + (t >> 5), k = k0 + (t & 31);
+    // pi j2 k / D; j2 < D and k < N, so 2 j2 k fits in 32 bits for N < 32768
+    const int m = (int)((2u * (unsigned)j2 * (unsigned)k) % (unsigned)D4);
+    sm2[2 * t] = twiddle(J.q, D, m);
+    sm2[2 * t + 1] = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int k = k0 + lane;
   const bool on = k < J.nout && k >= J.klo && k < J.khi;
-  const int D = J.D, D4 = 4 * D, A = J.A;
-  int kp = on ? k % (2 * A) : 0;
+  int kp = k % (2 * A);
   double ssign = 1.0;
   if (kp > A) {
     kp = 2 * A - kp;
     ssign = -1.0;
   }
   const bool is_sin = (J.off != 0);
-  const double* cs = J.cs + ((long long)line * J.B * (A + 1) + kp) * 2;
-  const unsigned d4 = (unsigned)D4;
-  const unsigned step2 = on ? (2u * (unsigned)k) % d4 : 0u;
-  const int inc = (int)((step2 * (unsigned)SPLIT) % d4);
-  int m = (int)((step2 * (unsigned)sub) % d4);
+  const double* cs = J.cs + ((long long)line * B * (A + 1) + kp) * 2;
+  // C, S of this lane's j2 terms, loaded before the twiddles are needed
+  constexpr int kMaxOwn = 16;
+  double Cv[kMaxOwn], Sv[kMaxOwn];
+  const int nown = on ? min(kMaxOwn, (Bl - warp + kP2Warps - 1) / kP2Warps) : 0;
+#pragma unroll
+  for (int i = 0; i < kMaxOwn; ++i) {
+    if (i < nown) {
+      const long long o = (long long)(ja2 + warp + i * kP2Warps) * (A + 1) * 2;
+      Cv[i] = __ldcg(cs + o);
+      Sv[i] = __ldcg(cs + o + 1);
+    }
+  }
+  __syncthreads();
   double acc = 0.0;
-  const int jz = on ? J.B : 0;
-#pragma unroll 2
-  for (int j2 = sub; j2 < jz; j2 += SPLIT) {
-    const double C = __ldg(cs + (long long)j2 * (A + 1) * 2);
-    const double S = ssign * __ldg(cs + (long long)j2 * (A + 1) * 2 + 1);
-    const double cw = twiddle(J.q, D, m);
-    int ms = m - D;
-    if (ms < 0) ms += D4;
-    const double sw = twiddle(J.q, D, ms);
-    if (is_sin) acc = fma(cw, S, fma(sw, C, acc));
-    else acc = fma(cw, C, fma(-sw, S, acc));
-    m += inc;
-    if (m >= D4) m -= D4;
+#pragma unroll
+  for (int i = 0; i < kMaxOwn; ++i) {
+    if (i < nown) {
+      const int t = warp + i * kP2Warps;  // j2 - ja2
+      const double cw = sm2[2 * (t * 32 + lane)], sw = sm2[2 * (t * 32 + lane) + 1];
+      const double S = ssign * Sv[i];
+      if (is_sin) acc = fma(cw, S, fma(sw, Cv[i], acc));
+      else acc = fma(cw, Cv[i], fma(-sw, S, acc));
+    }
   }
-  acc = group_sum<SPLIT>(acc);
-  if (sub != 0 || k >= J.nout) return;
-  double* out = J.out + (long long)line * J.out_sl + (long long)k * J.out_sk;
-  if (!on) {
-    *out = 0.0;
-    return;
+  // j2 beyond the register-held terms
+  if (on) {
+    for (int t = warp + kMaxOwn * kP2Warps; t < Bl; t += kP2Warps) {
+      const long long o = (long long)(ja2 + t) * (A + 1) * 2;
+      const double cw = sm2[2 * (t * 32 + lane)], sw = sm2[2 * (t * 32 + lane) + 1];
+      const double C = __ldcg(cs + o), S = ssign * __ldcg(cs + o + 1);
+      if (is_sin) acc = fma(cw, S, fma(sw, C, acc));
+      else acc = fma(cw, C, fma(-sw, S, acc));
+    }
   }
-  const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
-  *out = acc * sc * J.gscale;
+  red[warp][lane] = acc;
+  __syncthreads();
+  if (warp == 0) {
+    double y = 0.0;
+#pragma unroll
+    for (int w = 0; w < kP2Warps; ++w) y += red[w][lane];
+    fin[lane] = y;
+  }
+  if (ncl > 1) cluster_sync_all();
+  else __syncthreads();
+  if (rank == 0 && warp == 0 && k < J.nout) {
+    double y = fin[lane];
+    for (int r = 1; r < ncl; ++r) y += ld_cluster(fin + lane, (unsigned)r);
+    double* out = J.out + (long long)line * J.out_sl + (long long)k * J.out_sk;
+    const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
+    *out = on ? y * sc * J.gscale : 0.0;
+  }
+  if (ncl > 1) cluster_sync_all();  // remote reads done before any CTA exits
 }
 
 // Fill the kind-dependent parameters of a pass.
@@ -484,7 +589,7 @@ void pick_factors(int D, int nin, int nout, int* Aout, int* Bout) {
   for (int A = 2; A <= D / 2; ++A) {
     if (D % A) continue;
     const int B = D / A;
-    if (B < 2) continue;
+    if (B < 2 || B > 256) continue;  // pass 2 stages B x 32 twiddle pairs
     const double cost = 2.0 * (A + 1) * (double)nin + 2.0 * B * (double)nout;
     if (cost < best) {
       best = cost;
@@ -494,65 +599,81 @@ void pick_factors(int D, int nin, int nout, int* Aout, int* Bout) {
   }
 }
 
-// Lanes per output: enough threads to fill the GPU (about 1024 per SM), no
-// more lanes than terms, at most a warp.
-int pick_split(long long outputs, int terms, int nsm) {
-  const long long target = 1024LL * std::max(nsm, 1);
-  int split = 1;
-  while (split < 32 && outputs * split < target && 2 * split <= std::max(terms, 1)) split *= 2;
-  return split;
+// Shared memory of pass 1 for a job with kpc values of k' per cluster and
+// ncl CTAs per cluster, and of pass 2 with ncl CTAs per cluster.
+size_t pass1_smem(const AxisJob& J, int kpc, int ncl) {
+  const int j_end = std::min(J.jhi, J.nin);
+  const int K = (j_end + J.B - 1) / J.B;
+  const int Kc = (K + ncl - 1) / ncl;
+  const int nkp = std::min(kpc, J.A + 1);
+  const int items = std::max(kP1Threads, nkp * J.B);
+  return sizeof(double) *
+         (2 * (size_t)kpc * J.B + (size_t)Kc * J.B + 2 * (size_t)kpc * Kc + 2 * (size_t)items);
+}
+size_t pass2_smem(const AxisJob& J, int ncl) {
+  return sizeof(double) * 2 * 32 * (size_t)((J.B + ncl - 1) / ncl);
 }
 
-template <int SPLIT>
-void launch_pass1(AxisBatch& b, cudaStream_t st) {
-  constexpr int kOut = kTThreads / SPLIT;
-  int total = 0;
-  for (int i = 0; i < b.njobs; ++i) {
-    b.start[i] = total;
-    total += b.job[i].nlines * ((b.job[i].B * (b.job[i].A + 1) + kOut - 1) / kOut);
-  }
-  b.start[b.njobs] = total;
-  if (total > 0) launch_pdl(two_level_pass1<SPLIT>, dim3(total), dim3(kTThreads), 0, st, b);
+// Cluster size: the smallest power of two (at most 8) that gives about
+// four CTAs per SM, and no more CTAs than slices of `terms` work.
+int pick_cluster(long long units, int terms, int nsm) {
+  int ncl = 1;
+  while (ncl < 8 && units * ncl < 4LL * std::max(nsm, 1) && 2 * ncl * 4 <= terms) ncl *= 2;
+  return ncl;
 }
-
-template <int SPLIT>
-void launch_pass2(AxisBatch& b, cudaStream_t st) {
-  constexpr int kOut = kTThreads / SPLIT;
-  int total = 0;
-  for (int i = 0; i < b.njobs; ++i) {
-    b.start[i] = total;
-    total += b.job[i].nlines * ((b.job[i].nout + kOut - 1) / kOut);
-  }
-  b.start[b.njobs] = total;
-  if (total > 0) launch_pdl(two_level_pass2<SPLIT>, dim3(total), dim3(kTThreads), 0, st, b);
-}
-
-template <template <int> class F>
-void with_split(int split, AxisBatch& b, cudaStream_t st) {
-  switch (split) {
-    case 1: F<1>::run(b, st); break;
-    case 2: F<2>::run(b, st); break;
-    case 4: F<4>::run(b, st); break;
-    case 8: F<8>::run(b, st); break;
-    case 16: F<16>::run(b, st); break;
-    default: F<32>::run(b, st); break;
-  }
-}
-template <int S> struct Pass1 { static void run(AxisBatch& b, cudaStream_t st) { launch_pass1<S>(b, st); } };
-template <int S> struct Pass2 { static void run(AxisBatch& b, cudaStream_t st) { launch_pass2<S>(b, st); } };
 
 void launch_two_level(AxisBatch& b, int nsm, cudaStream_t st) {
-  long long out1 = 0, out2 = 0;
-  int terms1 = 0, terms2 = 0;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(two_level_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(two_level_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr_set = true;
+  }
+  // pass 1: one k' per cluster while that gives fewer than two clusters per
+  // SM, else up to 8 k' per cluster so that each CTA reuses its staged row;
+  // the j1 sums are split over a cluster when there are few rows
+  long long rows = 0;
+  int kmin = 1 << 30;
   for (int i = 0; i < b.njobs; ++i) {
     const AxisJob& J = b.job[i];
-    out1 += (long long)J.nlines * J.B * (J.A + 1);
-    out2 += (long long)J.nlines * J.nout;
-    terms1 = std::max(terms1, (std::min(J.jhi, J.nin) + J.B - 1) / J.B);
-    terms2 = std::max(terms2, J.B);
+    rows += (long long)J.nlines * (J.A + 1);
+    kmin = std::min(kmin, (std::min(J.jhi, J.nin) + J.B - 1) / J.B);
   }
-  with_split<Pass1>(pick_split(out1, terms1, nsm), b, st);
-  with_split<Pass2>(pick_split(out2, terms2, nsm), b, st);
+  int kpc = (int)std::min<long long>(8, std::max<long long>(1, rows / (2LL * std::max(nsm, 1))));
+  const int ncl1 = pick_cluster((rows + kpc - 1) / kpc, kmin, nsm);
+  size_t smem1 = 0, smem2 = 0;
+  for (int i = 0; i < b.njobs; ++i) smem1 = std::max(smem1, pass1_smem(b.job[i], kpc, ncl1));
+  while (kpc > 1 && smem1 > 160 * 1024) {
+    kpc /= 2;
+    smem1 = 0;
+    for (int i = 0; i < b.njobs; ++i) smem1 = std::max(smem1, pass1_smem(b.job[i], kpc, ncl1));
+  }
+  int total = 0;
+  for (int i = 0; i < b.njobs; ++i) {
+    b.start[i] = total;
+    total += b.job[i].nlines * ((b.job[i].A + 1 + kpc - 1) / kpc) * ncl1;
+  }
+  b.start[b.njobs] = total;
+  if (total > 0)
+    launch_pdl_cluster(two_level_pass1, dim3(total), dim3(kP1Threads), smem1, ncl1, st, b, kpc, ncl1);
+  // pass 2: 32 outputs per cluster, the j2 sums split over a cluster when
+  // there are few output blocks
+  long long blocks = 0;
+  int bmin = 1 << 30;
+  for (int i = 0; i < b.njobs; ++i) {
+    blocks += (long long)b.job[i].nlines * ((b.job[i].nout + 31) / 32);
+    bmin = std::min(bmin, b.job[i].B);
+  }
+  const int ncl2 = pick_cluster(blocks, bmin, nsm);
+  total = 0;
+  for (int i = 0; i < b.njobs; ++i) {
+    b.start[i] = total;
+    total += b.job[i].nlines * ((b.job[i].nout + 31) / 32) * ncl2;
+    smem2 = std::max(smem2, pass2_smem(b.job[i], ncl2));
+  }
+  b.start[b.njobs] = total;
+  if (total > 0)
+    launch_pdl_cluster(two_level_pass2, dim3(total), dim3(kP2Threads), smem2, ncl2, st, b, ncl2);
 }
 
 // Decide the symmetry mode and the split of every x-pass job, then launch.
