@@ -15,13 +15,14 @@
 namespace hos {
 
 // Programmatic dependent launch: kernels are launched with programmatic
-// stream serialization so that a kernel's launch overlaps the end of the
-// previous one; every kernel waits for its predecessor's completion and
-// memory at its start (griddepcontrol.wait is a no-op without a
-// programmatic predecessor).
+// stream serialization.  Every kernel waits for its predecessor's
+// completion and memory before it touches data the predecessor may write
+// (griddepcontrol.wait is a no-op without a programmatic predecessor), then
+// lets its own successor launch, so that the successor's launch and its
+// work on constant data (twiddle tables, indices) overlap this kernel.
 __device__ __forceinline__ void pdl_wait() {
 #if defined(__CUDA_ARCH__)
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.wait;\n\tgriddepcontrol.launch_dependents;" ::: "memory");
 #endif
 }
 
@@ -123,6 +124,8 @@ struct AxisBatch {
   AxisJob job[kMaxJobs];
   int start[kMaxJobs + 1];   // first CTA of each job
   int njobs;
+  int early;                 // 1: the twiddle tables are constant and are staged
+                             //    before waiting for the previous kernel
 };
 
 // grid ids of the transform requests
@@ -164,6 +167,7 @@ struct Tables {
   int cnt_cap;
   double* cs;                // scratch of the two-level passes (may be null)
   long long cs_cap;
+  bool q_const = true;       // tables written before the first launch that reads them
   // quarter-wave tables for D = n1-1, n2-1, nd1-1, nd2-1, n3_add
   const double* q_n1;
   const double* q_n2;

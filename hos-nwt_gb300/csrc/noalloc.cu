@@ -91,6 +91,7 @@ extern "C" int hosnwt_transform_noalloc(int dir, int cs, int n, int nlines, cons
   tb.part_cap = kPartLen;
   tb.cnt = cnt;
   tb.cnt_cap = kCntLen;
+  tb.q_const = false;  // the table kernel above runs right before the passes
   double* no_tmp[kMaxJobs] = {};
   XfReq rq[kMaxJobs];
   for (int l0 = 0; l0 < nlines; l0 += kMaxJobs) {

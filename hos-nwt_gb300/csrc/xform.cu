@@ -58,7 +58,6 @@ __device__ __forceinline__ double twiddle_s(const double* q, int D, int m) {
 //   mode 2: input symmetry: terms are pairs (j, D-j) staged as
 //           u = x_j + x_{D-j}, v = x_j - x_{D-j} (outputs k <= D/2)
 __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b) {
-  pdl_wait();
   extern __shared__ double smem[];
   __shared__ double red[kXWarps][32][2];
   __shared__ bool amlast;
@@ -83,7 +82,11 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b
   double* q = smem;                    // D + 1 table entries
   double* su = smem + (D + 1);         // staged inputs (or u)
   double* sv = su + kMaxPairChunk;     // v (mode 2)
-  for (int t = threadIdx.x; t <= D; t += kXThreads) q[t] = __ldg(J.q + t);
+  if (b.early)
+    for (int t = threadIdx.x; t <= D; t += kXThreads) q[t] = __ldg(J.q + t);
+  pdl_wait();
+  if (!b.early)
+    for (int t = threadIdx.x; t <= D; t += kXThreads) q[t] = __ldg(J.q + t);
   const int ca = J.ta + chunk_id * J.chunk;
   const int cb = min(J.tb, ca + J.chunk);
   // cos: even k pairs with u; sin: even k pairs with v (mode 2)
@@ -339,7 +342,6 @@ __device__ __forceinline__ double ld_cluster(const double* local, unsigned rank)
 // with j2 fastest: staged inputs are read without bank conflicts and the j1
 // twiddles are broadcast.
 __global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatch b, int kpc, int ncl) {
-  pdl_wait();
   extern __shared__ double sm1[];
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
@@ -362,6 +364,19 @@ __global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatch b,
   double* red = ts + kpc * Kc;      // partial sums of the items
   const double* __restrict__ x = J.in + (long long)line * J.in_sl;
   const double* __restrict__ wr = J.win ? J.win + (long long)line * J.win_sl : nullptr;
+  auto stage_twiddles = [&]() {
+    for (int t = threadIdx.x; t < nkp * Kl; t += kP1Threads) {
+      const int kpl = t / Kl, j1 = ja1 + t - kpl * Kl;
+      // pi j1 k' / A = pi (2 B j1 k') / (2 D); both factors below 4D
+      const unsigned step = (2u * (unsigned)B * (unsigned)(kp0 + kpl)) % (unsigned)D4;
+      const int m = (int)((step * (unsigned)j1) % (unsigned)D4);
+      tc[kpl * Kc + j1 - ja1] = twiddle(J.q, D, m);
+      ts[kpl * Kc + j1 - ja1] = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
+    }
+  };
+  if (b.early) stage_twiddles();
+  pdl_wait();
+  if (!b.early) stage_twiddles();
   for (int t = threadIdx.x; t < Kl * B; t += kP1Threads) {
     const int j = ja1 * B + t;
     double v = 0.0;
@@ -370,14 +385,6 @@ __global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatch b,
       v = w * in_at(x, J.in_sk, wr, j);
     }
     xs[t] = v;
-  }
-  for (int t = threadIdx.x; t < nkp * Kl; t += kP1Threads) {
-    const int kpl = t / Kl, j1 = ja1 + t - kpl * Kl;
-    // pi j1 k' / A = pi (2 B j1 k') / (2 D); both factors below 4D
-    const unsigned step = (2u * (unsigned)B * (unsigned)(kp0 + kpl)) % (unsigned)D4;
-    const int m = (int)((step * (unsigned)j1) % (unsigned)D4);
-    tc[kpl * Kc + j1 - ja1] = twiddle(J.q, D, m);
-    ts[kpl * Kc + j1 - ja1] = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
   }
   __syncthreads();
   const int P = max(1, kP1Threads / (nkp * B));  // parts splitting the j1 sum
@@ -432,7 +439,6 @@ __global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatch b,
 // first; lanes own outputs (their C, S loads are contiguous), warps split
 // the slice and are combined in a fixed order.
 __global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatch b, int ncl) {
-  pdl_wait();
   extern __shared__ double sm2[];
   __shared__ double red[kP2Warps][32];
   __shared__ double fin[32];
@@ -447,13 +453,18 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatch b,
   const int k0 = (local - line * nkb) * 32;
   const int Bc = (B + ncl - 1) / ncl;
   const int ja2 = min(B, (int)rank * Bc), Bl = min(B, ja2 + Bc) - ja2;
-  for (int t = threadIdx.x; t < Bl * 32; t += kP2Threads) {
-    const int j2 = ja2 + (t >> 5), k = k0 + (t & 31);
-    // pi j2 k / D; j2 < D and k < N, so 2 j2 k fits in 32 bits for N < 32768
-    const int m = (int)((2u * (unsigned)j2 * (unsigned)k) % (unsigned)D4);
-    sm2[2 * t] = twiddle(J.q, D, m);
-    sm2[2 * t + 1] = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
-  }
+  auto stage_twiddles = [&]() {
+    for (int t = threadIdx.x; t < Bl * 32; t += kP2Threads) {
+      const int j2 = ja2 + (t >> 5), k = k0 + (t & 31);
+      // pi j2 k / D; j2 < D and k < N, so 2 j2 k fits in 32 bits for N < 32768
+      const int m = (int)((2u * (unsigned)j2 * (unsigned)k) % (unsigned)D4);
+      sm2[2 * t] = twiddle(J.q, D, m);
+      sm2[2 * t + 1] = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
+    }
+  };
+  if (b.early) stage_twiddles();
+  pdl_wait();
+  if (!b.early) stage_twiddles();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int k = k0 + lane;
   const bool on = k < J.nout && k >= J.klo && k < J.khi;
@@ -622,7 +633,8 @@ int pick_cluster(long long units, int terms, int nsm) {
   return ncl;
 }
 
-void launch_two_level(AxisBatch& b, int nsm, cudaStream_t st) {
+void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
+  b.early = early ? 1 : 0;
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(two_level_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
@@ -678,6 +690,7 @@ void launch_two_level(AxisBatch& b, int nsm, cudaStream_t st) {
 
 // Decide the symmetry mode and the split of every x-pass job, then launch.
 void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
+  b.early = tb.q_const ? 1 : 0;
   long long tiles_total = 0;
   for (int i = 0; i < b.njobs; ++i) {
     AxisJob& J = b.job[i];
@@ -850,7 +863,7 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
     }
     bd.job[bd.njobs++] = J;
   }
-  if (b2.njobs) launch_two_level(b2, tb.nsm, st);
+  if (b2.njobs) launch_two_level(b2, tb.nsm, tb.q_const, st);
   if (bd.njobs) launch_batch_x(bd, tb, st);
   if (by.njobs) launch_batch_y(by, st);
 }
