@@ -120,13 +120,18 @@ struct AxisJob {
 
 constexpr int kMaxJobs = 16;
 
-struct AxisBatch {
-  AxisJob job[kMaxJobs];
-  int start[kMaxJobs + 1];   // first CTA of each job
+// A batch of jobs for one launch.  Kernels take the batch by value as their
+// parameters, whose size costs launch time, so a launch passes the smallest
+// capacity NJ (1, 2, 4, 8 or kMaxJobs) that holds its jobs.
+template <int NJ>
+struct AxisBatchT {
+  AxisJob job[NJ];
+  int start[NJ + 1];         // first CTA of each job
   int njobs;
   int early;                 // 1: the twiddle tables are constant and are staged
                              //    before waiting for the previous kernel
 };
+using AxisBatch = AxisBatchT<kMaxJobs>;
 
 // grid ids of the transform requests
 enum GridId { GRID_N = 0, GRID_BIG = 1, GRID_ADD = 2 };

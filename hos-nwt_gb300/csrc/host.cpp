@@ -1400,19 +1400,35 @@ extern "C" int hosnwt_time_transform(hosnwt_ctx* h, int grid, int dir, int csx, 
     r.out = bufs[2 * i + 1]; r.out_ld = a; r.nout1 = nout1; r.nout2 = nout2;
     r.scale = 1.0;
   }
+  // nrep back-to-back transforms captured in one graph, as the step graph
+  // launches them; the second replay is timed
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   for (int w = 0; w < 3; ++w) launch_transforms(rq.data(), batch, c.tb, c.d.xtmp, c.st);
-  cudaEventRecord(e0, c.st);
-  for (int r = 0; r < nrep; ++r) launch_transforms(rq.data(), batch, c.tb, c.d.xtmp, c.st);
-  cudaEventRecord(e1, c.st);
-  cudaEventSynchronize(e1);
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ge = nullptr;
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, e0, e1);
+  bool ok = cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+  if (ok) {
+    for (int r = 0; r < nrep; ++r) launch_transforms(rq.data(), batch, c.tb, c.d.xtmp, c.st);
+    ok = cudaStreamEndCapture(c.st, &g) == cudaSuccess;
+  }
+  if (ok) ok = cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+  if (ok) {
+    cudaGraphLaunch(ge, c.st);
+    cudaEventRecord(e0, c.st);
+    cudaGraphLaunch(ge, c.st);
+    cudaEventRecord(e1, c.st);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+  }
+  if (ge) cudaGraphExecDestroy(ge);
+  if (g) cudaGraphDestroy(g);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   for (double* q : bufs) cudaFree(q);
+  if (!ok) return fail(c, HOSNWT_ERR_CUDA, "time_transform: graph capture failed");
   *ms_per_launch = ms / nrep;
   return cuda_check(c, "time_transform");
 }

@@ -13,6 +13,7 @@
 // warp-uniform twiddles) and several outputs per thread.
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "hosnwt_internal.h"
 
@@ -57,7 +58,8 @@ __device__ __forceinline__ double twiddle_s(const double* q, int D, int m) {
 //           and writes out[k] and out[D-k] (full outputs, D = N-1)
 //   mode 2: input symmetry: terms are pairs (j, D-j) staged as
 //           u = x_j + x_{D-j}, v = x_j - x_{D-j} (outputs k <= D/2)
-__global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatch b) {
+template <int NJ>
+__global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatchT<NJ> b) {
   extern __shared__ double smem[];
   __shared__ double red[kXWarps][32][2];
   __shared__ bool amlast;
@@ -242,7 +244,8 @@ constexpr int kYR = 8;  // outputs per thread
 
 // y pass: one thread = one line (consecutive lines are contiguous in memory)
 // and kYR outputs; twiddles are warp-uniform.
-__global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatch b) {
+template <int NJ>
+__global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatchT<NJ> b) {
   pdl_wait();
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
@@ -341,7 +344,8 @@ __device__ __forceinline__ double ld_cluster(const double* local, unsigned rank)
 // cluster sums j1 in its slice of [0, K).  Threads own (k', part, j2) items
 // with j2 fastest: staged inputs are read without bank conflicts and the j1
 // twiddles are broadcast.
-__global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatch b, int kpc, int ncl) {
+template <int NJ>
+__global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatchT<NJ> b, int kpc, int ncl) {
   extern __shared__ double sm1[];
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
@@ -438,7 +442,8 @@ __global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatch b,
 // its slice of [0, B).  The slice's twiddles cos/sin(pi j2 k / D) are staged
 // first; lanes own outputs (their C, S loads are contiguous), warps split
 // the slice and are combined in a fixed order.
-__global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatch b, int ncl) {
+template <int NJ>
+__global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatchT<NJ> b, int ncl) {
   extern __shared__ double sm2[];
   __shared__ double red[kP2Warps][32];
   __shared__ double fin[32];
@@ -610,6 +615,29 @@ void pick_factors(int D, int nin, int nout, int* Aout, int* Bout) {
   }
 }
 
+// Call f with the smallest batch capacity that holds b's jobs.
+template <int NJ>
+AxisBatchT<NJ> shrink(const AxisBatch& b) {
+  AxisBatchT<NJ> s{};
+  for (int i = 0; i < b.njobs; ++i) s.job[i] = b.job[i];
+  for (int i = 0; i <= b.njobs; ++i) s.start[i] = b.start[i];
+  s.njobs = b.njobs;
+  s.early = b.early;
+  return s;
+}
+template <typename F>
+void with_capacity(int njobs, F&& f) {
+  if (njobs <= 1) f(std::integral_constant<int, 1>{});
+  else if (njobs <= 2) f(std::integral_constant<int, 2>{});
+  else if (njobs <= 4) f(std::integral_constant<int, 4>{});
+  else if (njobs <= 8) f(std::integral_constant<int, 8>{});
+  else f(std::integral_constant<int, kMaxJobs>{});
+}
+template <typename K>
+void allow_smem(K kern) {
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
 // Shared memory of pass 1 for a job with kpc values of k' per cluster and
 // ncl CTAs per cluster, and of pass 2 with ncl CTAs per cluster.
 size_t pass1_smem(const AxisJob& J, int kpc, int ncl) {
@@ -625,11 +653,13 @@ size_t pass2_smem(const AxisJob& J, int ncl) {
   return sizeof(double) * 2 * 32 * (size_t)((J.B + ncl - 1) / ncl);
 }
 
-// Cluster size: the smallest power of two (at most 8) that gives about
-// four CTAs per SM, and no more CTAs than slices of `terms` work.
-int pick_cluster(long long units, int terms, int nsm) {
+// Cluster size: split a CTA's sum only while its FP64 work (`fmas`, at about
+// 2 FMAs per cycle per SM) exceeds the cost of the cluster barriers, the
+// launch has room on the SMs, and each CTA keeps at least 4 terms.
+int pick_cluster(long long units, long long fmas, int terms, int nsm) {
   int ncl = 1;
-  while (ncl < 8 && units * ncl < 4LL * std::max(nsm, 1) && 2 * ncl * 4 <= terms) ncl *= 2;
+  while (ncl < 8 && fmas / ncl > 4096 && units * ncl < 4LL * std::max(nsm, 1) && 2 * ncl * 4 <= terms)
+    ncl *= 2;
   return ncl;
 }
 
@@ -637,22 +667,27 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
   b.early = early ? 1 : 0;
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(two_level_pass1, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(two_level_pass2, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    for (int nj : {1, 2, 4, 8, kMaxJobs})
+      with_capacity(nj, [&](auto c) {
+        allow_smem(two_level_pass1<decltype(c)::value>);
+        allow_smem(two_level_pass2<decltype(c)::value>);
+      });
     attr_set = true;
   }
   // pass 1: one k' per cluster while that gives fewer than two clusters per
   // SM, else up to 8 k' per cluster so that each CTA reuses its staged row;
   // the j1 sums are split over a cluster when there are few rows
-  long long rows = 0;
+  long long rows = 0, kbmax = 0;
   int kmin = 1 << 30;
   for (int i = 0; i < b.njobs; ++i) {
     const AxisJob& J = b.job[i];
     rows += (long long)J.nlines * (J.A + 1);
-    kmin = std::min(kmin, (std::min(J.jhi, J.nin) + J.B - 1) / J.B);
+    const int K = (std::min(J.jhi, J.nin) + J.B - 1) / J.B;
+    kmin = std::min(kmin, K);
+    kbmax = std::max(kbmax, (long long)K * J.B);
   }
   int kpc = (int)std::min<long long>(8, std::max<long long>(1, rows / (2LL * std::max(nsm, 1))));
-  const int ncl1 = pick_cluster((rows + kpc - 1) / kpc, kmin, nsm);
+  const int ncl1 = pick_cluster((rows + kpc - 1) / kpc, 2 * kbmax * kpc, kmin, nsm);
   size_t smem1 = 0, smem2 = 0;
   for (int i = 0; i < b.njobs; ++i) smem1 = std::max(smem1, pass1_smem(b.job[i], kpc, ncl1));
   while (kpc > 1 && smem1 > 160 * 1024) {
@@ -667,16 +702,21 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
   }
   b.start[b.njobs] = total;
   if (total > 0)
-    launch_pdl_cluster(two_level_pass1, dim3(total), dim3(kP1Threads), smem1, ncl1, st, b, kpc, ncl1);
+    with_capacity(b.njobs, [&](auto c) {
+      constexpr int NJ = decltype(c)::value;
+      launch_pdl_cluster(two_level_pass1<NJ>, dim3(total), dim3(kP1Threads), smem1, ncl1, st, shrink<NJ>(b),
+                         kpc, ncl1);
+    });
   // pass 2: 32 outputs per cluster, the j2 sums split over a cluster when
   // there are few output blocks
   long long blocks = 0;
-  int bmin = 1 << 30;
+  int bmin = 1 << 30, bmax = 0;
   for (int i = 0; i < b.njobs; ++i) {
     blocks += (long long)b.job[i].nlines * ((b.job[i].nout + 31) / 32);
     bmin = std::min(bmin, b.job[i].B);
+    bmax = std::max(bmax, b.job[i].B);
   }
-  const int ncl2 = pick_cluster(blocks, bmin, nsm);
+  const int ncl2 = pick_cluster(blocks, 64LL * bmax, bmin, nsm);
   total = 0;
   for (int i = 0; i < b.njobs; ++i) {
     b.start[i] = total;
@@ -685,7 +725,11 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
   }
   b.start[b.njobs] = total;
   if (total > 0)
-    launch_pdl_cluster(two_level_pass2, dim3(total), dim3(kP2Threads), smem2, ncl2, st, b, ncl2);
+    with_capacity(b.njobs, [&](auto c) {
+      constexpr int NJ = decltype(c)::value;
+      launch_pdl_cluster(two_level_pass2<NJ>, dim3(total), dim3(kP2Threads), smem2, ncl2, st, shrink<NJ>(b),
+                         ncl2);
+    });
 }
 
 // Decide the symmetry mode and the split of every x-pass job, then launch.
@@ -756,10 +800,15 @@ void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
     smem = std::max(smem, sizeof(double) * ((size_t)b.job[i].D + 1 + 2 * (size_t)kMaxPairChunk));
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(axis_pass_lanes_k, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    for (int nj : {1, 2, 4, 8, kMaxJobs})
+      with_capacity(nj, [&](auto c) { allow_smem(axis_pass_lanes_k<decltype(c)::value>); });
     attr_set = true;
   }
-  if (total > 0) launch_pdl(axis_pass_lanes_k, dim3(total), dim3(kXThreads), smem, st, b);
+  if (total > 0)
+    with_capacity(b.njobs, [&](auto c) {
+      constexpr int NJ = decltype(c)::value;
+      launch_pdl(axis_pass_lanes_k<NJ>, dim3(total), dim3(kXThreads), smem, st, shrink<NJ>(b));
+    });
 }
 
 void launch_batch_y(AxisBatch& b, cudaStream_t st) {
@@ -770,7 +819,11 @@ void launch_batch_y(AxisBatch& b, cudaStream_t st) {
     total += nlb * ((b.job[i].nout + kYR - 1) / kYR);
   }
   b.start[b.njobs] = total;
-  if (total > 0) launch_pdl(axis_pass_lanes_line, dim3(total), dim3(kYThreads), 0, st, b);
+  if (total > 0)
+    with_capacity(b.njobs, [&](auto c) {
+      constexpr int NJ = decltype(c)::value;
+      launch_pdl(axis_pass_lanes_line<NJ>, dim3(total), dim3(kYThreads), 0, st, shrink<NJ>(b));
+    });
 }
 
 }  // namespace

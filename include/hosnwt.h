@@ -165,9 +165,10 @@ int hosnwt_transform(hosnwt_ctx* ctx, int grid, int dir, int csx, int csy,
 
 /* Measurement hooks (no counterpart in the reference).
  * hosnwt_time_transform: average device time (ms, CUDA events on the
- * context's stream) of `nrep` launches of one batched transform of `batch`
- * requests on the given grid with nonzero input extent nin1 x nin2 and
- * written output extent nout1 x nout2.
+ * context's stream) of one batched transform of `batch` requests on the
+ * given grid with nonzero input extent nin1 x nin2 and written output
+ * extent nout1 x nout2, from `nrep` of them run back to back in one CUDA
+ * graph (as the step graph runs its transforms).
  * hosnwt_fp64_peak: FP64 FMA throughput of the current device (GFLOP/s). */
 int hosnwt_time_transform(hosnwt_ctx* ctx, int grid, int dir, int csx, int csy, int nin1, int nin2,
                           int nout1, int nout2, int batch, int nrep, double* ms_per_launch);
