@@ -535,6 +535,150 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatchT<N
   if (ncl > 1) cluster_sync_all();  // remote reads done before any CTA exits
 }
 
+// Two-level y passes (REDFT00 / RODFT00 along a strided axis, lines
+// contiguous): the same split as above, with lanes owning lines so that
+// every load and store is coalesced and every twiddle is warp-uniform.
+// The partial sums are stored [((j2 (A+1) + k') 2 + {C, S}) nlines + line].
+constexpr int kYT = 128;   // lines per CTA
+constexpr int kYKP = 18;   // k' per pass-1 CTA (accumulator pairs per thread)
+constexpr int kYQ = 20;    // outputs of one k' class per pass-2 thread
+
+// pass 1: CTA = (job, k' chunk, j2, block of kYT lines)
+template <int NJ>
+__global__ void __launch_bounds__(kYT) ytl_pass1(const AxisBatchT<NJ> b) {
+  extern __shared__ double smy[];
+  int jb = 0;
+  while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
+  const AxisJob& J = b.job[jb];
+  const int A = J.A, B = J.B, D = J.D, D4 = 4 * D;
+  const int nkc = (A + 1 + kYKP - 1) / kYKP;
+  int local = blockIdx.x - b.start[jb];
+  const int kc = local % nkc;
+  local /= nkc;
+  const int j2 = local % B;
+  const int lb = local / B;
+  const int kp0 = kc * kYKP, nkp = min(kYKP, A + 1 - kp0);
+  const int j_end = min(J.jhi, J.nin);
+  const int K = (j_end + B - 1) / B;
+  double* tc = smy;               // K x kYKP cos(pi j1 k' / A)
+  double* ts = tc + K * kYKP;     // K x kYKP sin(pi j1 k' / A)
+  auto stage = [&]() {
+    for (int t = threadIdx.x; t < K * kYKP; t += kYT) {
+      const int j1 = t / kYKP, kpl = t - j1 * kYKP;
+      double c = 0.0, sn = 0.0;
+      if (kpl < nkp) {
+        const unsigned step = (2u * (unsigned)B * (unsigned)(kp0 + kpl)) % (unsigned)D4;
+        const int m = (int)((step * (unsigned)j1) % (unsigned)D4);
+        c = twiddle(J.q, D, m);
+        sn = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
+      }
+      tc[t] = c;
+      ts[t] = sn;
+    }
+  };
+  if (b.early) stage();
+  pdl_wait();
+  if (!b.early) stage();
+  __syncthreads();
+  const int line = lb * kYT + threadIdx.x;
+  if (line >= J.nlines) return;
+  const double* __restrict__ x = J.in + (long long)line * J.in_sl;
+  double c[kYKP], sn[kYKP];
+#pragma unroll
+  for (int r = 0; r < kYKP; ++r) c[r] = sn[r] = 0.0;
+  for (int j1 = 0; j1 < K; ++j1) {
+    const int j = B * j1 + j2;
+    if (j < J.jlo || j >= j_end) continue;
+    const double w = (j == 0) ? J.w0 : ((j == J.N - 1) ? J.wl : J.wm);
+    const double v = w * __ldg(x + (long long)j * J.in_sk);
+#pragma unroll
+    for (int r = 0; r < kYKP; ++r) {
+      c[r] = fma(v, tc[j1 * kYKP + r], c[r]);
+      sn[r] = fma(v, ts[j1 * kYKP + r], sn[r]);
+    }
+  }
+  const long long nl = J.nlines;
+  double* o = J.cs + ((long long)j2 * (A + 1) + kp0) * 2 * nl + line;
+#pragma unroll
+  for (int r = 0; r < kYKP; ++r) {
+    if (r < nkp) {
+      o[(2 * r) * nl] = c[r];
+      o[(2 * r + 1) * nl] = sn[r];
+    }
+  }
+}
+
+// output o of class k': k = 2 A o + k' when k' is 0 or A, else alternately
+// 2 A q + k' and 2 A (q + 1) - k' (folded, S enters with a minus sign)
+__device__ __forceinline__ int ytl_k(int o, int A, int kp, bool pair) {
+  if (!pair) return 2 * A * o + kp;
+  const int q = o >> 1;
+  return (o & 1) ? 2 * A * (q + 1) - kp : 2 * A * q + kp;
+}
+
+// pass 2: CTA = (job, k', block of kYT lines); each C, S value is read once
+// and feeds every output of its class
+template <int NJ>
+__global__ void __launch_bounds__(kYT) ytl_pass2(const AxisBatchT<NJ> b) {
+  extern __shared__ double smy[];
+  int jb = 0;
+  while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
+  const AxisJob& J = b.job[jb];
+  const int A = J.A, B = J.B, D = J.D, D4 = 4 * D;
+  const int local = blockIdx.x - b.start[jb];
+  const int kp = local % (A + 1);
+  const int lb = local / (A + 1);
+  const bool pair = kp > 0 && kp < A;
+  double* tw = smy;  // B x kYQ (cos, sin)(pi j2 k / D)
+  auto stage = [&]() {
+    for (int t = threadIdx.x; t < B * kYQ; t += kYT) {
+      const int j2 = t / kYQ, oi = t - j2 * kYQ;
+      const int k = ytl_k(oi, A, kp, pair);
+      double c = 0.0, sn = 0.0;
+      if (k < J.nout) {
+        const int m = (int)((2u * (unsigned)j2 * (unsigned)k) % (unsigned)D4);
+        c = twiddle(J.q, D, m);
+        sn = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
+      }
+      tw[2 * t] = c;
+      tw[2 * t + 1] = sn;
+    }
+  };
+  if (b.early) stage();
+  pdl_wait();
+  if (!b.early) stage();
+  __syncthreads();
+  const int line = lb * kYT + threadIdx.x;
+  if (line >= J.nlines) return;
+  const bool is_sin = (J.off != 0);
+  const long long nl = J.nlines;
+  const double* cs = J.cs + (long long)kp * 2 * nl + line;
+  double acc[kYQ];
+#pragma unroll
+  for (int oi = 0; oi < kYQ; ++oi) acc[oi] = 0.0;
+  for (int j2 = 0; j2 < B; ++j2) {
+    const long long base = (long long)j2 * (A + 1) * 2 * nl;
+    const double C = __ldcg(cs + base), S = __ldcg(cs + base + nl);
+    const double* t = tw + 2 * j2 * kYQ;
+#pragma unroll
+    for (int oi = 0; oi < kYQ; ++oi) {
+      const double Ss = (pair && (oi & 1)) ? -S : S;
+      const double cw = t[2 * oi], sw = t[2 * oi + 1];
+      acc[oi] = is_sin ? fma(cw, Ss, fma(sw, C, acc[oi])) : fma(cw, C, fma(-sw, Ss, acc[oi]));
+    }
+  }
+  double* out = J.out + (long long)line * J.out_sl;
+#pragma unroll
+  for (int oi = 0; oi < kYQ; ++oi) {
+    const int k = ytl_k(oi, A, kp, pair);
+    if (k < J.nout) {
+      const bool on = k >= J.klo && k < J.khi;
+      const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
+      out[(long long)k * J.out_sk] = on ? acc[oi] * sc * J.gscale : 0.0;
+    }
+  }
+}
+
 // Fill the kind-dependent parameters of a pass.
 void set_kind(AxisJob& J, int kind, int N, const double* q) {
   J.N = N;
@@ -811,7 +955,93 @@ void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
     });
 }
 
-void launch_batch_y(AxisBatch& b, cudaStream_t st) {
+// Factor pair of a y pass: minimum 2 (A+1) nin + 2 B nout FMAs, with every
+// k' class (at most 2 nout / (2A) + 2 outputs) held by one pass-2 thread;
+// A = 0 when the direct sum (nin * nout FMAs) is cheaper.
+void pick_factors_y(int D, int nin, int nout, int* Aout, int* Bout) {
+  *Aout = *Bout = 0;
+  double best = 0.6 * (double)nin * (double)nout;
+  for (int A = 2; A <= D / 2; ++A) {
+    if (D % A) continue;
+    const int B = D / A;
+    if (B < 2 || B > 256) continue;
+    if (2 * ((nout + 2 * A - 1) / (2 * A)) + 1 > kYQ) continue;
+    const double cost = 2.0 * (A + 1) * (double)nin + 2.0 * B * (double)nout;
+    if (cost < best) {
+      best = cost;
+      *Aout = A;
+      *Bout = B;
+    }
+  }
+}
+
+void launch_ytl(AxisBatch& b, bool early, cudaStream_t st) {
+  b.early = early ? 1 : 0;
+  static bool attr_set = false;
+  if (!attr_set) {
+    for (int nj : {1, 2, 4, 8, kMaxJobs})
+      with_capacity(nj, [&](auto c) {
+        allow_smem(ytl_pass1<decltype(c)::value>);
+        allow_smem(ytl_pass2<decltype(c)::value>);
+      });
+    attr_set = true;
+  }
+  int total = 0;
+  size_t smem1 = 0, smem2 = 0;
+  for (int i = 0; i < b.njobs; ++i) {
+    const AxisJob& J = b.job[i];
+    const int nlb = (J.nlines + kYT - 1) / kYT;
+    const int K = (std::min(J.jhi, J.nin) + J.B - 1) / J.B;
+    b.start[i] = total;
+    total += nlb * J.B * ((J.A + 1 + kYKP - 1) / kYKP);
+    smem1 = std::max(smem1, sizeof(double) * 2 * (size_t)K * kYKP);
+    smem2 = std::max(smem2, sizeof(double) * 2 * (size_t)J.B * kYQ);
+  }
+  b.start[b.njobs] = total;
+  with_capacity(b.njobs, [&](auto c) {
+    constexpr int NJ = decltype(c)::value;
+    launch_pdl(ytl_pass1<NJ>, dim3(total), dim3(kYT), smem1, st, shrink<NJ>(b));
+  });
+  total = 0;
+  for (int i = 0; i < b.njobs; ++i) {
+    b.start[i] = total;
+    total += ((b.job[i].nlines + kYT - 1) / kYT) * (b.job[i].A + 1);
+  }
+  b.start[b.njobs] = total;
+  with_capacity(b.njobs, [&](auto c) {
+    constexpr int NJ = decltype(c)::value;
+    launch_pdl(ytl_pass2<NJ>, dim3(total), dim3(kYT), smem2, st, shrink<NJ>(b));
+  });
+}
+
+// y passes: two-level where the length factors well (scratch permitting),
+// direct sums otherwise
+void launch_batch_y(AxisBatch& in, const Tables& tb, cudaStream_t st) {
+  AxisBatch b{}, b2{};
+  b.njobs = b2.njobs = 0;
+  long long cs_used = 0;
+  for (int i = 0; i < in.njobs; ++i) {
+    AxisJob J = in.job[i];
+    J.A = J.B = 0;
+    J.cs = nullptr;
+    const bool c1s1 = (J.aj == 2 && J.bj == 0 && J.ak == 1 && J.bk == 0);
+    if (c1s1 && tb.cs) {
+      int A = 0, B = 0;
+      pick_factors_y(J.D, std::min(J.nin, J.N), J.nout, &A, &B);
+      const long long need = (long long)J.nlines * B * (A + 1) * 2;
+      if (A > 0 && cs_used + need <= tb.cs_cap) {
+        J.A = A;
+        J.B = B;
+        J.cs = tb.cs + cs_used;
+        cs_used += need;
+        b2.job[b2.njobs++] = J;
+        continue;
+      }
+    }
+    b.job[b.njobs++] = J;
+  }
+  if (b2.njobs) launch_ytl(b2, tb.q_const, st);
+  if (b.njobs == 0) return;
   int total = 0;
   for (int i = 0; i < b.njobs; ++i) {
     b.start[i] = total;
@@ -918,7 +1148,7 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
   }
   if (b2.njobs) launch_two_level(b2, tb.nsm, tb.q_const, st);
   if (bd.njobs) launch_batch_x(bd, tb, st);
-  if (by.njobs) launch_batch_y(by, st);
+  if (by.njobs) launch_batch_y(by, tb, st);
 }
 
 namespace {
@@ -977,7 +1207,7 @@ void launch_y_f2s(const Tables& tb, const double* in, int nlines, long long y_st
   J.out_sk = out_y_stride;
   J.out_sl = 1;
   J.gscale = 1.0;
-  launch_batch_y(b, st);
+  launch_batch_y(b, tb, st);
 }
 
 }  // namespace hos

@@ -20,4 +20,11 @@ JONSWAP_1D = dict(inp=default_input(icase=4, Hs=0.05, Tp=1.2, gamma=3.3, iseed=5
                                     toler=1e-7, f_out=10.0),
                   n1=65, n2=1, n3=17, mHOS=3, p1=3, p2=1)
 
-ALL = {"reg1d": REG_1D, "reg1d_m5": REG_1D_M5, "reg3d": REG_3D, "slosh": SLOSH, "jonswap1d": JONSWAP_1D}
+# 3-D tank with a long y axis: n2 - 1 = 128 takes the two-level y passes
+# (free-surface grid and the phiadd_SL y sums); Nd2 - 1 = 257 is prime
+WIDE_3D = dict(inp=default_input(T_stop=20.0, amp_mono=0.02, nu_mono=0.7, theta_mono=10.0, toler=1e-7,
+                                 f_out=4.0, ylen=20.0),
+               n1=17, n2=129, n3=9, mHOS=3, p1=3, p2=3)
+
+ALL = {"reg1d": REG_1D, "reg1d_m5": REG_1D_M5, "reg3d": REG_3D, "slosh": SLOSH, "jonswap1d": JONSWAP_1D,
+       "wide3d": WIDE_3D}

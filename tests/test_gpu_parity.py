@@ -33,7 +33,7 @@ def _rel(a, b):
     return float(np.max(np.abs(a - b)) / scale)
 
 
-@pytest.mark.parametrize("name", ["reg1d", "reg3d"])
+@pytest.mark.parametrize("name", ["reg1d", "reg3d", "wide3d"])
 def test_transforms(lib, name):
     case = cases.ALL[name]
     g = _gtank(case)
@@ -72,7 +72,7 @@ def _state(o, rng, amp=1e-3):
     return y
 
 
-@pytest.mark.parametrize("name", ["reg1d", "reg1d_m5", "reg3d", "slosh", "jonswap1d"])
+@pytest.mark.parametrize("name", ["reg1d", "reg1d_m5", "reg3d", "slosh", "jonswap1d", "wide3d"])
 def test_solveHOS2(lib, name):
     case = cases.ALL[name]
     g = _gtank(case)
