@@ -243,7 +243,12 @@ constexpr int kYThreads = 128;
 constexpr int kYR = 8;  // outputs per thread
 
 // y pass: one thread = one line (consecutive lines are contiguous in memory)
-// and kYR outputs; twiddles are warp-uniform.
+// and kYR lane outputs; twiddles are warp-uniform.  The two symmetries of
+// the x pass halve the FP64 work of REDFT00 / RODFT00 kinds:
+//   mode 1: lane output k (k <= D/2) keeps even-j and odd-j sums E, O and
+//           writes out[k] and out[D-k]
+//   mode 2: inputs are paired, u = x_j + x_{D-j}, v = x_j - x_{D-j}
+//           (outputs k <= D/2)
 template <int NJ>
 __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatchT<NJ> b) {
   pdl_wait();
@@ -257,48 +262,138 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
   const int line = lb * kYThreads + threadIdx.x;
   if (line >= J.nlines) return;
   const int k0 = kgrp * kYR;
-  const int D4 = 4 * J.D;
+  const int D = J.D, D4 = 4 * D;
   const double* __restrict__ x = J.in + (long long)line * J.in_sl;
+  const long long sk = J.in_sk;
   const int j_end = min(J.jhi, J.nin);
-
-  double acc[kYR];
-  int m[kYR], inc[kYR];
-#pragma unroll
-  for (int r = 0; r < kYR; ++r) {
-    acc[r] = 0.0;
-    const int kk = J.ak * (k0 + r) + J.bk;
-    inc[r] = mod4d((long long)J.aj * kk, D4);
-    const int ja = max(J.jlo, 1);
-    m[r] = mod4d((long long)(J.aj * ja + J.bj) * kk + J.off, D4);
-  }
-  const int a0 = max(J.jlo, 1), a1 = min(j_end, J.N - 1);
-  for (int j = a0; j < a1; ++j) {
-    const double v = __ldg(x + (long long)j * J.in_sk);
-#pragma unroll
-    for (int r = 0; r < kYR; ++r) {
-      acc[r] = fma(v, twiddle(J.q, J.D, m[r]), acc[r]);
-      m[r] += inc[r];
-      if (m[r] >= D4) m[r] -= D4;
-    }
-  }
-#pragma unroll
-  for (int r = 0; r < kYR; ++r) {
-    const int k = k0 + r;
-    if (k >= J.nout) break;
-    double t = J.wm * acc[r];
-    const int kk = J.ak * k + J.bk;
-    if (J.jlo == 0 && 0 < j_end) {
-      const int mm = mod4d((long long)J.bj * kk + J.off, D4);
-      t = fma(J.w0 * __ldg(x), twiddle(J.q, J.D, mm), t);
-    }
-    const int jl = J.N - 1;
-    if (jl > 0 && jl >= J.jlo && jl < j_end) {
-      const int mm = mod4d((long long)(J.aj * jl + J.bj) * kk + J.off, D4);
-      t = fma(J.wl * __ldg(x + (long long)jl * J.in_sk), twiddle(J.q, J.D, mm), t);
-    }
+  const bool is_sin = (J.off != 0);
+  double* out = J.out + (long long)line * J.out_sl;
+  auto put = [&](int k, double v) {
+    if (k >= J.nout) return;
     const bool active = (k >= J.klo) && (k < J.khi);
     const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
-    J.out[(long long)line * J.out_sl + (long long)k * J.out_sk] = active ? t * sc * J.gscale : 0.0;
+    out[(long long)k * J.out_sk] = active ? v * sc * J.gscale : 0.0;
+  };
+  auto step = [&](int& m, int inc) {
+    m += inc;
+    if (m >= D4) m -= D4;
+  };
+  int m[kYR], inc[kYR];
+  const int a0 = max(J.jlo, 1);
+#pragma unroll
+  for (int r = 0; r < kYR; ++r) {
+    const int kk = J.ak * (k0 + r) + J.bk;
+    inc[r] = mod4d((long long)J.aj * kk, D4);
+    m[r] = mod4d((long long)(J.aj * a0 + J.bj) * kk + J.off, D4);
+  }
+  if (J.mode == 1) {
+    double E[kYR], O[kYR];
+#pragma unroll
+    for (int r = 0; r < kYR; ++r) E[r] = O[r] = 0.0;
+    const int a1 = min(j_end, J.N - 1);
+    int j = a0;
+    if (j < a1 && (j & 1)) {
+      const double v = __ldg(x + (long long)j * sk);
+#pragma unroll
+      for (int r = 0; r < kYR; ++r) {
+        O[r] = fma(v, twiddle(J.q, D, m[r]), O[r]);
+        step(m[r], inc[r]);
+      }
+      ++j;
+    }
+    for (; j + 1 < a1; j += 2) {
+      const double v0 = __ldg(x + (long long)j * sk), v1 = __ldg(x + (long long)(j + 1) * sk);
+#pragma unroll
+      for (int r = 0; r < kYR; ++r) {
+        E[r] = fma(v0, twiddle(J.q, D, m[r]), E[r]);
+        step(m[r], inc[r]);
+        O[r] = fma(v1, twiddle(J.q, D, m[r]), O[r]);
+        step(m[r], inc[r]);
+      }
+    }
+    if (j < a1) {
+      const double v = __ldg(x + (long long)j * sk);
+#pragma unroll
+      for (int r = 0; r < kYR; ++r) E[r] = fma(v, twiddle(J.q, D, m[r]), E[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < kYR; ++r) {
+      const int k = k0 + r;
+      if (k >= J.nlane) break;
+      double e = J.wm * E[r], o = J.wm * O[r];
+      if (J.jlo == 0 && 0 < j_end) e = fma(J.w0 * __ldg(x), twiddle(J.q, D, mod4d(J.off, D4)), e);
+      if (D >= J.jlo && D < j_end) {
+        const double t = J.wl * __ldg(x + (long long)D * sk) *
+                         twiddle(J.q, D, mod4d((long long)2 * D * k + J.off, D4));
+        if (D & 1) o += t;
+        else e += t;
+      }
+      put(k, e + o);
+      if (D - k != k) put(D - k, is_sin ? o - e : e - o);
+    }
+  } else if (J.mode == 2) {
+    double acc[kYR];
+#pragma unroll
+    for (int r = 0; r < kYR; ++r) acc[r] = 0.0;
+    // cos: even k pairs with u; sin: even k pairs with v
+    const int pe = (D + 1) / 2;  // interior pairs j < D - j
+    for (int j = 1; j < pe; ++j) {
+      const double xa = __ldg(x + (long long)j * sk), xb = __ldg(x + (long long)(D - j) * sk);
+      const double u = xa + xb, v = xa - xb;
+#pragma unroll
+      for (int r = 0; r < kYR; ++r) {
+        const bool use_v = (((k0 + r) & 1) == 0) != !is_sin;
+        acc[r] = fma(use_v ? v : u, twiddle(J.q, D, m[r]), acc[r]);
+        step(m[r], inc[r]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < kYR; ++r) {
+      const int k = k0 + r;
+      if (k >= J.nlane) break;
+      double t = J.wm * acc[r];
+      if (J.jlo == 0) {  // the end pair (0, D) with the end weight
+        const double xa = __ldg(x), xb = __ldg(x + (long long)D * sk);
+        t = fma(J.w0 * (((k & 1) == 0) ? xa + xb : xa - xb), twiddle(J.q, D, mod4d(J.off, D4)), t);
+      }
+      if ((D & 1) == 0) {
+        const int jm = D / 2;
+        if (jm >= J.jlo && jm < J.jhi)
+          t = fma(J.wm * __ldg(x + (long long)jm * sk),
+                  twiddle(J.q, D, mod4d((long long)2 * jm * k + J.off, D4)), t);
+      }
+      put(k, t);
+    }
+  } else {
+    double acc[kYR];
+#pragma unroll
+    for (int r = 0; r < kYR; ++r) acc[r] = 0.0;
+    const int a1 = min(j_end, J.N - 1);
+    for (int j = a0; j < a1; ++j) {
+      const double v = __ldg(x + (long long)j * sk);
+#pragma unroll
+      for (int r = 0; r < kYR; ++r) {
+        acc[r] = fma(v, twiddle(J.q, D, m[r]), acc[r]);
+        step(m[r], inc[r]);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < kYR; ++r) {
+      const int k = k0 + r;
+      if (k >= J.nout) break;
+      double t = J.wm * acc[r];
+      const int kk = J.ak * k + J.bk;
+      if (J.jlo == 0 && 0 < j_end) {
+        const int mm = mod4d((long long)J.bj * kk + J.off, D4);
+        t = fma(J.w0 * __ldg(x), twiddle(J.q, D, mm), t);
+      }
+      const int jl = J.N - 1;
+      if (jl > 0 && jl >= J.jlo && jl < j_end) {
+        const int mm = mod4d((long long)(J.aj * jl + J.bj) * kk + J.off, D4);
+        t = fma(J.wl * __ldg(x + (long long)jl * sk), twiddle(J.q, D, mm), t);
+      }
+      put(k, t);
+    }
   }
 }
 
@@ -1044,9 +1139,19 @@ void launch_batch_y(AxisBatch& in, const Tables& tb, cudaStream_t st) {
   if (b.njobs == 0) return;
   int total = 0;
   for (int i = 0; i < b.njobs; ++i) {
+    AxisJob& J = b.job[i];
+    const bool c1s1 = (J.aj == 2 && J.bj == 0 && J.ak == 1 && J.bk == 0);
+    J.mode = 0;
+    J.nlane = J.nout;
+    if (c1s1 && J.nout == J.N && J.D >= 4) {
+      J.mode = 1;
+      J.nlane = J.D / 2 + 1;
+    } else if (c1s1 && J.nin >= J.N && J.nout <= J.D / 2 + 1 && J.D >= 4 && J.w0 == J.wl) {
+      J.mode = 2;
+    }
     b.start[i] = total;
-    const int nlb = (b.job[i].nlines + kYThreads - 1) / kYThreads;
-    total += nlb * ((b.job[i].nout + kYR - 1) / kYR);
+    const int nlb = (J.nlines + kYThreads - 1) / kYThreads;
+    total += nlb * ((J.nlane + kYR - 1) / kYR);
   }
   b.start[b.njobs] = total;
   if (total > 0)
