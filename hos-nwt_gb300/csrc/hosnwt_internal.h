@@ -105,6 +105,8 @@ struct AxisJob {
   const double* win;         // optional input weights (first pass only):
   long long win_sl;          //   input j of line l is multiplied by win[j + l * win_sl]
   const double* q;           // quarter-wave table cos(pi*m/(2D)), m = 0..D
+  const double* ty;          // y passes: twiddle rows [j * ldy + k], k <= D/2 (or null)
+  int ldy;
   // work decomposition of the x pass (set by the launcher)
   int mode;                  // 0 direct, 1 output symmetry k <-> D-k, 2 input symmetry j <-> D-j
   int nlane;                 // lane outputs: tiles of 32 cover [0, nlane)
@@ -173,6 +175,10 @@ struct Tables {
   double* cs;                // scratch of the two-level passes (may be null)
   long long cs_cap;
   bool q_const = true;       // tables written before the first launch that reads them
+  // twiddle rows of the y passes (cos, sin kinds) for D = n2-1 and nd2-1
+  const double* ty_n2[2] = {nullptr, nullptr};
+  const double* ty_nd2[2] = {nullptr, nullptr};
+  int ldy_n2 = 0, ldy_nd2 = 0;
   // quarter-wave tables for D = n1-1, n2-1, nd1-1, nd2-1, n3_add
   const double* q_n1;
   const double* q_n2;
@@ -186,5 +192,9 @@ double measure_fp64_peak_gflops();
 
 // Build the quarter-wave table cos(pi*m/(2D)), m = 0..D, on the host.
 std::vector<double> quarter_table(int D);
+// Twiddle rows of a REDFT00 (sin_kind false) or RODFT00 y pass of length N:
+// row j holds cos(pi (2 j k + off) / (2D)) for k = 0..D/2 (off = 0 or 3D),
+// the same values as the quarter-wave table gives; *ld is the row length.
+std::vector<double> y_twiddle_rows(int N, bool sin_kind, int* ld);
 
 }  // namespace hos

@@ -627,6 +627,13 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
   d.q_nd1 = upload(c, quarter_table(nd1 - 1));
   d.q_nd2 = upload(c, quarter_table(std::max(nd2 - 1, 1)));
   d.q_add = upload(c, quarter_table(n3a));
+  if (n2 > 1) {
+    // twiddle rows of the direct y passes (cos and sin kinds, n2 and nd2)
+    for (int kind = 0; kind < 2; ++kind) {
+      c.tb.ty_n2[kind] = upload(c, y_twiddle_rows(n2, kind == 1, &c.tb.ldy_n2));
+      c.tb.ty_nd2[kind] = upload(c, y_twiddle_rows(nd2, kind == 1, &c.tb.ldy_nd2));
+    }
+  }
   c.tb.n1 = n1; c.tb.n2 = n2; c.tb.nd1 = nd1; c.tb.nd2 = nd2; c.tb.n3_add = n3a;
   {
     int dev = 0, sms = 0;

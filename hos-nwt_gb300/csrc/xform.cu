@@ -249,6 +249,17 @@ constexpr int kYR = 8;  // outputs per thread
 //           writes out[k] and out[D-k]
 //   mode 2: inputs are paired, u = x_j + x_{D-j}, v = x_j - x_{D-j}
 //           (outputs k <= D/2)
+// kYR consecutive twiddles of a y row (rows are 64-byte aligned)
+__device__ __forceinline__ void row8(const double* __restrict__ p, double (&t)[kYR]) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int i = 0; i < kYR / 2; ++i) {
+    const double2 v = __ldg(q + i);
+    t[2 * i] = v.x;
+    t[2 * i + 1] = v.y;
+  }
+}
+
 template <int NJ>
 __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatchT<NJ> b) {
   pdl_wait();
@@ -286,7 +297,92 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
     inc[r] = mod4d((long long)J.aj * kk, D4);
     m[r] = mod4d((long long)(J.aj * a0 + J.bj) * kk + J.off, D4);
   }
-  if (J.mode == 1) {
+  if (J.mode == 1 && J.ty) {
+    // twiddle rows: row j, columns k0 .. k0 + kYR - 1
+    const double* __restrict__ T = J.ty + k0;
+    const long long ld = J.ldy;
+    double E[kYR], O[kYR], t[kYR];
+#pragma unroll
+    for (int r = 0; r < kYR; ++r) E[r] = O[r] = 0.0;
+    const int a1 = min(j_end, J.N - 1);
+    int j = a0;
+    if (j < a1 && (j & 1)) {
+      const double v = __ldg(x + (long long)j * sk);
+      row8(T + j * ld, t);
+#pragma unroll
+      for (int r = 0; r < kYR; ++r) O[r] = fma(v, t[r], O[r]);
+      ++j;
+    }
+    for (; j + 1 < a1; j += 2) {
+      const double v0 = __ldg(x + (long long)j * sk), v1 = __ldg(x + (long long)(j + 1) * sk);
+      double t1[kYR];
+      row8(T + j * ld, t);
+      row8(T + (j + 1) * ld, t1);
+#pragma unroll
+      for (int r = 0; r < kYR; ++r) {
+        E[r] = fma(v0, t[r], E[r]);
+        O[r] = fma(v1, t1[r], O[r]);
+      }
+    }
+    if (j < a1) {
+      const double v = __ldg(x + (long long)j * sk);
+      row8(T + j * ld, t);
+#pragma unroll
+      for (int r = 0; r < kYR; ++r) E[r] = fma(v, t[r], E[r]);
+    }
+    double t0[kYR], tD[kYR];
+    row8(T, t0);
+    row8(T + D * ld, tD);
+#pragma unroll
+    for (int r = 0; r < kYR; ++r) {
+      const int k = k0 + r;
+      if (k >= J.nlane) break;
+      double e = J.wm * E[r], o = J.wm * O[r];
+      if (J.jlo == 0 && 0 < j_end) e = fma(J.w0 * __ldg(x), t0[r], e);
+      if (D >= J.jlo && D < j_end) {
+        const double tt = J.wl * __ldg(x + (long long)D * sk) * tD[r];
+        if (D & 1) o += tt;
+        else e += tt;
+      }
+      put(k, e + o);
+      if (D - k != k) put(D - k, is_sin ? o - e : e - o);
+    }
+  } else if (J.mode == 2 && J.ty) {
+    const double* __restrict__ T = J.ty + k0;
+    const long long ld = J.ldy;
+    double acc[kYR], t[kYR];
+#pragma unroll
+    for (int r = 0; r < kYR; ++r) acc[r] = 0.0;
+    const int pe = (D + 1) / 2;  // interior pairs j < D - j
+    for (int j = 1; j < pe; ++j) {
+      const double xa = __ldg(x + (long long)j * sk), xb = __ldg(x + (long long)(D - j) * sk);
+      const double u = xa + xb, v = xa - xb;
+      row8(T + j * ld, t);
+#pragma unroll
+      for (int r = 0; r < kYR; ++r) {
+        const bool use_v = (((k0 + r) & 1) == 0) != !is_sin;
+        acc[r] = fma(use_v ? v : u, t[r], acc[r]);
+      }
+    }
+    double t0[kYR], tm[kYR];
+    row8(T, t0);
+    row8(T + (D / 2) * ld, tm);
+#pragma unroll
+    for (int r = 0; r < kYR; ++r) {
+      const int k = k0 + r;
+      if (k >= J.nlane) break;
+      double tt = J.wm * acc[r];
+      if (J.jlo == 0) {
+        const double xa = __ldg(x), xb = __ldg(x + (long long)D * sk);
+        tt = fma(J.w0 * (((k & 1) == 0) ? xa + xb : xa - xb), t0[r], tt);
+      }
+      if ((D & 1) == 0) {
+        const int jm = D / 2;
+        if (jm >= J.jlo && jm < J.jhi) tt = fma(J.wm * __ldg(x + (long long)jm * sk), tm[r], tt);
+      }
+      put(k, tt);
+    }
+  } else if (J.mode == 1) {
     double E[kYR], O[kYR];
 #pragma unroll
     for (int r = 0; r < kYR; ++r) E[r] = O[r] = 0.0;
@@ -1174,6 +1270,22 @@ std::vector<double> quarter_table(int D) {
   return q;
 }
 
+std::vector<double> y_twiddle_rows(int N, bool sin_kind, int* ld) {
+  const int D = N - 1;
+  const int nk = D / 2 + 1;
+  *ld = (nk + 7) / 8 * 8;
+  const std::vector<double> q = quarter_table(D);
+  std::vector<double> t((size_t)N * *ld, 0.0);
+  const long long D4 = 4LL * D, off = sin_kind ? 3LL * D : 0;
+  for (int j = 0; j < N; ++j)
+    for (int k = 0; k < nk; ++k) {
+      const long long m = (2LL * j * k + off) % D4;
+      const long long mm = (m > 2LL * D) ? D4 - m : m;
+      t[(size_t)j * *ld + k] = (mm > D) ? -q[2 * D - mm] : q[mm];
+    }
+  return t;
+}
+
 void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* const* tmp,
                        cudaStream_t st) {
   AxisBatch bx{}, by{};
@@ -1215,6 +1327,8 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
     if (twod) {
       AxisJob& Y = by.job[by.njobs++];
       set_kind(Y, axis_kind(false, R.dir, R.csy), Ny, qy);
+      Y.ty = (R.grid == GRID_BIG) ? tb.ty_nd2[R.csy ? 1 : 0] : tb.ty_n2[R.csy ? 1 : 0];
+      Y.ldy = (R.grid == GRID_BIG) ? tb.ldy_nd2 : tb.ldy_n2;
       Y.in = tmp[r];
       Y.in_sk = R.nout1;
       Y.in_sl = 1;
@@ -1302,6 +1416,8 @@ void launch_y_f2s(const Tables& tb, const double* in, int nlines, long long y_st
   b.njobs = 1;
   AxisJob& J = b.job[0];
   set_kind(J, cs ? K_S1_F2S : K_C1_F2S, tb.n2, tb.q_n2);
+  J.ty = tb.ty_n2[cs ? 1 : 0];
+  J.ldy = tb.ldy_n2;
   J.in = in;
   J.in_sk = y_stride;
   J.in_sl = 1;
