@@ -726,6 +726,67 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatchT<N
   if (ncl > 1) cluster_sync_all();  // remote reads done before any CTA exits
 }
 
+// pass 2 for launches with many lines (the x passes of 3-D tanks):
+// CTA = (job, 32 outputs, group of lpc lines).  The B x 32 twiddle tile is
+// staged once for the group; each warp takes lines in turn and sums all of
+// their j2 terms, so no cross-warp reduction is needed.
+template <int NJ>
+__global__ void __launch_bounds__(kP2Threads) two_level_pass2_lines(const AxisBatchT<NJ> b, int lpc) {
+  extern __shared__ double sm2[];
+  int jb = 0;
+  while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
+  const AxisJob& J = b.job[jb];
+  const int A = J.A, B = J.B, D = J.D, D4 = 4 * D;
+  const int nkb = (J.nout + 31) / 32;
+  const int local = blockIdx.x - b.start[jb];
+  const int kb = local % nkb;
+  const int l0 = (local / nkb) * lpc;
+  const int k0 = kb * 32;
+  auto stage_twiddles = [&]() {
+    for (int t = threadIdx.x; t < B * 32; t += kP2Threads) {
+      const int j2 = t >> 5, k = k0 + (t & 31);
+      const int m = (int)((2u * (unsigned)j2 * (unsigned)k) % (unsigned)D4);
+      sm2[2 * t] = twiddle(J.q, D, m);
+      sm2[2 * t + 1] = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
+    }
+  };
+  if (b.early) stage_twiddles();
+  pdl_wait();
+  if (!b.early) stage_twiddles();
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int k = k0 + lane;
+  const bool on = k < J.nout && k >= J.klo && k < J.khi;
+  int kp = k % (2 * A);
+  double ssign = 1.0;
+  if (kp > A) {
+    kp = 2 * A - kp;
+    ssign = -1.0;
+  }
+  const bool is_sin = (J.off != 0);
+  const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
+  const double2* tw = reinterpret_cast<const double2*>(sm2) + lane;
+  const int l1 = min(J.nlines, l0 + lpc);
+  for (int line = l0 + warp; line < l1; line += kP2Warps) {
+    const double* cs = J.cs + ((long long)line * B * (A + 1) + kp) * 2;
+    double acc = 0.0;
+    if (on) {
+#pragma unroll 4
+      for (int j2 = 0; j2 < B; ++j2) {
+        const long long o = (long long)j2 * (A + 1) * 2;
+        const double C = __ldcg(cs + o), S = ssign * __ldcg(cs + o + 1);
+        const double2 t = tw[j2 * 32];
+        if (is_sin) acc = fma(t.x, S, fma(t.y, C, acc));
+        else acc = fma(t.x, C, fma(-t.y, S, acc));
+      }
+    }
+    if (k < J.nout) {
+      double* out = J.out + (long long)line * J.out_sl + (long long)k * J.out_sk;
+      *out = on ? acc * sc * J.gscale : 0.0;
+    }
+  }
+}
+
 // Two-level y passes (REDFT00 / RODFT00 along a strided axis, lines
 // contiguous): the same split as above, with lanes owning lines so that
 // every load and store is coalesced and every twiddle is warp-uniform.
@@ -844,18 +905,24 @@ __global__ void __launch_bounds__(kYT) ytl_pass2(const AxisBatchT<NJ> b) {
   const bool is_sin = (J.off != 0);
   const long long nl = J.nlines;
   const double* cs = J.cs + (long long)kp * 2 * nl + line;
+  // outputs of this class below nout (uniform over the CTA)
+  int nq = 0;
+  while (nq < kYQ && ytl_k(nq, A, kp, pair) < J.nout) ++nq;
   double acc[kYQ];
 #pragma unroll
   for (int oi = 0; oi < kYQ; ++oi) acc[oi] = 0.0;
+#pragma unroll 2
   for (int j2 = 0; j2 < B; ++j2) {
     const long long base = (long long)j2 * (A + 1) * 2 * nl;
     const double C = __ldcg(cs + base), S = __ldcg(cs + base + nl);
-    const double* t = tw + 2 * j2 * kYQ;
+    const double2* t = reinterpret_cast<const double2*>(tw) + j2 * kYQ;
 #pragma unroll
     for (int oi = 0; oi < kYQ; ++oi) {
-      const double Ss = (pair && (oi & 1)) ? -S : S;
-      const double cw = t[2 * oi], sw = t[2 * oi + 1];
-      acc[oi] = is_sin ? fma(cw, Ss, fma(sw, C, acc[oi])) : fma(cw, C, fma(-sw, Ss, acc[oi]));
+      if (oi < nq) {
+        const double Ss = (pair && (oi & 1)) ? -S : S;
+        const double2 w = t[oi];
+        acc[oi] = is_sin ? fma(w.x, Ss, fma(w.y, C, acc[oi])) : fma(w.x, C, fma(-w.y, Ss, acc[oi]));
+      }
     }
   }
   double* out = J.out + (long long)line * J.out_sl;
@@ -1042,6 +1109,32 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
       launch_pdl_cluster(two_level_pass1<NJ>, dim3(total), dim3(kP1Threads), smem1, ncl1, st, shrink<NJ>(b),
                          kpc, ncl1);
     });
+  // pass 2 with many lines per job: line groups share their staged twiddles
+  int minl = 1 << 30;
+  for (int i = 0; i < b.njobs; ++i) minl = std::min(minl, b.job[i].nlines);
+  if (minl >= 16) {
+    static bool attr_l = false;
+    if (!attr_l) {
+      for (int nj : {1, 2, 4, 8, kMaxJobs})
+        with_capacity(nj, [&](auto c) { allow_smem(two_level_pass2_lines<decltype(c)::value>); });
+      attr_l = true;
+    }
+    long long blocks = 0;
+    for (int i = 0; i < b.njobs; ++i) blocks += (long long)b.job[i].nlines * ((b.job[i].nout + 31) / 32);
+    const int lpc = (int)std::min<long long>(16, std::max<long long>(4, blocks / (4LL * std::max(nsm, 1))));
+    total = 0;
+    for (int i = 0; i < b.njobs; ++i) {
+      b.start[i] = total;
+      total += ((b.job[i].nlines + lpc - 1) / lpc) * ((b.job[i].nout + 31) / 32);
+      smem2 = std::max(smem2, pass2_smem(b.job[i], 1));
+    }
+    b.start[b.njobs] = total;
+    with_capacity(b.njobs, [&](auto c) {
+      constexpr int NJ = decltype(c)::value;
+      launch_pdl(two_level_pass2_lines<NJ>, dim3(total), dim3(kP2Threads), smem2, st, shrink<NJ>(b), lpc);
+    });
+    return;
+  }
   // pass 2: 32 outputs per cluster, the j2 sums split over a cluster when
   // there are few output blocks
   long long blocks = 0;
