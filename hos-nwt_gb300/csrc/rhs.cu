@@ -153,6 +153,9 @@ __global__ void k_pow_run(PowArgs a, long long n) {
 // Products of HOSphis_modes' quadratic terms accumulated per dealiasing
 // group: out[g] = sum over the group's terms of s * x * y (x, y big-grid
 // fields); the terms of each group keep the reference's order.
+// Optionally also the outer sums oscale * (sum of the groups q with
+// outer_of[q] == u), u < nouter: the geta2phiz2 sums of groups that are
+// not dealiased themselves, in the order of k_sum_fields.
 struct GroupTerms {
   const double* x[48];
   const double* y[48];
@@ -161,6 +164,10 @@ struct GroupTerms {
   int nterm;
   double* out[16];
   int ngroup;
+  int outer_of[16];
+  double* out_outer[4];
+  const double* oscale;
+  int nouter;
 };
 __global__ void k_group_products(GroupTerms g, long long n) {
   pdl_wait();
@@ -175,7 +182,23 @@ __global__ void k_group_products(GroupTerms g, long long n) {
     for (int q = 0; q < 16; ++q)
       if (q == g.group[t]) acc[q] += v;
   }
-  for (int q = 0; q < g.ngroup; ++q) g.out[q][i] = acc[q];
+#pragma unroll
+  for (int q = 0; q < 16; ++q)
+    if (q < g.ngroup) g.out[q][i] = acc[q];
+  if (g.nouter > 0) {
+    double os[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      if (q >= g.ngroup) break;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (u == g.outer_of[q]) os[u] += acc[q];
+    }
+    const double sc = g.oscale[i];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (u < g.nouter) g.out_outer[u][i] = sc * os[u];
+  }
 }
 
 // out = sum of listed fields, optionally times gradeta2 (scale field)
@@ -1205,34 +1228,60 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   for (int g = 0; g < gt.ngroup; ++g) gt.out[g] = d.grp[g];
   AssembleArgs aa{};
   aa.ng1 = aa.ng2 = aa.nt1 = 0;
+  // fields dealiased together after the products
+  std::vector<std::pair<int, double*>> dl;
+  for (int q = 0; q < 16; ++q) gt.outer_of[q] = -1;
+  gt.nouter = 0;
+  gt.oscale = d.gradeta2;
   if (gt.ngroup > 0) {
-    E.ew(k_group_products, nB, gt, nB);
-    {
-      std::vector<std::pair<int, double*>> dl;
+    // geta2phiz2: gradeta2 times the kind-2 groups, dealiased by outer class.
+    // When no kind-2 group is dealiased itself, the products kernel forms
+    // these sums too and everything is dealiased in one batch.
+    bool fused = true;
+    for (int g = 0; g < gt.ngroup; ++g)
+      if (gkind[g] == 2 && gc1[g] != 0) fused = false;
+    if (fused) {
+      for (int c2 = 0; c2 < 4; ++c2) {
+        bool any = false;
+        for (int g = 0; g < gt.ngroup; ++g)
+          if (gkind[g] == 2 && gc2[g] == c2) {
+            gt.outer_of[g] = gt.nouter;
+            any = true;
+          }
+        if (!any) continue;
+        double* o = d.grp[gt.ngroup + gt.nouter];
+        gt.out_outer[gt.nouter++] = o;
+        dl.push_back({c2, o});
+        aa.g2[aa.ng2++] = o;
+      }
+      E.ew(k_group_products, nB, gt, nB);
       for (int g = 0; g < gt.ngroup; ++g) dl.push_back({gc1[g], d.grp[g]});
-      E.dealias_many(dl);
+    } else {
+      E.ew(k_group_products, nB, gt, nB);
+      {
+        std::vector<std::pair<int, double*>> dl1;
+        for (int g = 0; g < gt.ngroup; ++g) dl1.push_back({gc1[g], d.grp[g]});
+        E.dealias_many(dl1);
+      }
+      int nu_ = 0;
+      for (int c2 = 0; c2 < 4; ++c2) {
+        SumArgs sa{};
+        sa.nin = 0;
+        for (int g = 0; g < gt.ngroup; ++g)
+          if (gkind[g] == 2 && gc2[g] == c2) sa.in[sa.nin++] = d.grp[g];
+        if (sa.nin == 0) continue;
+        sa.scale = d.gradeta2;
+        sa.out = d.grp[gt.ngroup + nu_];
+        E.ew(k_sum_fields, nB, sa, nB);
+        dl.push_back({c2, sa.out});
+        aa.g2[aa.ng2++] = sa.out;
+        nu_++;
+      }
     }
     for (int g = 0; g < gt.ngroup; ++g) {
       if (gkind[g] == 0) aa.g1[aa.ng1++] = d.grp[g];
       else aa.t1[aa.nt1++] = d.grp[g];
     }
-    // geta2phiz2: gradeta2 times the kind-2 groups, dealiased by outer class
-    std::vector<std::pair<int, double*>> dl2;
-    int nu_ = 0;
-    for (int c2 = 0; c2 < 4; ++c2) {
-      SumArgs sa{};
-      sa.nin = 0;
-      for (int g = 0; g < gt.ngroup; ++g)
-        if (gkind[g] == 2 && gc2[g] == c2) sa.in[sa.nin++] = d.grp[g];
-      if (sa.nin == 0) continue;
-      sa.scale = d.gradeta2;
-      sa.out = d.grp[gt.ngroup + nu_];
-      E.ew(k_sum_fields, nB, sa, nB);
-      dl2.push_back({c2, sa.out});
-      aa.g2[aa.ng2++] = sa.out;
-      nu_++;
-    }
-    E.dealias_many(dl2);
   }
 
   // 7. free-surface terms, filters to the n grid, final RHS
@@ -1242,10 +1291,12 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   if (E.dealias_on(2)) {
     E.ew(k_fs_products, nB, (const double*)d.etax, (const double*)d.etay, (const double*)d.phisx,
          (const double*)d.phisy, d.tbig, d.tbig2, nB);
-    E.dealias_many({{E.dclass(2), d.tbig}, {E.dclass(2), d.tbig2}});
+    dl.push_back({E.dclass(2), d.tbig});
+    dl.push_back({E.dclass(2), d.tbig2});
     aa.detext = d.tbig;
     aa.dphext = d.tbig2;
   }
+  E.dealias_many(dl);
   aa.nphizm = 0;
   for (int j = 1; j <= M - 1; ++j) aa.phizm[aa.nphizm++] = d.phizm[j];
   aa.phizmM = d.phizm[M];

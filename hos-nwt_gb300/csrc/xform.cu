@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatchT<
   }
 }
 
-constexpr int kYThreads = 128;
+constexpr int kYThreads = 64;
 constexpr int kYR = 8;  // outputs per thread
 
 // y pass: one thread = one line (consecutive lines are contiguous in memory)
