@@ -1152,6 +1152,12 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     cudaEventRecord(c.ev_pow, sp);
   }
   bool pow_joined = false;
+  // Dealiasing of phizm(iHOS): the recursion goes on with the undealiased
+  // phimext, so intermediate orders are dealiased on the third stream (joined
+  // before the quadratic products) and the last order, which only the
+  // assembly reads, joins the batch after the products.
+  std::vector<std::pair<int, double*>> dl_late;
+  bool side_dealias = false;
 
   // 4. HOS recursion (HOSphis_modes)
   std::vector<int> ext1(M + 2, nd1), ext2(M + 2, nd2);
@@ -1168,7 +1174,17 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
       aa.etapm[j - 1] = d.etapm[j - 1];
     }
     E.ew(k_hos_accum, nB, aa, d.phimext, d.phizm[iHOS], nB);
-    if (iHOS > 1) E.dealias(iHOS, d.phizm[iHOS]);
+    if (iHOS > 1 && E.dealias_on(iHOS)) {
+      if (iHOS == M) {
+        dl_late.push_back({E.dclass(M), d.phizm[M]});
+      } else {
+        cudaEventRecord(c.ev_acc, st);
+        cudaStreamWaitEvent(c.st3, c.ev_acc, 0);
+        Enq Pd(c, c.st3, c.tb3, d.xtmp3, &d.ptmp, 1);
+        Pd.dealias(iHOS, d.phizm[iHOS]);
+        side_dealias = true;
+      }
+    }
     if (iHOS < M) {
       const int o = iHOS + 1;
       const int e1 = E.act_x(o) ? n1 : nd1;
@@ -1185,6 +1201,10 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     }
   }
   if (!pow_joined) cudaStreamWaitEvent(st, c.ev_pow, 0);
+  if (side_dealias) {
+    cudaEventRecord(c.ev_dl, c.st3);
+    cudaStreamWaitEvent(st, c.ev_dl, 0);
+  }
   // Quadratic terms of HOSphis_modes (resol_HOS.f90:797-905): every term is
   // dealiased at its order; dealiasing is linear, so terms are summed per
   // dealiasing class first (class = which directions the order truncates).
@@ -1229,7 +1249,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   AssembleArgs aa{};
   aa.ng1 = aa.ng2 = aa.nt1 = 0;
   // fields dealiased together after the products
-  std::vector<std::pair<int, double*>> dl;
+  std::vector<std::pair<int, double*>> dl = dl_late;
   for (int q = 0; q < 16; ++q) gt.outer_of[q] = -1;
   gt.nouter = 0;
   gt.oscale = d.gradeta2;

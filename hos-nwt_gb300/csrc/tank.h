@@ -119,6 +119,7 @@ struct Ctx {
   cudaStream_t st2 = nullptr;     // wavemaker branch of each right-hand side
   cudaStream_t st3 = nullptr;     // eta powers and |grad eta|^2 with their dealiasing
   cudaEvent_t ev_fork = nullptr, ev_eta = nullptr, ev_join = nullptr, ev_pow = nullptr;
+  cudaEvent_t ev_acc = nullptr, ev_dl = nullptr;  // intermediate-order dealiasing
   cudaGraphExec_t step_graph = nullptr;
   double time_cur = 0.0;
   int endramp = 0;
