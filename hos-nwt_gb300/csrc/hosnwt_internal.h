@@ -107,6 +107,7 @@ struct AxisJob {
   const double* q;           // quarter-wave table cos(pi*m/(2D)), m = 0..D
   const double* ty;          // y passes: twiddle rows [j * ldy + k], k <= D/2 (or null)
   int ldy;
+  int epi;                   // 1: the batch's AccEpi follows each output write
   // work decomposition of the x pass (set by the launcher)
   int mode;                  // 0 direct, 1 output symmetry k <-> D-k, 2 input symmetry j <-> D-j
   int nlane;                 // lane outputs: tiles of 32 cover [0, nlane)
@@ -122,6 +123,33 @@ struct AxisJob {
 
 constexpr int kMaxJobs = 16;
 
+// HOS order accumulation (HOSphis_modes, resol_HOS.f90:716-764) fused into
+// the final pass of the transform that produces its first term z1 =
+// phizi(iHOS, 1): at every output element e,
+//   phimext[e] = -sum_{j=iHOS..2} z_j[e] eta_{j-1}[e] - z1 eta_0[e]
+//   phizm[e]   =  sum_{j=iHOS..2} z_j[e] eta_{j-2}[e] + z1
+// in the order of k_hos_accum.  z[j-1] = phizi(iHOS+1-j, j), e[j-1] = eta^j/j!.
+constexpr int kAccMax = 8;
+struct AccEpi {
+  int iHOS;
+  const double* z[kAccMax];
+  const double* e[kAccMax];
+  double* phimext;
+  double* phizm;
+};
+#if defined(__CUDACC__)
+__device__ __forceinline__ void acc_epilogue(const AccEpi& a, long long i, double z1) {
+  double pm = 0.0, pz = 0.0;
+  for (int j = a.iHOS; j >= 2; --j) {
+    const double z = __ldcg(a.z[j - 1] + i);
+    pm = pm - z * __ldcg(a.e[j - 1] + i);
+    pz = pz + z * __ldcg(a.e[j - 2] + i);
+  }
+  a.phimext[i] = pm - z1 * __ldcg(a.e[0] + i);
+  a.phizm[i] = pz + z1;
+}
+#endif
+
 // A batch of jobs for one launch.  Kernels take the batch by value as their
 // parameters, whose size costs launch time, so a launch passes the smallest
 // capacity NJ (1, 2, 4, 8 or kMaxJobs) that holds its jobs.
@@ -132,6 +160,7 @@ struct AxisBatchT {
   int njobs;
   int early;                 // 1: the twiddle tables are constant and are staged
                              //    before waiting for the previous kernel
+  AccEpi acc;                // applied to the outputs of jobs with epi set
 };
 using AxisBatch = AxisBatchT<kMaxJobs>;
 
@@ -150,6 +179,7 @@ struct XfReq {
   double scale;
   const double* win = nullptr;  // optional weights: input (i1, i2) times win[i1 + win_ld * i2]
   int win_ld = 0;
+  const AccEpi* acc = nullptr;  // optional accumulation on the outputs (final pass)
 };
 
 struct Tables;

@@ -717,6 +717,8 @@ int alloc_device(Ctx& c) {
   if (cudaStreamCreateWithFlags(&c.st3, cudaStreamNonBlocking) != cudaSuccess) return 1;
   for (cudaEvent_t* e : {&c.ev_fork, &c.ev_eta, &c.ev_join, &c.ev_pow, &c.ev_acc, &c.ev_dl})
     if (cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) return 1;
+  for (cudaEvent_t& e : c.ev_pw)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return 1;
   d.sc = dalloc<double>(c, SC_COUNT);
   const size_t nparts = 10 * ((S + 255) / 256) + (std::max(nB, nN) + 63) / 64 + 1024;
   d.part = dalloc<double>(c, nparts);
@@ -742,6 +744,10 @@ void free_device(Ctx& c) {
   for (cudaEvent_t e : {c.ev_fork, c.ev_eta, c.ev_join, c.ev_pow, c.ev_acc, c.ev_dl})
     if (e) cudaEventDestroy(e);
   c.ev_fork = c.ev_eta = c.ev_join = c.ev_pow = c.ev_acc = c.ev_dl = nullptr;
+  for (cudaEvent_t& e : c.ev_pw) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
   for (cudaStream_t* s : {&c.st2, &c.st3}) {
     if (*s) cudaStreamDestroy(*s);
     *s = nullptr;

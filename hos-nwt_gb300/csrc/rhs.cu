@@ -1128,6 +1128,9 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   W.xf({W.F2S_B(d.pmode[0], n1, n1, n2, d.pxe), W.F2S_B(d.pmode[1], n1, n1, n2, d.pye),
         W.F2S_B(d.pmode[2], n1, n1, n2, d.pze)});
   cudaEventRecord(c.ev_join, sw);
+  // event after which eta^o/o! is final (orders >= 2), -1: the full join
+  std::vector<int> pw_ev(M + 2, -1);
+  int npw = 0;
   // 3. powers eta^j / j! with partial dealiasing (one kernel per run of
   //    orders up to the next order that is dealiased) and |grad eta|^2.
   //    Order 1 of the HOS recursion needs none of them, so they run on a
@@ -1144,7 +1147,20 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
       pa.j0 = j;
       pa.j1 = jend;
       Pw.ew(k_pow_run, nB, pa, nB);
-      Pw.dealias(jend, d.etapm[jend - 1]);
+      // orders j+1 .. jend are final here, except jend when it is dealiased
+      const bool dl_end = E.dealias_on(jend);
+      if (npw < Ctx::kPowEvents) {
+        cudaEventRecord(c.ev_pw[npw], sp);
+        for (int o = j + 1; o <= jend - (dl_end ? 1 : 0); ++o) pw_ev[o] = npw;
+        ++npw;
+      }
+      if (dl_end) {
+        Pw.dealias(jend, d.etapm[jend - 1]);
+        if (npw < Ctx::kPowEvents) {
+          cudaEventRecord(c.ev_pw[npw], sp);
+          pw_ev[jend] = npw++;
+        }
+      }
       j = jend;
     }
     Pw.ew(k_sq2, nB, (const double*)d.etax, (const double*)d.etay, d.gradeta2, nB);
@@ -1161,19 +1177,46 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
 
   // 4. HOS recursion (HOSphis_modes)
   std::vector<int> ext1(M + 2, nd1), ext2(M + 2, nd2);
-  for (int iHOS = 1; iHOS <= M; ++iHOS) {
-    if (iHOS == 2) {
+  // In 3-D tanks, orders 2 .. kAccMax are accumulated by the final pass of
+  // the F2S batch that produces their first term (AccEpi), which saves a
+  // pass over the big grid per order; order 1 follows batch A, which also
+  // produces eta, so it keeps its own kernel.  In 2-D tanks the separate
+  // kernel is cheaper than the epilogue's dependent loads.
+  const bool fuse_acc = (n2 > 1);
+  auto join_pow = [&]() {
+    if (!pow_joined) {
       cudaStreamWaitEvent(st, c.ev_pow, 0);
       pow_joined = true;
     }
-    AccArgs aa{};
-    aa.iHOS = iHOS;
-    for (int j = 1; j <= iHOS; ++j) {
-      const int m = iHOS + 1 - j;
-      aa.phizi[j - 1] = d.phizi[(m - 1) * M + (j - 1)];
-      aa.etapm[j - 1] = d.etapm[j - 1];
+  };
+  // wait until eta^j/j! is final for every j <= o
+  int pw_waited = -1;
+  auto wait_powers = [&](int o) {
+    for (int q = 2; q <= o; ++q)
+      if (pw_ev[q] < 0) {
+        join_pow();
+        return;
+      }
+    if (pow_joined || o < 2) return;
+    const int idx = pw_ev[o];
+    if (idx > pw_waited) {
+      cudaStreamWaitEvent(st, c.ev_pw[idx], 0);
+      pw_waited = idx;
     }
-    E.ew(k_hos_accum, nB, aa, d.phimext, d.phizm[iHOS], nB);
+  };
+  std::vector<AccEpi> epis(M + 2);
+  for (int iHOS = 1; iHOS <= M; ++iHOS) {
+    if (iHOS == 1 || iHOS > kAccMax || !fuse_acc) {
+      wait_powers(iHOS);
+      AccArgs aa{};
+      aa.iHOS = iHOS;
+      for (int j = 1; j <= iHOS; ++j) {
+        const int m = iHOS + 1 - j;
+        aa.phizi[j - 1] = d.phizi[(m - 1) * M + (j - 1)];
+        aa.etapm[j - 1] = d.etapm[j - 1];
+      }
+      E.ew(k_hos_accum, nB, aa, d.phimext, d.phizm[iHOS], nB);
+    }
     if (iHOS > 1 && E.dealias_on(iHOS)) {
       if (iHOS == M) {
         dl_late.push_back({E.dclass(M), d.phizm[M]});
@@ -1197,6 +1240,19 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
       for (int j = 1; j <= M + 1 - o; ++j)
         rq.push_back(E.weighted(E.F2S_B(d.aHOS[o], nd1, e1, e2, d.phizi[(o - 1) * M + (j - 1)]),
                                 d.kth_ext + (long long)nd1 * nd2 * (j - 1), nd1));
+      if (fuse_acc && o <= kAccMax) {
+        // order o's accumulation on the outputs of its first term, phizi(o, 1)
+        AccEpi& ae = epis[o];
+        ae.iHOS = o;
+        for (int j = 1; j <= o; ++j) {
+          ae.z[j - 1] = d.phizi[(o - j) * M + (j - 1)];
+          ae.e[j - 1] = d.etapm[j - 1];
+        }
+        ae.phimext = d.phimext;
+        ae.phizm = d.phizm[o];
+        rq[0].acc = &ae;
+        wait_powers(o);
+      }
       E.xf(rq);
     }
   }

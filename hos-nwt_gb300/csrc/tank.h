@@ -120,6 +120,8 @@ struct Ctx {
   cudaStream_t st3 = nullptr;     // eta powers and |grad eta|^2 with their dealiasing
   cudaEvent_t ev_fork = nullptr, ev_eta = nullptr, ev_join = nullptr, ev_pow = nullptr;
   cudaEvent_t ev_acc = nullptr, ev_dl = nullptr;  // intermediate-order dealiasing
+  static constexpr int kPowEvents = 8;
+  cudaEvent_t ev_pw[kPowEvents] = {};  // eta powers final up to a given order
   cudaGraphExec_t step_graph = nullptr;
   double time_cur = 0.0;
   int endramp = 0;

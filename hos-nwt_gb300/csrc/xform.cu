@@ -231,11 +231,23 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatchT<
     const bool is_sin = (J.off != 0);
     const double yk = E + O;
     const double yr = is_sin ? (O - E) : (E - O);
-    if (k < J.nout) out[(long long)k * J.out_sk] = active(k) ? yk * scale(k) * g : 0.0;
+    if (k < J.nout) {
+      const double v = active(k) ? yk * scale(k) * g : 0.0;
+      out[(long long)k * J.out_sk] = v;
+      if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, v);
+    }
     const int kr = D - k;
-    if (kr != k && kr < J.nout) out[(long long)kr * J.out_sk] = active(kr) ? yr * scale(kr) * g : 0.0;
+    if (kr != k && kr < J.nout) {
+      const double v = active(kr) ? yr * scale(kr) * g : 0.0;
+      out[(long long)kr * J.out_sk] = v;
+      if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)kr * J.out_sk, v);
+    }
   } else {
-    if (k < J.nout) out[(long long)k * J.out_sk] = active(k) ? E * scale(k) * g : 0.0;
+    if (k < J.nout) {
+      const double v = active(k) ? E * scale(k) * g : 0.0;
+      out[(long long)k * J.out_sk] = v;
+      if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, v);
+    }
   }
 }
 
@@ -283,7 +295,9 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
     if (k >= J.nout) return;
     const bool active = (k >= J.klo) && (k < J.khi);
     const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
-    out[(long long)k * J.out_sk] = active ? v * sc * J.gscale : 0.0;
+    const double y = active ? v * sc * J.gscale : 0.0;
+    out[(long long)k * J.out_sk] = y;
+    if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, y);
   };
   auto step = [&](int& m, int inc) {
     m += inc;
@@ -721,7 +735,9 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatchT<N
     for (int r = 1; r < ncl; ++r) y += ld_cluster(fin + lane, (unsigned)r);
     double* out = J.out + (long long)line * J.out_sl + (long long)k * J.out_sk;
     const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
-    *out = on ? y * sc * J.gscale : 0.0;
+    const double v = on ? y * sc * J.gscale : 0.0;
+    *out = v;
+    if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, v);
   }
   if (ncl > 1) cluster_sync_all();  // remote reads done before any CTA exits
 }
@@ -782,7 +798,9 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2_lines(const AxisBa
     }
     if (k < J.nout) {
       double* out = J.out + (long long)line * J.out_sl + (long long)k * J.out_sk;
-      *out = on ? acc * sc * J.gscale : 0.0;
+      const double v = on ? acc * sc * J.gscale : 0.0;
+      *out = v;
+      if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, v);
     }
   }
 }
@@ -932,7 +950,9 @@ __global__ void __launch_bounds__(kYT) ytl_pass2(const AxisBatchT<NJ> b) {
     if (k < J.nout) {
       const bool on = k >= J.klo && k < J.khi;
       const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
-      out[(long long)k * J.out_sk] = on ? acc[oi] * sc * J.gscale : 0.0;
+      const double v = on ? acc[oi] * sc * J.gscale : 0.0;
+      out[(long long)k * J.out_sk] = v;
+      if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, v);
     }
   }
 }
@@ -1025,6 +1045,7 @@ AxisBatchT<NJ> shrink(const AxisBatch& b) {
   for (int i = 0; i <= b.njobs; ++i) s.start[i] = b.start[i];
   s.njobs = b.njobs;
   s.early = b.early;
+  s.acc = b.acc;
   return s;
 }
 template <typename F>
@@ -1303,6 +1324,7 @@ void launch_ytl(AxisBatch& b, bool early, cudaStream_t st) {
 void launch_batch_y(AxisBatch& in, const Tables& tb, cudaStream_t st) {
   AxisBatch b{}, b2{};
   b.njobs = b2.njobs = 0;
+  b.acc = b2.acc = in.acc;
   long long cs_used = 0;
   for (int i = 0; i < in.njobs; ++i) {
     AxisJob J = in.job[i];
@@ -1383,6 +1405,8 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
                        cudaStream_t st) {
   AxisBatch bx{}, by{};
   bx.njobs = by.njobs = 0;
+  for (int r = 0; r < nreq; ++r)
+    if (reqs[r].acc) bx.acc = by.acc = *reqs[r].acc;
   for (int r = 0; r < nreq; ++r) {
     const XfReq& R = reqs[r];
     int Nx, Ny;
@@ -1402,6 +1426,7 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
     X.win_sl = R.win_ld;
     X.nin = R.nin1;
     X.gscale = twod ? 1.0 : R.scale;
+    X.epi = (!twod && R.acc) ? 1 : 0;
     if (twod) {
       // the y-sin plans zero the boundary columns of the input and output
       // (fourier_FFTW.f90:282-285, 296-299): skip those lines here
@@ -1420,6 +1445,7 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
     if (twod) {
       AxisJob& Y = by.job[by.njobs++];
       set_kind(Y, axis_kind(false, R.dir, R.csy), Ny, qy);
+      Y.epi = R.acc ? 1 : 0;
       Y.ty = (R.grid == GRID_BIG) ? tb.ty_nd2[R.csy ? 1 : 0] : tb.ty_n2[R.csy ? 1 : 0];
       Y.ldy = (R.grid == GRID_BIG) ? tb.ldy_nd2 : tb.ldy_n2;
       Y.in = tmp[r];
@@ -1437,6 +1463,7 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
   // two-level passes for the jobs whose length factors well
   AxisBatch b2{}, bd{};
   b2.njobs = bd.njobs = 0;
+  b2.acc = bd.acc = bx.acc;
   long long cs_used = 0;
   for (int i = 0; i < bx.njobs; ++i) {
     AxisJob J = bx.job[i];
