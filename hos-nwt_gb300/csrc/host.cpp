@@ -381,6 +381,10 @@ static int wave_cfg(Ctx& c, const char* wave_dir) {
   for (int i3 = 0; i3 < P.n3; ++i3) c.gzed[i3] = gzed_fn(P, c.cz[i3]);
   if (P.icase == 1) return HOSNWT_OK;
   wave_init(w, typ, hinge);
+  if (!w.k.empty()) {
+    c.k_mono = w.k[0];
+    if (std::fabs(c.k_mono) < TINY && w.k.size() > 1) c.k_mono = w.k[1];
+  }
   // wmk_ini (wavemaking.f90:37-175), full-width wavemaker
   int n_max = std::max(1, (int)std::floor(w.clock * std::sqrt(G / w.depth)));
   n_max = (1 << w.rnum) / n_max;
@@ -1022,6 +1026,20 @@ static std::string fortran_ES(double v, int w, int d) {
   return buf;
 }
 
+// Fortran Fw.d and Iw: asterisks when the value does not fit in w
+static std::string fortran_F(double v, int w, int d) {
+  char buf[64];
+  const int n = std::snprintf(buf, sizeof buf, "%*.*f", w, d, v);
+  if (n > w || !std::isfinite(v)) return std::string(w, '*');
+  return buf;
+}
+static std::string fortran_I(long long v, int w) {
+  char buf[32];
+  const int n = std::snprintf(buf, sizeof buf, "%*lld", w, v);
+  if (n > w) return std::string(w, '*');
+  return buf;
+}
+
 static std::string rjust(const std::string& s, size_t w) {
   if (s.size() >= w) return s.substr(0, w);
   return std::string(w - s.size(), ' ') + s;
@@ -1176,10 +1194,55 @@ extern "C" int hosnwt_run(hosnwt_ctx* h, const char* results_dir) {
     std::fprintf(fv, dimensional ? "VARIABLES=\"time\", \"voltot\", \"enepot\", \"enekin\", \"enetot\"\n"
                                  : "VARIABLES=\"time*sqrt(g/h)\", \"voltot\", \"enepot\", \"enekin\", \"enetot\"\n");
   }
+  // 3d.dat (i3d = 1): free-surface zones (output.f90:47-56, 291-345)
+  FILE* f3 = nullptr;
+  if (results_dir && c.in.i3d == 1) {
+    const std::string path = std::string(results_dir) + "/3d.dat";
+    f3 = std::fopen(path.c_str(), "w");
+    if (!f3) {
+      if (fp) std::fclose(fp);
+      if (fv) std::fclose(fv);
+      return fail(c, HOSNWT_ERR_IO, "cannot open %s", path.c_str());
+    }
+    write_input(f3, c);
+    std::fprintf(f3, " TITLE=\" 3D free surface elevation \"\n");
+    std::fprintf(f3, dimensional ? "VARIABLES=\"x\",\"y\",\"eta\",\"phis\"\n"
+                                 : "VARIABLES=\"x/h\",\"y/h\",\"eta/h\",\"phis*sqrt(h/g)/h**2\"\n");
+  }
+  const size_t nN = (size_t)P.n1 * P.n2;
+  std::vector<double> eta_h, phis_h;
+  auto write_3d = [&]() {
+    eta_h.resize(nN);
+    phis_h.resize(nN);
+    cudaMemcpy(eta_h.data(), c.d.eta, nN * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(phis_h.data(), c.d.phis, nN * sizeof(double), cudaMemcpyDeviceToHost);
+    const bool first = std::fabs(c.time_cur) < TINY;
+    std::fprintf(f3, "ZONE SOLUTIONTIME = %s%s I=%s, J=%s\n", fortran_F(c.time_cur * t_adim, 6, 2).c_str(),
+                 first ? "," : ", D=(1,2),", fortran_I(P.n1, 4).c_str(), fortran_I(P.n2, 4).c_str());
+    for (int i2 = 0; i2 < P.n2; ++i2)
+      for (int i1 = 0; i1 < P.n1; ++i1) {
+        const size_t i = i1 + (size_t)P.n1 * i2;
+        if (first) {
+          std::fprintf(f3, "%s %s %s %s \n", fortran_F(c.cx[i1] * x_adim, 10, 5).c_str(),
+                       fortran_F(c.cy[i2] * x_adim, 10, 5).c_str(), fortran_ES(eta_h[i] * x_adim, 12, 5).c_str(),
+                       fortran_ES(phis_h[i] * x_adim * x_adim / t_adim, 12, 5).c_str());
+        } else {
+          double target = 0.0;
+          if (P.icase == 2 && (P.igeom == 1 || P.igeom == 2))
+            target = P.amp_mono * std::cos(P.w_mono * c.time_cur -
+                                           c.k_mono * (c.cx[i1] * std::cos(P.theta_mono) +
+                                                       c.cy[i2] * std::sin(P.theta_mono)) +
+                                           P.ph_mono);
+          std::fprintf(f3, "%s %s \n", fortran_ES(eta_h[i] * x_adim, 12, 5).c_str(),
+                       fortran_ES((eta_h[i] - target) * x_adim, 12, 5).c_str());
+        }
+      }
+  };
   std::vector<double> pv(std::max(c.nprobes, 1));
   double delt = P.delt;
   int rc = HOSNWT_OK;
   while (c.time_cur < P.T_stop + P.delt_out) {
+    if (f3) write_3d();
     if (fv) {
       // output_time_step (output.f90:232-282)
       double dg[5];
@@ -1216,6 +1279,7 @@ extern "C" int hosnwt_run(hosnwt_ctx* h, const char* results_dir) {
   }
   if (fp) std::fclose(fp);
   if (fv) std::fclose(fv);
+  if (f3) std::fclose(f3);
   return rc;
 }
 

@@ -110,6 +110,7 @@ struct Ctx {
   std::vector<double> probes;  // nondimensional (x, y)
   int nprobes = 0;
   int nf = 0;
+  double k_mono = 0.0;  // wave number of the first wave component (initial_condition.f90:175, 209-210)
   StateLayout L{};
   Dev d{};
   Tables tb{};

@@ -115,10 +115,11 @@ int hosnwt_accept(hosnwt_ctx* ctx, double h_loc);
  * with step control on the host; h_rk is the in/out step size. */
 int hosnwt_advance(hosnwt_ctx* ctx, double time_next, double* h_rk, int* n_acc, int* n_rej);
 
-/* Whole time loop (HOS-NWT.f90:446-581) writing Results/probes.dat and
- * Results/vol_energy.dat into results_dir (NULL: no files), in the formats of
- * output.f90 (input echo, 61d13.5 probe records, 5(ES12.5,X) energies),
- * with check_slope after each output interval. */
+/* Whole time loop (HOS-NWT.f90:446-581) writing Results/probes.dat,
+ * Results/vol_energy.dat and, when i3d = 1, Results/3d.dat into results_dir
+ * (NULL: no files), in the formats of output.f90 (input echo, 61d13.5 probe
+ * records, 5(ES12.5,X) energies, free-surface zones with tecplot = 11), with
+ * check_slope after each output interval. */
 int hosnwt_run(hosnwt_ctx* ctx, const char* results_dir);
 
 /* Diagnostics of the current state (vol_energy.f90:36-119 and
