@@ -259,6 +259,57 @@ struct Wave {
   double clock = 0.0, depth = 0.0;
 };
 
+// phase (wave_def.f90:491-523) as the reference writes it: its first test
+// returns 0 for every |z| > tiny, so only |z| <= tiny reaches the angle
+// formula.  Results match the reference's Benchmark/Regular_3D output only
+// with this behaviour.
+static double fortran_phase(std::complex<double> z) {
+  if (std::abs(z) > TINY) return 0.0;
+  const std::complex<double> zt = z / std::abs(z);
+  const double pt = std::asin(zt.imag());
+  if (zt.real() >= 0.0) return zt.imag() >= 0.0 ? pt : TWOPI + pt;
+  return PI - pt;
+}
+
+// dalrymple (wave_def.f90:111-177): an oblique wave of one frequency as
+// 2 (N+1) components over the tank's y-modes, focused at x = X_d;
+// appended to w (add_wave, wave_def.f90:333-384).
+static void dalrymple_append(Wave& w, double Ly, double X_d, int harmo, double ampli, double angle,
+                             double phas) {
+  using cd = std::complex<double>;
+  const cd I(0.0, 1.0);
+  const double freq = harmo * w.clock / std::pow(2.0, w.rnum);
+  const double k = wave_number_adim(freq, 1.0e-12);
+  const int N = (int)std::floor(k * Ly / PI);
+  const double beta = k * std::sin(angle);
+  std::vector<cd> a_on(N + 1);
+  std::vector<double> theta(N + 1);
+  cd tmp = -std::exp(-I * beta * Ly);
+  for (int n = 0; n <= N; ++n) {
+    const double mu = n * PI / Ly;
+    theta[n] = std::asin(mu / k);
+    const double delta = n == 0 ? 1.0 : 0.0;
+    cd In;
+    if (std::fabs(angle) < TINY) {
+      In = delta;
+    } else {
+      tmp = -tmp;
+      if (std::fabs(mu - std::fabs(beta)) < TINY) In = 1.0;
+      else In = 2.0 * I * beta * (tmp - 1.0) / (beta * beta - mu * mu) / ((1.0 + delta) * Ly);
+    }
+    const cd kn = I * std::sqrt(k * k - mu * mu);
+    a_on[n] = ampli * std::exp(I * phas) * In * std::exp((kn - I * k * std::cos(angle)) * X_d);
+  }
+  for (int half = 0; half < 2; ++half)
+    for (int n = 0; n <= N; ++n) {
+      w.harmo.push_back(harmo);
+      w.freq.push_back(freq);
+      w.ampli.push_back(std::abs(a_on[n] / 2.0));
+      w.angle.push_back(half == 0 ? theta[n] : -theta[n]);
+      w.phase.push_back(fortran_phase(a_on[n]));
+    }
+}
+
 static void wave_init(Wave& w, const std::string& typ, double hinge) {
   // wave_init (wave_def.f90:282-329)
   const size_t n = w.freq.size();
@@ -285,15 +336,20 @@ static int wave_cfg(Ctx& c, const char* wave_dir) {
   if (P.icase == 1) {
     c.nf = 0;
   } else if (P.icase == 2) {
-    if (in.ibat != 2) return fail(c, HOSNWT_ERR_UNSUPPORTED, "only snake wavemaking (ibat=2) is supported");
+    if (in.ibat != 2 && in.ibat != 3)
+      return fail(c, HOSNWT_ERR_UNSUPPORTED, "only snake (ibat=2) and Dalrymple (ibat=3) wavemaking");
     w.rnum = 1;
     w.clock = 2.0 * P.nu_mono;
     w.depth = P.h;
-    w.harmo = {1};
-    w.freq = {1 * w.clock / (double)(1 << w.rnum)};
-    w.ampli = {P.amp_mono};
-    w.angle = {P.theta_mono};
-    w.phase = {P.ph_mono};
+    if (in.ibat == 3) {
+      dalrymple_append(w, P.ylen, in.xd_mono / P.h, 1, P.amp_mono, P.theta_mono, P.ph_mono);
+    } else {
+      w.harmo = {1};
+      w.freq = {1 * w.clock / (double)(1 << w.rnum)};
+      w.ampli = {P.amp_mono};
+      w.angle = {P.theta_mono};
+      w.phase = {P.ph_mono};
+    }
   } else if (P.icase == 3) {
     std::string base = std::string(wave_dir ? wave_dir : ".") + "/" + trim(in.file_name);
     std::ifstream cf(base + ".cfg");
@@ -343,8 +399,13 @@ static int wave_cfg(Ctx& c, const char* wave_dir) {
       w.angle.push_back(ga[i] * PI / 180.0);
       w.phase.push_back(pa[i]);
     }
-    if (in.ibat == 3 && P.n2 != 1)
-      return fail(c, HOSNWT_ERR_UNSUPPORTED, "Dalrymple wavemaking (ibat=3) is not supported");
+    if (in.ibat == 3 && P.n2 != 1) {
+      // initial_condition.f90:192-199: the Dalrymple waves of every component
+      Wave src = w;
+      w.harmo.clear(); w.freq.clear(); w.ampli.clear(); w.angle.clear(); w.phase.clear();
+      for (size_t i = 0; i < src.harmo.size(); ++i)
+        dalrymple_append(w, P.ylen, in.xd_mono / P.h, src.harmo[i], src.ampli[i], src.angle[i], src.phase[i]);
+    }
   } else if (P.icase == 4) {
     const double Tp = in.Tp, Hs = in.Hs, gam = in.gamma;
     const double clock = 32.0;

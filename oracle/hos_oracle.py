@@ -379,6 +379,7 @@ class Tank:
         self.xlen = p["xlen"] / h
         self.ylen = p["ylen"] / h
         self.amp_mono = p["amp_mono"] / h
+        self.xd_mono = p["xd_mono"] / self.h
         self.xlen_add = 2.0 * float(self.l_add)
         self.d_hinge = p["d_hinge"] / h
         self.aslosh = p["aslosh"] / h
@@ -470,12 +471,16 @@ class Tank:
         if self.icase == 2:
             rnum, clock = 1, 2.0 * self.nu_mono
             harmo = np.array([1])
-            if p["ibat"] != 2:
-                raise NotImplementedError("only snake (ibat=2) wavemaking")
-            freq = np.array([1 * clock / 2 ** rnum])
-            ampli = np.array([self.amp_mono])
-            angle = np.array([self.theta_mono])
-            phase = np.array([self.ph_mono])
+            if p["ibat"] not in (2, 3):
+                raise NotImplementedError("snake (ibat=2) or Dalrymple (ibat=3) wavemaking only")
+            if p["ibat"] == 3:
+                harmo, freq, ampli, angle, phase = self._dalrymple(
+                    clock, rnum, 1, self.amp_mono, self.theta_mono, self.ph_mono)
+            else:
+                freq = np.array([1 * clock / 2 ** rnum])
+                ampli = np.array([self.amp_mono])
+                angle = np.array([self.theta_mono])
+                phase = np.array([self.ph_mono])
             depth, hinge = h, self.d_hinge
         elif self.icase == 3:
             base = os.path.join(self.wave_files_dir, p["file_name"].strip())
@@ -517,7 +522,15 @@ class Tank:
             angle = ang_a[sl] * PI / 180.0
             phase = ph_a[sl]
             if p["ibat"] == 3 and self.n2 != 1:
-                raise NotImplementedError("Dalrymple wavemaking (ibat=3)")
+                # initial_condition.f90:192-199: the Dalrymple waves of every
+                # component, concatenated (add_wave, wave_def.f90:333-384)
+                parts = [self._dalrymple(clock, rnum, int(hh), a, an, ph)
+                         for hh, a, an, ph in zip(harmo, ampli, angle, phase)]
+                harmo = np.concatenate([q[0] for q in parts])
+                freq = np.concatenate([q[1] for q in parts])
+                ampli = np.concatenate([q[2] for q in parts])
+                angle = np.concatenate([q[3] for q in parts])
+                phase = np.concatenate([q[4] for q in parts])
         elif self.icase == 4:
             Tp, Hs, gam = p["Tp"], p["Hs"], p["gamma"]
             clock = 32.0
@@ -553,6 +566,51 @@ class Tank:
         self.wave = dict(harmo=harmo, freq=freq, ampli=ampli, angle=angle, phase=phase,
                          k=k, TF=TF, rnum=rnum, clock=clock, depth=depth)
         self._wmk_ini()
+
+    @staticmethod
+    def _phase(z):
+        """phase (wave_def.f90:491-523) as written: its first test returns 0
+        for every |z| > tiny, so only |z| <= tiny reaches the angle formula."""
+        if abs(z) > TINY:
+            return 0.0
+        with np.errstate(invalid="ignore", divide="ignore"):
+            zt = z / abs(z)
+            pt = math.asin(zt.imag) if abs(zt.imag) <= 1.0 else float("nan")
+        if zt.real >= 0.0:
+            return pt if zt.imag >= 0.0 else TWOPI + pt
+        return PI - pt
+
+    def _dalrymple(self, clock, rnum, harmo, ampli, angle, phas):
+        """dalrymple (wave_def.f90:111-177): the oblique wave of one
+        frequency as 2 (N+1) components over the tank's y-modes, focused at
+        x = xd_mono."""
+        Ly, X_d = self.ylen, self.xd_mono
+        freq = harmo * clock / 2 ** rnum
+        k = wave_number_adim_r(freq, 1.0e-12)
+        N = int(math.floor(k * Ly / PI))
+        mu = np.arange(N + 1) * PI / Ly
+        theta = np.arcsin(mu / k)
+        beta = k * math.sin(angle)
+        delta = np.zeros(N + 1)
+        delta[0] = 1.0
+        if abs(angle) < TINY:
+            I_n = delta.astype(np.complex128)
+        else:
+            I_n = np.zeros(N + 1, dtype=np.complex128)
+            tmp = -np.exp(-1j * beta * Ly)
+            for n in range(N + 1):
+                tmp = -tmp
+                if abs(mu[n] - abs(beta)) < TINY:
+                    I_n[n] = 1.0
+                else:
+                    I_n[n] = 2 * 1j * beta * (tmp - 1) / (beta ** 2 - mu[n] ** 2) / ((1 + delta[n]) * Ly)
+        k_n = 1j * np.sqrt(k ** 2 - mu ** 2 + 0j)
+        a_on = ampli * np.exp(1j * phas) * I_n * np.exp((k_n - 1j * k * math.cos(angle)) * X_d)
+        ph = np.array([self._phase(z) for z in a_on])
+        amp = np.abs(a_on / 2.0)
+        n_f = 2 * (N + 1)
+        return (np.full(n_f, harmo), np.full(n_f, freq), np.concatenate([amp, amp]),
+                np.concatenate([theta, -theta]), np.concatenate([ph, ph]))
 
     def _gzed(self, z):
         """gzed (wavemaking.f90:184-213)."""

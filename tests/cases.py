@@ -26,5 +26,16 @@ WIDE_3D = dict(inp=default_input(T_stop=20.0, amp_mono=0.02, nu_mono=0.7, theta_
                                  f_out=4.0, ylen=20.0),
                n1=17, n2=129, n3=9, mHOS=3, p1=3, p2=3)
 
+# The reference's own Benchmark runs (configuration from their Ref_data input
+# echo; fixtures tests/golden/ref_*.npz hold the reference's probe records)
+REF_SLOSHING = dict(inp=default_input(xlen=50.0, ylen=29.74, h=5.0, icase=1, islosh=3, aslosh=0.2, iabsnb=0,
+                                      T_stop=20.0, toler=1e-6, f_out=20.0, idim=1),
+                    n1=129, n2=1, n3=33, mHOS=1, p1=1, p2=1)
+REF_REGULAR_3D = dict(inp=default_input(xlen=46.4, ylen=29.74, h=5.0, icase=2, amp_mono=0.1, nu_mono=0.5588,
+                                        theta_mono=30.0, ph_mono=0.0, ibat=3, xd_mono=25.0, i_wmk=1, igeom=2,
+                                        d_hinge=2.147, iramp=1, Tramp=3.0, T_stop=40.0, iabsnb=1, xabsf=0.8,
+                                        coeffabsf=1.0, toler=1e-4, f_out=10.0, idim=1),
+                      n1=256, n2=32, n3=16, mHOS=3, p1=3, p2=3)
+
 ALL = {"reg1d": REG_1D, "reg1d_m5": REG_1D_M5, "reg3d": REG_3D, "slosh": SLOSH, "jonswap1d": JONSWAP_1D,
        "wide3d": WIDE_3D}

@@ -1,0 +1,56 @@
+"""The CUDA path against the reference's own result files.
+
+Benchmark/Sloshing and Benchmark/Regular_3D ship probe records written by
+the reference HOS-NWT (tests/golden/ref_*.npz, made by
+tests/golden/make_ref_benchmarks.py).  The whole runs (20 s and 40 s) go
+through the C ABI; every probe value must agree with the reference's record
+within about half a unit of its last printed digit (5 significant digits).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _digit_unit(v):
+    a = np.abs(v)
+    return np.where(a > 0, 10.0 ** (np.floor(np.log10(np.where(a > 0, a, 1.0))) - 4), 1e-20)
+
+
+def _records(case, fx):
+    import hosnwt
+    probes = [tuple(p) for p in fx["probes"]]
+    g = hosnwt.Tank(case["inp"], case["n1"], case["n2"], case["n3"], case["mHOS"], case["p1"], case["p2"],
+                    probes=probes)
+    inf = g.info()
+    recs = g.simulate()
+    return np.array([[t * inf["Tscale"]] + list(np.asarray(p) * case["inp"]["h"]) for t, p in recs])
+
+
+def _fixture(name):
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", name))
+
+
+def test_sloshing_matches_reference_record(lib):
+    fx = _fixture("ref_sloshing.npz")
+    got = _records(cases.REF_SLOSHING, fx)
+    ref = fx["records"]
+    assert got.shape == ref.shape
+    assert np.max(np.abs(got[:, 0] - ref[:, 0])) < 1e-9
+    err = np.abs(got[:, 1:] - ref[:, 1:]) / (_digit_unit(ref[:, 1:]) + 1e-12)
+    assert np.max(err[:, [0, 2]]) <= 0.6, np.max(err)
+
+
+def test_regular3d_matches_reference_record(lib):
+    """Nonlinear (M = 3) 3-D tank with Dalrymple wavemaking over 40 s."""
+    fx = _fixture("ref_regular3d.npz")
+    got = _records(cases.REF_REGULAR_3D, fx)
+    ref = fx["records"]
+    assert got.shape == ref.shape
+    assert np.max(np.abs(got[:, 0] - ref[:, 0])) < 1e-9
+    err = np.abs(got[:, 1:] - ref[:, 1:]) / (_digit_unit(ref[:, 1:]) + 1e-14)
+    assert np.max(err) <= 0.6, (np.max(err), np.unravel_index(np.argmax(err), err.shape))

@@ -7,6 +7,8 @@ import pytest
 
 from oracle import hos_oracle as H
 
+import cases
+
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
@@ -126,3 +128,53 @@ def test_golden_fixtures(name):
     got = run_fixture_case(cases.ALL[name])
     for key, ref in fx.items():
         assert np.allclose(got[key], ref, rtol=0, atol=1e-12 * max(np.max(np.abs(ref)), 1e-300)), key
+
+
+# --------------------------------------------------------------------------
+# The oracle against the reference's own result files (Benchmark/*/Ref_data,
+# stored by tests/golden/make_ref_benchmarks.py): the probe records are
+# printed with 5 significant digits, so each value must agree within about
+# half a unit of its last printed digit.
+
+def _digit_unit(v):
+    a = np.abs(v)
+    return np.where(a > 0, 10.0 ** (np.floor(np.log10(np.where(a > 0, a, 1.0))) - 4), 1e-20)
+
+
+def _ref_fixture(name):
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", name))
+
+
+def _run_records(case, fx, T_end=None):
+    from oracle.hos_oracle import Tank
+    probes = [tuple(p) for p in fx["probes"]]
+    o = Tank(case["inp"], case["n1"], case["n2"], case["n3"], case["mHOS"], case["p1"], case["p2"], probes=probes)
+    recs = o.run(T_end=T_end)
+    return np.array([[r[0] * o.Tscale] + list(np.asarray(r[1]) * o.h) for r in recs])
+
+
+def test_oracle_matches_reference_sloshing_record():
+    """Benchmark/Sloshing: the 4th natural mode (0.2 m) over 20 s, 401 records."""
+    fx = _ref_fixture("ref_sloshing.npz")
+    assert [int(v) for v in fx["numerics"]] == [129, 1, 33, 1, 1, 1]
+    got = _run_records(cases.REF_SLOSHING, fx)
+    ref = fx["records"]
+    assert got.shape == ref.shape
+    assert np.max(np.abs(got[:, 0] - ref[:, 0])) < 1e-9
+    err = np.abs(got[:, 1:] - ref[:, 1:]) / (_digit_unit(ref[:, 1:]) + 1e-12)
+    assert np.max(err[:, [0, 2]]) <= 0.6, np.max(err)
+    assert np.max(np.abs(got[:, 2])) < 1e-12  # the node of the mode
+
+
+def test_oracle_matches_reference_regular3d_record():
+    """Benchmark/Regular_3D: a 30 deg Dalrymple wave, M = 3 on 256 x 32 modes;
+    the first second (11 records of the 401) on the CPU."""
+    fx = _ref_fixture("ref_regular3d.npz")
+    assert [int(v) for v in fx["numerics"]] == [256, 32, 16, 3, 3, 3]
+    case = cases.REF_REGULAR_3D
+    got = _run_records(case, fx, T_end=1.0)
+    ref = fx["records"][:len(got)]
+    assert len(got) == 11
+    assert np.max(np.abs(got[:, 0] - ref[:, 0])) < 1e-9
+    err = np.abs(got[:, 1:] - ref[:, 1:]) / (_digit_unit(ref[:, 1:]) + 1e-14)
+    assert np.max(err) <= 0.6, np.max(err)
