@@ -251,6 +251,17 @@ static double gzed_fn(const Params& P, double z) {
          (5.0 / 16.0 + u + 15.0 / 16.0 * (u * u - 1.0 / 3.0 * u * u * u * u + 1.0 / 15.0 * u * u * u * u * u * u));
 }
 
+static double dgzeddz_fn(const Params& P, double z) {
+  // dgzeddz (wavemaking.f90:222-250)
+  const double dh = P.d_hinge;
+  const double delta = std::min(dh, (1.0 - dh) / 10.0);
+  if (P.igeom == 1) return 0.0;
+  if (z >= (dh - 1.0 + delta)) return 1.0 / (1.0 - dh);
+  if (z <= (dh - 1.0 - delta)) return 0.0;
+  const double u = (z - (dh - 1.0)) / delta;
+  return 1.0 / (1.0 - dh) * (1.0 / 2.0 + 15.0 / 16.0 * (u - 2.0 / 3.0 * u * u * u + 1.0 / 5.0 * u * u * u * u * u));
+}
+
 struct Wave {
   std::vector<int> harmo;
   std::vector<double> freq, ampli, angle, phase, k;
@@ -459,18 +470,22 @@ static int wave_cfg(Ctx& c, const char* wave_dir) {
   c.nf = (int)groups.size();
   c.freq_w.resize(c.nf);
   c.pos_ini.assign((size_t)P.n2 * c.nf, std::complex<double>(0.0, 0.0));
+  c.dposdy_ini.assign((size_t)P.n2 * c.nf, std::complex<double>(0.0, 0.0));
   const std::complex<double> I(0.0, 1.0);
   for (int g = 0; g < c.nf; ++g) {
     c.freq_w[g] = w.freq[groups[g][0]];
     for (int j1 = 0; j1 < P.n2; ++j1) {
-      std::complex<double> acc(0.0, 0.0);
+      std::complex<double> acc(0.0, 0.0), dacc(0.0, 0.0);
       for (int i : groups[g]) {
         const double ang = w.angle[i];
         const std::complex<double> tmp = w.TF[i] * std::cos(ang) * w.ampli[i] *
                                          std::exp(I * (-w.k[i] * std::sin(ang) * c.cy[j1] + w.phase[i]));
         acc += 1.0 * tmp;
+        // dposdy_ini with rampy = 1, drampy = 0 (full-width wavemaker)
+        dacc += (0.0 - I * w.k[i] * std::sin(ang) * 1.0) * tmp;
       }
       c.pos_ini[j1 + (size_t)P.n2 * g] = acc;
+      c.dposdy_ini[j1 + (size_t)P.n2 * g] = dacc;
     }
   }
   return HOSNWT_OK;
@@ -518,8 +533,8 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
   if (P.n2 == 1) P.nd2 = 1;
   P.icase = in.icase; P.igeom = in.igeom; P.iramp = in.iramp; P.iabsnb = in.iabsnb;
   P.i_wmk = in.i_wmk; P.ibat = in.ibat;
-  if (P.icase != 1 && P.i_wmk != 1)
-    return fail(c, HOSNWT_ERR_UNSUPPORTED, "only the first-order wavemaker (i_wmk=1) is supported");
+  if (P.icase != 1 && P.i_wmk != 1 && P.i_wmk != 2)
+    return fail(c, HOSNWT_ERR_UNSUPPORTED, "only first- and second-order wavemakers (i_wmk = 1, 2) are supported");
   if (P.icase != 1 && P.igeom != 1 && P.igeom != 2)
     return fail(c, HOSNWT_ERR_UNSUPPORTED, "only flap/piston wavemakers (igeom 1, 2) are supported");
   // nondimensionalisation (HOS-NWT.f90:99-119)
@@ -678,6 +693,47 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
   d.kycsh = upload(c, kycsh);
   d.kxcsh = upload(c, kxcsh);
   d.ext = upload(c, extension_matrix(P.n3, n3a, P.l_add, P.delz));
+  if (P.i_wmk == 2) {
+    // second-order wavemaker (d1st_for_2nd, solveHOS_SWEET_2): free-surface
+    // modes on the wavemaker (HOS-NWT.f90:343-355), [i1 + n1 (i2 + n2 i3)]
+    const int n3 = P.n3;
+    std::vector<double> kx2c((size_t)n1 * n2 * n3), kyc(kx2c.size()), ks(kx2c.size());
+    for (int i3 = 0; i3 < n3; ++i3)
+      for (int i2 = 0; i2 < n2; ++i2)
+        for (int i1 = 0; i1 < n1; ++i1) {
+          const double kk = std::sqrt(c.kx[i1] * c.kx[i1] + c.ky[i2] * c.ky[i2]);
+          const double cxk = kk * (P.delz * i3), ch = std::cosh(kk);
+          const double cshx = std::cosh(cxk) / ch;
+          const size_t o = i1 + (size_t)n1 * (i2 + (size_t)n2 * i3);
+          kx2c[o] = cshx * c.kx[i1] * c.kx[i1];
+          kyc[o] = cshx * c.ky[i2];
+          ks[o] = kk * std::sinh(cxk) / ch;
+        }
+    d.kx2cshx = upload(c, kx2c);
+    d.kycshx = upload(c, kyc);
+    d.kshx = upload(c, ks);
+    d.k_add = upload(c, k_add);
+    // dnux as absorb writes it: coeffabsf * 2 * x3 (initial_condition.f90:764-768)
+    std::vector<double> dnux((size_t)n1 * n2, 0.0);
+    if (P.iabsnb != 0 && std::fabs(in.xabsf - 1.0) > TINY) {
+      const double x0 = P.xlen * in.xabsf, x2 = P.xlen - x0;
+      for (int i1 = 0; i1 < n1; ++i1)
+        if (c.cx[i1] >= x0)
+          for (int i2 = 0; i2 < n2; ++i2) dnux[i1 + (size_t)n1 * i2] = in.coeffabsf * 2 * ((c.cx[i1] - x0) / x2);
+    }
+    d.dnux = upload(c, dnux);
+    std::vector<double> dgz(n3), dre(std::max<size_t>(c.dposdy_ini.size(), 1)), dim(dre.size());
+    for (int i3 = 0; i3 < n3; ++i3) dgz[i3] = dgzeddz_fn(P, c.cz[i3]);
+    for (size_t i = 0; i < c.dposdy_ini.size(); ++i) {
+      dre[i] = c.dposdy_ini[i].real();
+      dim[i] = c.dposdy_ini[i].imag();
+    }
+    d.dgzed = upload(c, dgz);
+    d.dposdy_re = upload(c, dre);
+    d.dposdy_im = upload(c, dim);
+    const size_t nw = std::max((size_t)n1 * n2, (size_t)n3a * n2);
+    for (int i = 0; i < Dev::kW2; ++i) d.w2[i] = dalloc<double>(c, nw);
+  }
   std::vector<double> pre(std::max<size_t>(c.pos_ini.size(), 1)), pim(pre.size());
   for (size_t i = 0; i < c.pos_ini.size(); ++i) { pre[i] = c.pos_ini[i].real(); pim[i] = c.pos_ini[i].imag(); }
   d.pos_re = upload(c, pre);
@@ -885,6 +941,15 @@ extern "C" int hosnwt_create(const hosnwt_input* in, const hosnwt_numerics* num,
     enqueue_initialize(c, c.st);
     cudaMemcpyAsync(c.d.eta, eta.data(), nN * sizeof(double), cudaMemcpyHostToDevice, c.st);
     cudaMemsetAsync(c.d.phis, 0, nN * sizeof(double), c.st);
+    if (c.P.icase != 1) {
+      // phi_add at t = 0 (initial_condition.f90:458-466: SWEET_1/2 and
+      // phiadd_SL on the initial state): one right-hand side with dt = 0
+      // into scratch slopes; the state is zero apart from the wavemaker
+      // amplitudes, and the ramp and paddle position stay those of t = 0
+      enqueue_set_scalar(c, SC_DT, 0.0, c.st);
+      enqueue_rhs(c, c.d.y0, c.d.k[0], true, c.st);
+      c.n_rhs = 0;
+    }
     cudaStreamSynchronize(c.st);
     rc = cuda_check(c, "initialize");
     if (rc == HOSNWT_OK) rc = build_step_graph(c);

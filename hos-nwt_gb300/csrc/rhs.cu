@@ -568,14 +568,276 @@ __global__ void k_sum3(const double* a, const double* b, const double* c, double
   if (i < n) out[i] = a[i] + b[i] + c[i];
 }
 
+// ---------------------------------------------------------------------------
+// second-order wavemaker (i_wmk = 2)
+// ---------------------------------------------------------------------------
+// phiadd_1st_SWEET's free-surface set (resol_wmkr.f90:446-574) at z = 0,
+// y-modal in j2 (the y sums follow as FOURIER_2_SPACE_y in 3-D tanks):
+//   out_f(i1, j2) = s_f sum_i3 c_f(i3, j2) T_f(i1, j2, i3)
+// with c_f one of a cos, da cos, a sin, da sin, a cos kx_add, a cos k_add^2,
+// a sin kx_add, a sin ky (cos, sin of kx_add(i3)) and T_f one of csh,
+// k_add sh, ky csh, kx_add csh.
+enum { W_T = 0, W_Z, W_X, W_Y, W_ZZ, W_XT, W_YT, W_ZT, W_XX, W_XZ, W_YZ, W_NF };
+struct Contract1Out {
+  double* f[W_NF];
+};
+__global__ void __launch_bounds__(kCx * kCy) k_fs_contract1(
+    const double* __restrict__ a, const double* __restrict__ da, const double* __restrict__ cosk,
+    const double* __restrict__ sink, const double* __restrict__ kx_add, const double* __restrict__ k_add,
+    const double* __restrict__ ky, const double* __restrict__ csh, const double* __restrict__ ksh,
+    const double* __restrict__ kycsh, const double* __restrict__ kxcsh, int n1, int n2, int n3a,
+    Contract1Out o) {
+  pdl_wait();
+  __shared__ double cf[8][512];
+  __shared__ double red[W_NF][kCy][kCx];
+  const int j2 = blockIdx.y;
+  const int tx = threadIdx.x % kCx, ty = threadIdx.x / kCx;
+  const int i1 = blockIdx.x * kCx + tx;
+  for (int t = threadIdx.x; t < n3a; t += blockDim.x) {
+    const double aa = a[t + (long long)n3a * j2], dd = da[t + (long long)n3a * j2];
+    const double c = cosk[t], sn = sink[t], ka = k_add[t + (long long)n3a * j2];
+    cf[0][t] = aa * c;
+    cf[1][t] = dd * c;
+    cf[2][t] = aa * sn;
+    cf[3][t] = dd * sn;
+    cf[4][t] = aa * c * kx_add[t];
+    cf[5][t] = aa * c * (ka * ka);
+    cf[6][t] = aa * sn * kx_add[t];
+    cf[7][t] = aa * sn * ky[j2];
+  }
+  __syncthreads();
+  const int ch = (n3a + kCy - 1) / kCy;
+  double sm[W_NF];
+#pragma unroll
+  for (int f = 0; f < W_NF; ++f) sm[f] = 0.0;
+  if (i1 < n1) {
+    for (int i3 = ty * ch; i3 < min(n3a, (ty + 1) * ch); ++i3) {
+      const long long q = i1 + (long long)n1 * i3 + (long long)n1 * n3a * j2;
+      const double tc = csh[q], tk = ksh[q], ty_ = kycsh[q], tx_ = kxcsh[q];
+      sm[W_T] = fma(cf[1][i3], tc, sm[W_T]);
+      sm[W_Z] = fma(cf[2][i3], tx_, sm[W_Z]);
+      sm[W_X] = fma(cf[0][i3], tk, sm[W_X]);
+      sm[W_Y] = fma(cf[0][i3], ty_, sm[W_Y]);
+      sm[W_ZZ] = fma(cf[4][i3], tx_, sm[W_ZZ]);
+      sm[W_XT] = fma(cf[1][i3], tk, sm[W_XT]);
+      sm[W_YT] = fma(cf[1][i3], ty_, sm[W_YT]);
+      sm[W_ZT] = fma(cf[3][i3], tx_, sm[W_ZT]);
+      sm[W_XX] = fma(cf[5][i3], tc, sm[W_XX]);
+      sm[W_XZ] = fma(cf[6][i3], tk, sm[W_XZ]);
+      sm[W_YZ] = fma(cf[7][i3], tc, sm[W_YZ]);
+    }
+  }
+#pragma unroll
+  for (int f = 0; f < W_NF; ++f) red[f][ty][tx] = sm[f];
+  __syncthreads();
+  if (ty == 0 && i1 < n1) {
+    // signs of resol_wmkr.f90:500-532
+    const double sg[W_NF] = {1.0, -1.0, -1.0, -1.0, -1.0, -1.0, -1.0, -1.0, 1.0, 1.0, 1.0};
+#pragma unroll
+    for (int f = 0; f < W_NF; ++f) {
+      double v = 0.0;
+      for (int c = 0; c < kCy; ++c) v += red[f][c][tx];
+      o.f[f][i1 + (long long)n1 * j2] = sg[f] * v;
+    }
+  }
+}
+
+// the wavemaker-grid terms of phiadd_1st_SWEET before their F2S_add
+// (resol_wmkr.f90:536-543): a k_add^2, da k_add^2, -a ky, -da ky,
+// -a kx_add, -da kx_add on the n3_add x n2 modes
+struct AddProdOut {
+  double* p[6];
+};
+__global__ void k_add_prod(const double* __restrict__ a, const double* __restrict__ da,
+                           const double* __restrict__ k_add, const double* __restrict__ kx_add,
+                           const double* __restrict__ ky, int n3a, long long n, AddProdOut o) {
+  pdl_wait();
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int i3 = (int)(i % n3a), i2 = (int)(i / n3a);
+  const double aa = a[i], dd = da[i], ka = k_add[i];
+  o.p[0][i] = aa * ka * ka;
+  o.p[1][i] = dd * ka * ka;
+  o.p[2][i] = -aa * ky[i2];
+  o.p[3][i] = -dd * ky[i2];
+  o.p[4][i] = -aa * kx_add[i3];
+  o.p[5][i] = -dd * kx_add[i3];
+}
+
+// the free-surface mode products of d1st_for_2nd (resol_wmkr.f90:737-747)
+// before their F2S: -a kx, -a ky, da kx, da ky, da kth1, -a kx^2, a k^2,
+// -a kx kth1, (-a ky) kth1
+struct FsProdOut {
+  double* p[9];
+};
+__global__ void k_fs_prod1(const double* __restrict__ a, const double* __restrict__ da,
+                           const double* __restrict__ kx, const double* __restrict__ ky,
+                           const double* __restrict__ kth1, int n1, long long n, FsProdOut o) {
+  pdl_wait();
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int i1 = (int)(i % n1), i2 = (int)(i / n1);
+  const double aa = a[i], dd = da[i], x = kx[i1], y = ky[i2], t = kth1[i];
+  const double k = sqrt(x * x + y * y);
+  o.p[0][i] = -aa * x;
+  o.p[1][i] = -aa * y;
+  o.p[2][i] = dd * x;
+  o.p[3][i] = dd * y;
+  o.p[4][i] = dd * t;
+  o.p[5][i] = -aa * (x * x);
+  o.p[6][i] = aa * k * k;
+  o.p[7][i] = -aa * x * t;
+  o.p[8][i] = (-aa * y) * t;
+}
+
+// d1st_for_2nd on the wavemaker (resol_wmkr.f90:703-717): the free-surface
+// modes at the n3 wavemaker nodes, y-modal; one block per (i3, i2).
+// out: -sum a T_xx, -sum da T_xx, -sum a T_y, -sum da T_y, sum a T_z, sum da T_z
+struct WmkFsOut {
+  double* w[6];
+};
+__global__ void k_wmk_from_fs(const double* __restrict__ a, const double* __restrict__ da,
+                              const double* __restrict__ txx, const double* __restrict__ tyy,
+                              const double* __restrict__ tz, int n1, int n2, int n3, WmkFsOut o) {
+  pdl_wait();
+  const int i3 = blockIdx.x, i2 = blockIdx.y;
+  double s[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int i1 = threadIdx.x; i1 < n1; i1 += blockDim.x) {
+    const long long fi = i1 + (long long)n1 * i2;
+    const long long q = fi + (long long)n1 * n2 * i3;
+    const double aa = a[fi], dd = da[fi];
+    s[0] = fma(aa, txx[q], s[0]);
+    s[1] = fma(dd, txx[q], s[1]);
+    s[2] = fma(aa, tyy[q], s[2]);
+    s[3] = fma(dd, tyy[q], s[3]);
+    s[4] = fma(aa, tz[q], s[4]);
+    s[5] = fma(dd, tz[q], s[5]);
+  }
+  const double sg[6] = {-1.0, -1.0, -1.0, -1.0, 1.0, 1.0};
+  for (int q = 0; q < 6; ++q) {
+    const double v = block_reduce<0>(s[q]);
+    if (threadIdx.x == 0) o.w[q][i3 + (long long)n3 * i2] = sg[q] * v;
+    __syncthreads();
+  }
+}
+
+// d1st_for_2nd on the free surface (resol_wmkr.f90:749-775): transformed
+// products T (k_fs_prod1 order) plus the phiadd_1st_SWEET fields F
+struct D1stArgs {
+  const double* T[9];
+  const double* F[W_NF];
+  const double* phiz1st;  // F2S(a1st kth1)
+  double* phix1st;
+  double* phiy1st;
+  double* etax1st;
+  double* etay1st;
+  double* phizt1st;
+  double* phixx1st;
+  double* phizz1st;
+  double* phiz1st_tot;
+};
+__global__ void k_d1st_combine(D1stArgs g, const double* __restrict__ nu, const double* __restrict__ dnux,
+                               double iabsnb, long long n) {
+  pdl_wait();
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double pz = g.phiz1st[i] + g.F[W_Z][i];
+  const double phixz = g.T[7][i] + g.F[W_XZ][i];
+  const double phiyz = g.T[8][i] + g.F[W_YZ][i];
+  g.phix1st[i] = g.T[0][i] + g.F[W_X][i];
+  g.phiy1st[i] = g.T[1][i] + g.F[W_Y][i];
+  g.etax1st[i] = g.T[2][i] - g.F[W_XT][i] - iabsnb * (dnux[i] * pz + nu[i] * phixz);
+  g.etay1st[i] = g.T[3][i] - g.F[W_YT][i] - iabsnb * (0.0 * pz + nu[i] * phiyz);
+  g.phizt1st[i] = g.T[4][i] + g.F[W_ZT][i];
+  g.phixx1st[i] = g.T[5][i] + g.F[W_XX][i];
+  g.phizz1st[i] = g.T[6][i] + g.F[W_ZZ][i];
+  g.phiz1st_tot[i] = pz;
+}
+
+// solveHOS_SWEET_2's wavemaker condition (resol_wmkr.f90:262-281) with
+// dposdy_1st / dposdz_1st (wavemaking.f90:313-406), no free-wave correction:
+// one block per i2 sums the frequencies, then rows i3 < n3 of bc2.
+// W: the six first-order wavemaker fields (wmk part n3 x n2, add part
+// n3_add x n2, summed here).
+struct Sweet2Wmk {
+  const double* wf[6];  // k_wmk_from_fs outputs in space, n3 x n2
+  const double* wa[6];  // F2S_add outputs, n3_add x n2
+};
+__global__ void k_sweet2_wmk(const double* __restrict__ pos_re, const double* __restrict__ pos_im,
+                             const double* __restrict__ dy_re, const double* __restrict__ dy_im,
+                             const double* __restrict__ freq, const double* __restrict__ eiwt,
+                             const double* __restrict__ gzed, const double* __restrict__ dgzed,
+                             const double* __restrict__ sc, int nf, int n2, int n3, int n3a, Sweet2Wmk W,
+                             double* bc2) {
+  pdl_wait();
+  const int i2 = blockIdx.x;
+  const double a = sc[SC_ALPHA], at = sc[SC_ALPHAT];
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int n = threadIdx.x; n < nf; n += blockDim.x) {
+    const double w = 6.283185307179586476925286766559005768394 * freq[n];
+    const double c = eiwt[2 * n], sn = eiwt[2 * n + 1];
+    const long long q = i2 + (long long)n2 * n;
+    const double pr = pos_re[q], pi = pos_im[q], yr = dy_re[q], yi = dy_im[q];
+    s[0] += pr * c - pi * sn;            // Re(pos e^{iwt})
+    s[1] += -(pr * sn + pi * c) * w;     // Re(pos e^{iwt} i w)
+    s[2] += yr * c - yi * sn;            // Re(dposdy e^{iwt})
+    s[3] += -(yr * sn + yi * c) * w;     // Re(dposdy e^{iwt} i w)
+  }
+  __shared__ double S[4];
+  for (int q = 0; q < 4; ++q) {
+    const double v = block_reduce<0>(s[q]);
+    if (threadIdx.x == 0) S[q] = v;
+    __syncthreads();
+  }
+  for (int i3 = threadIdx.x; i3 < n3; i3 += blockDim.x) {
+    const double g = gzed[i3], dg = dgzed[i3];
+    const double pos = g * S[0], dpos = g * S[1], dy = g * S[2], dyt = g * S[3], dz = dg * S[0], dzt = dg * S[1];
+    const long long wi = i3 + (long long)n3 * i2, ai = i3 + (long long)n3a * i2;
+    const double XX = W.wf[0][wi] + W.wa[0][ai], XXT = W.wf[1][wi] + W.wa[1][ai];
+    const double Y = W.wf[2][wi] + W.wa[2][ai], YT = W.wf[3][wi] + W.wa[3][ai];
+    const double Z = W.wf[4][wi] + W.wa[4][ai], ZT = W.wf[5][wi] + W.wa[5][ai];
+    const double noramp = -pos * XX + dy * Y + dz * Z;
+    bc2[ai] = -a * (-pos * XXT - dpos * XX + dy * YT + dyt * Y + dz * ZT + dzt * Z) - at * noramp;
+  }
+}
+
+// solveHOS_SWEET_2's free-surface conditions (resol_wmkr.f90:301-312)
+struct Sweet2Fs {
+  const double* phiz2nd_spec;  // F2S(a2nd kth1)
+  const double* p2z;
+  const double* p2t;
+  const double* eta2nd;
+  const double* eta1st;
+  const double* phix1st;
+  const double* etax1st;
+  const double* phiy1st;
+  const double* etay1st;
+  const double* phizz1st;
+  const double* phiz1st;
+  const double* phizt1st;
+};
+__global__ void k_sweet2_fs(Sweet2Fs g, const double* __restrict__ nu, double iabsnb, double* keta2,
+                            double* rhs2, long long n) {
+  pdl_wait();
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double pz2 = g.phiz2nd_spec[i] + g.p2z[i];
+  const double px = g.phix1st[i], py = g.phiy1st[i], pz = g.phiz1st[i];
+  const double deta = pz2 - px * g.etax1st[i] - py * g.etay1st[i] + g.eta1st[i] * g.phizz1st[i];
+  keta2[i] = deta;
+  rhs2[i] = -g.eta2nd[i] - g.p2t[i] - 5.0e-1 * (px * px + py * py + pz * pz) - g.eta1st[i] * g.phizt1st[i] -
+            iabsnb * nu[i] * deta;
+}
+
 // phiadd_SL on a 1-D tank (n2 = 1): the i3 contraction at z = eta.
 // kx_add(i3) = (2 i3 + 1) pi / 4, so cos/sin(kx_add(i3) (eta + 1)) follow
 // from one sincos per chunk start and rotations by 2 phi, phi = pi (eta+1)/4.
 __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
     const double* __restrict__ eta, const double* __restrict__ a1, const double* __restrict__ a2,
-    const double* __restrict__ a3, const double* __restrict__ da, const double* __restrict__ kx_add,
-    const double* __restrict__ csh, const double* __restrict__ ksh, const double* __restrict__ kxcsh,
-    int n1, int n3a, double* phix, double* phiy, double* phiz, double* phit, double* phi) {
+    const double* __restrict__ a3, const double* __restrict__ da, const double* __restrict__ da2,
+    const double* __restrict__ kx_add, const double* __restrict__ csh, const double* __restrict__ ksh,
+    const double* __restrict__ kxcsh, int n1, int n3a, double* phix, double* phiy, double* phiz, double* phit,
+    double* phi) {
   pdl_wait();
   __shared__ double sa[512], sd[512];
   __shared__ double r[4][kCy][kCx];
@@ -583,7 +845,7 @@ __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
   const int i1 = blockIdx.x * kCx + tx;
   for (int t = threadIdx.x; t < n3a; t += blockDim.x) {
     sa[t] = a1[t] + a2[t] + a3[t];
-    sd[t] = da[t];
+    sd[t] = da2 ? da[t] + da2[t] : da[t];  // da_add_1 + da_add_2 (resol_HOS.f90:490)
   }
   __syncthreads();
   const int ch = (n3a + kCy - 1) / kCy;
@@ -626,7 +888,8 @@ __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
 // phiadd_SL (3-D): products Q_q(i1, i3, j2) = a(i3, j2) * T_q(i1, i3, j2)
 __global__ void k_phiadd_q(const double* __restrict__ a1, const double* __restrict__ a2,
                            const double* __restrict__ a3, const double* __restrict__ da,
-                           const double* __restrict__ csh, const double* __restrict__ ksh,
+                           const double* __restrict__ da2, const double* __restrict__ csh,
+                           const double* __restrict__ ksh,
                            const double* __restrict__ kycsh, const double* __restrict__ kxcsh,
                            int n1, int n2, int n3a, double* Qt, double* Qx, double* Qy, double* Qz,
                            double* Qp) {
@@ -636,7 +899,7 @@ __global__ void k_phiadd_q(const double* __restrict__ a1, const double* __restri
   if (o >= n) return;
   const long long r = o / n1;  // i3 + n3a * j2
   const double a = a1[r] + a2[r] + a3[r];
-  Qt[o] = da[r] * csh[o];
+  Qt[o] = (da2 ? da[r] + da2[r] : da[r]) * csh[o];
   Qx[o] = a * ksh[o];
   Qy[o] = a * kycsh[o];
   Qz[o] = a * kxcsh[o];
@@ -991,6 +1254,127 @@ static bool has_wavemaker(const Params& P) {
   return P.icase != 1 && (P.igeom == 1 || P.igeom == 2);
 }
 
+// work fields of the second order in Dev::w2
+enum {
+  W2_F = 0,     // phiadd_1st_SWEET set in space (W_NF)
+  W2_FM = 11,   // the same, y-modal (3-D tanks)
+  W2_P9 = 22,   // free-surface products of d1st_for_2nd (9)
+  W2_T9 = 31,   // their F2S (9)
+  W2_AP = 40,   // wavemaker-grid products (6)
+  W2_WA = 46,   // their F2S_add (6)
+  W2_WFM = 52,  // free-surface modes on the wavemaker, y-modal (6)
+  W2_WF = 58,   // the same in space (6)
+  W2_PHIX = 64, W2_PHIY, W2_ETAX, W2_ETAY, W2_PHIZT, W2_PHIXX, W2_PHIZZ, W2_PZ,
+  W2_BC2 = 72, W2_P2T, W2_P2Z, W2_P2TM, W2_P2ZM, W2_PZ2S, W2_RHS2, W2_A2K,
+  W2_COUNT
+};
+static_assert(W2_COUNT <= Dev::kW2, "second-order work fields");
+
+// d1st_for_2nd and solveHOS_SWEET_2 (resol_wmkr.f90:219-329, 645-864) on the
+// wavemaker stream, after solveHOS_SWEET_1 of the same stage: fills the
+// slopes of a_add_2, a2nd and eta2nd.
+void enqueue_sweet2(Ctx& c, Enq& W, const double* y, double* k) {
+  const Params& P = c.P;
+  const Dev& d = c.d;
+  const StateLayout& L = c.L;
+  const int n1 = P.n1, n2 = P.n2, n3 = P.n3, n3a = P.n3a;
+  const long long nN = (long long)n1 * n2, nA = (long long)n3a * n2;
+  cudaStream_t sw = W.st;
+  const double* aA1 = y + L.off[S_AADD1];
+  const double* kA1 = k + L.off[S_AADD1];
+  const double* a1 = y + L.off[S_A1ST];
+  const double* da1 = k + L.off[S_A1ST];
+  double* const* w = d.w2;
+  // wavemaker-grid terms of phiadd_1st_SWEET
+  AddProdOut ap{};
+  for (int q = 0; q < 6; ++q) ap.p[q] = w[W2_AP + q];
+  W.ew(k_add_prod, nA, aA1, kA1, (const double*)d.k_add, (const double*)d.kx_add, (const double*)d.ky, n3a,
+       nA, ap);
+  {
+    std::vector<XfReq> rq;
+    const int kz[6] = {0, 0, 0, 0, 1, 1}, ky_[6] = {0, 0, 1, 1, 0, 0};
+    for (int q = 0; q < 6; ++q)
+      rq.push_back(W.R(GRID_ADD, -1, kz[q], ky_[q], w[W2_AP + q], n3a, n3a, n2, w[W2_WA + q], n3a, n3a, n2));
+    W.xf(rq);
+  }
+  // d1st_for_2nd on the free surface: products and their F2S
+  FsProdOut fp{};
+  for (int q = 0; q < 9; ++q) fp.p[q] = w[W2_P9 + q];
+  W.ew(k_fs_prod1, nN, a1, da1, (const double*)d.kx, (const double*)d.ky, (const double*)d.kth1, n1, nN, fp);
+  {
+    std::vector<XfReq> rq;
+    const int kx_[9] = {1, 0, 1, 0, 0, 0, 0, 1, 0}, ky_[9] = {0, 1, 0, 1, 0, 0, 0, 0, 1};
+    for (int q = 0; q < 9; ++q) rq.push_back(W.F2S_N(w[W2_P9 + q], w[W2_T9 + q], kx_[q], ky_[q]));
+    W.xf(rq);
+  }
+  // d1st_for_2nd on the wavemaker
+  WmkFsOut wo{};
+  for (int q = 0; q < 6; ++q) wo.w[q] = n2 == 1 ? w[W2_WF + q] : w[W2_WFM + q];
+  launch_pdl(k_wmk_from_fs, dim3(n3, n2), dim3(128), 0, sw, a1, da1, (const double*)d.kx2cshx,
+             (const double*)d.kycshx, (const double*)d.kshx, n1, n2, n3, wo);
+  if (n2 != 1)
+    for (int q = 0; q < 6; ++q)
+      launch_y_f2s(W.tb, w[W2_WFM + q], n3, n3, w[W2_WF + q], n3, (q == 2 || q == 3) ? 1 : 0, sw);
+  D1stArgs g{};
+  for (int q = 0; q < 9; ++q) g.T[q] = w[W2_T9 + q];
+  for (int f = 0; f < W_NF; ++f) g.F[f] = w[W2_F + f];
+  g.phiz1st = d.phiz1st;
+  g.phix1st = w[W2_PHIX];
+  g.phiy1st = w[W2_PHIY];
+  g.etax1st = w[W2_ETAX];
+  g.etay1st = w[W2_ETAY];
+  g.phizt1st = w[W2_PHIZT];
+  g.phixx1st = w[W2_PHIXX];
+  g.phizz1st = w[W2_PHIZZ];
+  g.phiz1st_tot = w[W2_PZ];
+  W.ew(k_d1st_combine, nN, g, (const double*)d.nu, (const double*)d.dnux, (double)P.iabsnb, nN);
+  // the second-order wavemaker condition, matched, transformed, divided
+  Sweet2Wmk sv{};
+  for (int q = 0; q < 6; ++q) {
+    sv.wf[q] = w[W2_WF + q];
+    sv.wa[q] = w[W2_WA + q];
+  }
+  launch_pdl(k_sweet2_wmk, dim3(n2), dim3(128), 0, sw, (const double*)d.pos_re, (const double*)d.pos_im,
+             (const double*)d.dposdy_re, (const double*)d.dposdy_im, (const double*)d.freq_w,
+             (const double*)d.eiwt, (const double*)d.gzed, (const double*)d.dgzed, (const double*)d.sc, c.nf, n2,
+             n3, n3a, sv, w[W2_BC2]);
+  {
+    const int tot = (n3a - n3) * n2;
+    launch_pdl(k_extend, dim3(nblk(tot)), dim3(kEW), 0, sw, w[W2_BC2], (double*)nullptr, d.ext, n2, n3, n3a);
+  }
+  double* kA2 = k + L.off[S_AADD2];
+  W.xf({W.R(GRID_ADD, 1, 0, 0, w[W2_BC2], n3a, n3a, n2, kA2, n3a, n3a, n2)});
+  W.ew(k_div, nA, kA2, (double*)nullptr, (const double*)d.k_add_thk, nA);
+  // phiadd_2nd: phit_add_2, phiz_add_2 at z = 0
+  const double* aA2 = y + L.off[S_AADD2];
+  launch_pdl(k_sweet_contract, dim3((n1 + kCx - 1) / kCx, n2), dim3(kCx * kCy), 0, sw, aA2,
+             (const double*)kA2, (const double*)d.cosk, (const double*)d.sink, (const double*)d.csh,
+             (const double*)d.kxcsh, n1, n2, n3a, n2 == 1 ? w[W2_P2T] : w[W2_P2TM],
+             n2 == 1 ? w[W2_P2Z] : w[W2_P2ZM]);
+  if (n2 != 1) {
+    launch_y_f2s(W.tb, w[W2_P2TM], n1, n1, w[W2_P2T], n1, 0, sw);
+    launch_y_f2s(W.tb, w[W2_P2ZM], n1, n1, w[W2_P2Z], n1, 0, sw);
+  }
+  // phidphiz of the second order and the free-surface conditions
+  W.ew(k_mul, nN, y + L.off[S_A2ND], (const double*)d.kth1, 1.0, w[W2_A2K], nN);
+  W.xf({W.F2S_N(w[W2_A2K], w[W2_PZ2S])});
+  Sweet2Fs fs{};
+  fs.phiz2nd_spec = w[W2_PZ2S];
+  fs.p2z = w[W2_P2Z];
+  fs.p2t = w[W2_P2T];
+  fs.eta2nd = y + L.off[S_ETA2ND];
+  fs.eta1st = y + L.off[S_ETA1ST];
+  fs.phix1st = w[W2_PHIX];
+  fs.etax1st = w[W2_ETAX];
+  fs.phiy1st = w[W2_PHIY];
+  fs.etay1st = w[W2_ETAY];
+  fs.phizz1st = w[W2_PHIZZ];
+  fs.phiz1st = w[W2_PZ];
+  fs.phizt1st = w[W2_PHIZT];
+  W.ew(k_sweet2_fs, nN, fs, (const double*)d.nu, (double)P.iabsnb, k + L.off[S_ETA2ND], w[W2_RHS2], nN);
+  W.xf({W.S2F_N(w[W2_RHS2], k + L.off[S_A2ND])});
+}
+
 void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t st) {
   Enq E(c, st);
   const Params& P = c.P;
@@ -1017,6 +1401,7 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   //    main stream before assembly.
   cudaStream_t sw = c.st2;
   Enq W(c, sw, c.tb2, d.xtmp2, nullptr, 0);
+  const bool wmk2 = has_wavemaker(P) && P.i_wmk == 2;
   cudaEventRecord(c.ev_fork, st);
   cudaStreamWaitEvent(sw, c.ev_fork, 0);
   double* kA1 = k + L.off[S_AADD1];
@@ -1037,32 +1422,53 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     W.ew(k_div, nA, kA1, kAR, (const double*)d.k_add_thk, nA);
     // reconstruction at z = 0 (phiadd_1st_SWEET) for phit_add_1, phiz_add_1
     const double* aA1 = y + L.off[S_AADD1];
-    launch_pdl(k_sweet_contract, dim3(dim3((n1 + kCx - 1) / kCx, n2)), dim3(kCx * kCy), 0, sw, 
-        aA1, kA1, d.cosk, d.sink, d.csh, d.kxcsh, n1, n2, P.n3a, n2 == 1 ? d.phit_add1 : d.Q[0],
-        n2 == 1 ? d.phiz_add1 : d.Q[1]);
-    if (n2 != 1) {
-      // y sums: sum_j2 A(i1, j2) cos(ky(j2) y(i2)) = FOURIER_2_SPACE_y
-      launch_y_f2s(W.tb, d.Q[0], n1, n1, d.phit_add1, n1, 0, sw);
-      launch_y_f2s(W.tb, d.Q[1], n1, n1, d.phiz_add1, n1, 0, sw);
+    const double* phit1 = d.phit_add1;
+    const double* phiz1 = d.phiz_add1;
+    if (wmk2) {
+      // the whole first-order set that the second order needs
+      Contract1Out co{};
+      for (int f = 0; f < W_NF; ++f) co.f[f] = n2 == 1 ? d.w2[W2_F + f] : d.w2[W2_FM + f];
+      launch_pdl(k_fs_contract1, dim3((n1 + kCx - 1) / kCx, n2), dim3(kCx * kCy), 0, sw, aA1,
+                 (const double*)kA1, (const double*)d.cosk, (const double*)d.sink, (const double*)d.kx_add,
+                 (const double*)d.k_add, (const double*)d.ky, (const double*)d.csh, (const double*)d.ksh,
+                 (const double*)d.kycsh, (const double*)d.kxcsh, n1, n2, P.n3a, co);
+      if (n2 != 1)
+        for (int f = 0; f < W_NF; ++f)
+          launch_y_f2s(W.tb, d.w2[W2_FM + f], n1, n1, d.w2[W2_F + f], n1,
+                       (f == W_Y || f == W_YT || f == W_YZ) ? 1 : 0, sw);
+      phit1 = d.w2[W2_F + W_T];
+      phiz1 = d.w2[W2_F + W_Z];
+    } else {
+      launch_pdl(k_sweet_contract, dim3(dim3((n1 + kCx - 1) / kCx, n2)), dim3(kCx * kCy), 0, sw,
+          aA1, kA1, d.cosk, d.sink, d.csh, d.kxcsh, n1, n2, P.n3a, n2 == 1 ? d.phit_add1 : d.Q[0],
+          n2 == 1 ? d.phiz_add1 : d.Q[1]);
+      if (n2 != 1) {
+        // y sums: sum_j2 A(i1, j2) cos(ky(j2) y(i2)) = FOURIER_2_SPACE_y
+        launch_y_f2s(W.tb, d.Q[0], n1, n1, d.phit_add1, n1, 0, sw);
+        launch_y_f2s(W.tb, d.Q[1], n1, n1, d.phiz_add1, n1, 0, sw);
+      }
     }
     // phidphiz + SWEET_1 RHS
     W.ew(k_mul, nN, y + L.off[S_A1ST], (const double*)d.kth1, 1.0, d.a1k, nN);
     W.xf({W.F2S_N(d.a1k, d.phiz1st)});
-    W.ew(k_sweet_rhs, nN, y + L.off[S_ETA1ST], (const double*)d.phit_add1,
-         (const double*)d.phiz1st, (const double*)d.phiz_add1, (const double*)d.nu,
-         (double)P.iabsnb, d.rhs1, kEta1, nN);
+    W.ew(k_sweet_rhs, nN, y + L.off[S_ETA1ST], phit1, (const double*)d.phiz1st, phiz1,
+         (const double*)d.nu, (double)P.iabsnb, d.rhs1, kEta1, nN);
     W.xf({W.S2F_N(d.rhs1, kA1st)});
+    if (wmk2) enqueue_sweet2(c, W, y, k);
   } else {
     cudaMemsetAsync(kA1, 0, sizeof(double) * nA, sw);
     cudaMemsetAsync(kAR, 0, sizeof(double) * nA, sw);
     cudaMemsetAsync(kA1st, 0, sizeof(double) * nN, sw);
     cudaMemsetAsync(kEta1, 0, sizeof(double) * nN, sw);
   }
-  // second- and third-order wavemaker slopes stay zero (i_wmk = 1)
-  cudaMemsetAsync(k + L.off[S_AADD2], 0, sizeof(double) * nA, sw);
+  // the third-order slope stays zero (i_wmk <= 2); so do the second-order
+  // slopes without a second-order wavemaker
+  if (!wmk2) {
+    cudaMemsetAsync(k + L.off[S_AADD2], 0, sizeof(double) * nA, sw);
+    cudaMemsetAsync(k + L.off[S_A2ND], 0, sizeof(double) * nN, sw);
+    cudaMemsetAsync(k + L.off[S_ETA2ND], 0, sizeof(double) * nN, sw);
+  }
   cudaMemsetAsync(k + L.off[S_AADD3], 0, sizeof(double) * nA, sw);
-  cudaMemsetAsync(k + L.off[S_A2ND], 0, sizeof(double) * nN, sw);
-  cudaMemsetAsync(k + L.off[S_ETA2ND], 0, sizeof(double) * nN, sw);
 
   // 2. transform batch A: eta in space, eta / eta_x / eta_y / phis_x / phis_y on
   //    the big grid (phisxy_etaxy) and the order-1 HOS terms F2S_big(a1 kth_ext(j))
@@ -1092,17 +1498,18 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   //     amplitudes at z = eta (needs eta in space from batch A) and the
   //     gradients of phi_add on the big grid (resol_HOS.f90:534-555)
   if (has_wavemaker(P)) {
+    const double* kA2 = wmk2 ? k + L.off[S_AADD2] : nullptr;
     cudaStreamWaitEvent(sw, c.ev_eta, 0);
     const double* aA1 = y + L.off[S_AADD1];
     const double* aA2 = y + L.off[S_AADD2];
     const double* aA3 = y + L.off[S_AADD3];
     if (n2 == 1) {
       launch_pdl(k_phiadd_sl_1d, dim3((n1 + kCx - 1) / kCx), dim3(kCx * kCy), 0, sw, d.eta_sp, aA1, aA2,
-                 aA3, kA1, d.kx_add, d.csh, d.ksh, d.kxcsh, n1, P.n3a, d.phix_add, d.phiy_add, d.phiz_add,
-                 d.phit_add, d.phi_add);
+                 aA3, (const double*)kA1, kA2, d.kx_add, d.csh, d.ksh, d.kxcsh, n1, P.n3a, d.phix_add,
+                 d.phiy_add, d.phiz_add, d.phit_add, d.phi_add);
     } else {
       const long long nq = (long long)n1 * P.n3a * n2;
-      W.ew(k_phiadd_q, nq, aA1, aA2, aA3, (const double*)kA1, (const double*)d.csh,
+      W.ew(k_phiadd_q, nq, aA1, aA2, aA3, (const double*)kA1, kA2, (const double*)d.csh,
            (const double*)d.ksh, (const double*)d.kycsh, (const double*)d.kxcsh, n1, n2, P.n3a,
            d.Q[0], d.Q[1], d.Q[2], d.Q[3], d.Q[4]);
       const int lines = n1 * P.n3a;

@@ -81,6 +81,12 @@ struct Dev {
   double* grp[24] = {};         // dealiasing groups of the quadratic terms
   // wavemaker grid
   double *bc1 = nullptr, *bcr = nullptr;
+  // second-order wavemaker (i_wmk = 2)
+  double *kx2cshx = nullptr, *kycshx = nullptr, *kshx = nullptr;  // [i1 + n1 (i2 + n2 i3)], i3 < n3
+  double *k_add = nullptr;                                         // n3_add x n2
+  double *dnux = nullptr, *dgzed = nullptr, *dposdy_re = nullptr, *dposdy_im = nullptr;
+  static constexpr int kW2 = 80;
+  double* w2[kW2] = {};  // work fields of the second order, max(n1 n2, n3_add n2) each
   // 3-D phiadd_SL workspace (n1 * n3a * n2 each)
   double *Q[5] = {}, *B[5] = {};
   // transform temporaries
@@ -106,6 +112,7 @@ struct Ctx {
   // host tables kept for the oracle-free host logic
   std::vector<double> kx, ky, cx, cy, cz, omega;
   std::vector<std::complex<double>> pos_ini;  // n2 x nf, i2 fastest
+  std::vector<std::complex<double>> dposdy_ini;  // d pos_ini / dy, n2 x nf
   std::vector<double> freq_w, gzed;
   std::vector<double> probes;  // nondimensional (x, y)
   int nprobes = 0;

@@ -320,6 +320,22 @@ class Fourier:
             out = tmp
         return out
 
+    def F2S_y(self, f, csy="cos"):
+        """FOURIER_2_SPACE_y (fourier_FFTW.f90:340-428) along axis 1; the
+        identity when n2 = 1."""
+        f = np.array(f, dtype=np.float64, copy=True)
+        n2 = self.n2
+        if n2 == 1:
+            return f
+        fy = np.ones(n2)
+        fy[1:n2 - 1] = 0.5
+        inp = f * fy[None, :]
+        if csy == "cos":
+            return _r2r(inp, 1, "REDFT00")
+        out = np.zeros_like(inp)
+        out[:, 1:n2 - 1] = _r2r(inp[:, 1:n2 - 1], 1, "RODFT00")
+        return out
+
     def S2F_add(self, f, csz="cos", csy="cos"):
         return self._execute_add(f, csz, csy, 1) * self.s2f_add
 
@@ -366,8 +382,8 @@ class Tank:
                 raise ValueError(f"forbidden value of {name}: {v}")
         if self.p1 > self.M or self.p2 > self.M:
             raise ValueError("p1/p2 higher than M")
-        if self.inp["i_wmk"] != 1 and self.inp["icase"] != 1:
-            raise NotImplementedError("only the first-order wavemaker (i_wmk=1)")
+        if self.inp["i_wmk"] not in (1, 2) and self.inp["icase"] != 1:
+            raise NotImplementedError("first- and second-order wavemakers (i_wmk = 1, 2) only")
 
     # ------------------------------------------------------------------ setup
     def _nondim(self):
@@ -626,6 +642,20 @@ class Tank:
         return delta / (2.0 * (1.0 - dh)) * (5.0 / 16.0 + (U / delta) + 15.0 / 16.0 * (
             (U / delta) ** 2 - 1.0 / 3.0 * (U / delta) ** 4 + 1.0 / 15.0 * (U / delta) ** 6))
 
+    def _dgzeddz(self, z):
+        """dgzeddz (wavemaking.f90:222-250)."""
+        dh = self.d_hinge
+        delta = min(dh, (1.0 - dh) / 10.0)
+        if self.igeom == 1:
+            return 0.0
+        if z >= (dh - 1.0 + delta):
+            return 1.0 / (1.0 - dh)
+        if z <= (dh - 1.0 - delta):
+            return 0.0
+        U = z - (dh - 1.0)
+        return 1.0 / (1.0 - dh) * (1.0 / 2.0 + 15.0 / 16.0 * ((U / delta) - 2.0 / 3.0 * (U / delta) ** 3
+                                                               + 1.0 / 5.0 * (U / delta) ** 5))
+
     def _wmk_ini(self):
         """wmk_ini (wavemaking.f90:37-175), full-width wavemaker (iwidth=1)."""
         w = self.wave
@@ -637,6 +667,7 @@ class Tank:
             if len(idx):
                 groups.append(idx)
         pos_ini = np.zeros((self.n2, len(groups)), dtype=np.complex128)
+        dposdy_ini = np.zeros((self.n2, len(groups)), dtype=np.complex128)
         freq = np.zeros(len(groups))
         for g_i, idx in enumerate(groups):
             freq[g_i] = w["freq"][idx[0]]
@@ -647,14 +678,27 @@ class Tank:
                     acc = acc + 1.0 * (w["TF"][i] * math.cos(ang) * w["ampli"][i] * np.exp(
                         1j * (-w["k"][i] * math.sin(ang) * self.cy[j1] + w["phase"][i])))
                 pos_ini[j1, g_i] = acc
+                # dposdy_ini, full-width wavemaker (rampy = 1, drampy = 0)
+                dacc = 0j
+                for i in idx:
+                    ang = w["angle"][i]
+                    pos_tmp = w["TF"][i] * math.cos(ang) * w["ampli"][i] * np.exp(
+                        1j * (-w["k"][i] * math.sin(ang) * self.cy[j1] + w["phase"][i]))
+                    dacc = dacc + (0.0 - 1j * w["k"][i] * math.sin(ang) * 1.0) * pos_tmp
+                dposdy_ini[j1, g_i] = dacc
         self.pos_ini = pos_ini
+        self.dposdy_ini = dposdy_ini
         self.freq_w = freq
         self.pos_gzed = np.array([self._gzed(z) for z in self.cz])
+        self.dpos_gzed = np.array([self._dgzeddz(z) for z in self.cz])
 
     def _absorb(self):
         """absorb (initial_condition.f90:724-794), iwidth=1, no back beach."""
         n1, n2 = self.n1, self.n2
         self.nu = np.zeros((n1, n2))
+        # dnux as written in absorb: coeffabsf * 2 * x3 (without 1 / x2)
+        self.dnux = np.zeros((n1, n2))
+        self.dnuy = np.zeros((n1, n2))
         if self.iabsnb == 0:
             return
         xabsf, coeff = self.inp["xabsf"], self.inp["coeffabsf"]
@@ -665,6 +709,7 @@ class Tank:
                 if self.cx[i1] >= x0:
                     x3 = (self.cx[i1] - x0) / x2
                     self.nu[i1, :] = coeff * x3 * x3
+                    self.dnux[i1, :] = coeff * 2 * x3
 
     def _tables(self):
         """Spectral tables (HOS-NWT.f90:267-406)."""
@@ -725,6 +770,15 @@ class Tank:
                                * np.cos(self.ky[None, :, None] * P[None, None, :, 1]))
 
     # --------------------------------------------------------- wavemaker law
+        if self.inp["i_wmk"] >= 2:
+            # free-surface modes on the wavemaker (HOS-NWT.f90:343-355)
+            arg = self.k[:, :, None] * self.cx_add[None, None, :]
+            csh0 = np.cosh(self.k)[:, :, None]
+            cshx = np.cosh(arg) / csh0
+            self.kx2cshx_add = cshx * kx2[:, None, None]
+            self.kycshx_add = cshx * self.ky[None, :, None]
+            self.kshx_add = self.k[:, :, None] * np.sinh(arg) / csh0
+
     def ramp(self, time):
         """ramp (resol_wmkr.f90:1268-1397)."""
         iramp, Tramp, T_stop = self.iramp, self.Tramp, self.T_stop
@@ -906,7 +960,7 @@ class Tank:
 
     # --------------------------------------------------------- initialize
     def _initialize(self):
-        """initialize (initial_condition.f90:314-482), i_wmk = 1."""
+        """initialize (initial_condition.f90:314-482), i_wmk = 1, 2."""
         n1, n2, n3, n3_add = self.n1, self.n2, self.n3, self.n3_add
         self.time = 0.0
         self.time_cur = 0.0
@@ -939,12 +993,17 @@ class Tank:
             self.a1st, self.eta1st, self.a1st_add, self.time)
         self.a_add_ramp = self.a1st_add.copy()
         self.da1st_add = da_add
+        if self.inp["i_wmk"] == 2:
+            _, _, da_add_2, _ = self.solveHOS_SWEET_2(self.a2nd, self.eta2nd, self.eta1st, self.a2nd_add,
+                                                      self.time)
+            da_add = da_add + da_add_2
         out = self.phiadd_SL(self.a1st_add + self.a2nd_add + self.a3rd_add, da_add, self.eta)
         self.phi_add = out[0]
 
     # --------------------------------------------------------- SWEET 1
     def solveHOS_SWEET_1(self, a1st, eta1st, a_add_1, time):
-        """solveHOS_SWEET_1 (resol_wmkr.f90:109-210), i_wmk = 1.
+        """solveHOS_SWEET_1 (resol_wmkr.f90:109-210); with i_wmk = 2 also the
+        first-order set of d1st_for_2nd for solveHOS_SWEET_2.
         Returns da1st (modes), deta1st (space), da_add_1, da_add_ramp and
         (phi_add_1, phit_add_1, phiz_add_1)."""
         n1, n2, n3 = self.n1, self.n2, self.n3
@@ -976,7 +1035,121 @@ class Tank:
         phiz1st = F.F2S(a1st * self.kth[:, :, 0], "cos", "cos") + phi2z
         self._tick(3)
         da1 = F.S2F(-eta1st - phi2t - self.iabsnb * self.nu * phiz1st, "cos", "cos")
+        if self.inp["i_wmk"] >= 2:
+            self._d1st = self._d1st_for_2nd(a1st, da1, a_add_1, d1, phiz1st)
         return da1, phiz1st, d1, dr, (phi2, phi2t, phi2z)
+
+    def _contract_fs(self, coef, tab, trig="cos"):
+        """sum_{i3, j2} coef(i3, j2) tab(i1, j2, i3) trig(ky(j2) y(i2)): the
+        z = 0 reconstructions of phiadd_1st_SWEET / phiadd_2nd."""
+        A = np.einsum("ij,kji->kj", coef, tab)
+        m = np.cos if trig == "cos" else np.sin
+        return A @ m(self.ky[:, None] * self.cy[None, :])
+
+    def _d1st_for_2nd(self, a1st, da1st, a_add, da_add, phiz1st):
+        """phiadd_1st_SWEET's full output set (resol_wmkr.f90:446-574) and
+        d1st_for_2nd (resol_wmkr.f90:645-793): first-order quantities on the
+        free surface and on the wavemaker that the second order needs."""
+        F = self.fourier
+        n3 = self.n3
+        ca = np.cos(self.kx_add)[:, None]
+        sa = np.sin(self.kx_add)[:, None]
+        kxa = self.kx_add[:, None]
+        ka2 = self.k_add * self.k_add
+        ky = self.ky
+        C = self._contract_fs
+        q = {}
+        q["phi2x"] = -C(a_add * ca, self.k_add_sh_add_x)
+        q["phi2y"] = -C(a_add * ca, self.kycsh_add_x, "sin")
+        q["phi2zz"] = -C(a_add * ca * kxa, self.kx_add_csh_add_x)
+        q["phi2xt"] = -C(da_add * ca, self.k_add_sh_add_x)
+        q["phi2yt"] = -C(da_add * ca, self.kycsh_add_x, "sin")
+        q["phi2zt"] = -C(da_add * sa, self.kx_add_csh_add_x)
+        q["phi2xx"] = C(a_add * ca * ka2, self.csh_add_x)
+        q["phi2xz"] = C(a_add * sa * kxa, self.k_add_sh_add_x)
+        q["phi2yz"] = C(a_add * sa * ky[None, :], self.csh_add_x, "sin")
+        # on the wavemaker (the add grid's first n3 nodes)
+        w_xx = F.F2S_add(a_add * ka2, "cos", "cos")[:n3]
+        w_xxt = F.F2S_add(da_add * ka2, "cos", "cos")[:n3]
+        w_y = F.F2S_add(-a_add * ky[None, :], "cos", "sin")[:n3]
+        w_yt = F.F2S_add(-da_add * ky[None, :], "cos", "sin")[:n3]
+        w_z = F.F2S_add(-a_add * kxa, "sin", "cos")[:n3]
+        w_zt = F.F2S_add(-da_add * kxa, "sin", "cos")[:n3]
+        # d1st_for_2nd: free-surface modes on the wavemaker, y to space
+        def onwmk(a, tab, sign):
+            return sign * np.einsum("ij,ijk->kj", a, tab)   # (n3, n2)
+        d = {}
+        d["phixx_add"] = F.F2S_y(onwmk(a1st, self.kx2cshx_add, -1.0), "cos") + w_xx
+        d["phixxt_add"] = F.F2S_y(onwmk(da1st, self.kx2cshx_add, -1.0), "cos") + w_xxt
+        d["phiy_add"] = F.F2S_y(onwmk(a1st, self.kycshx_add, -1.0), "sin") + w_y
+        d["phiyt_add"] = F.F2S_y(onwmk(da1st, self.kycshx_add, -1.0), "sin") + w_yt
+        d["phiz_add"] = F.F2S_y(onwmk(a1st, self.kshx_add, 1.0), "cos") + w_z
+        d["phizt_add"] = F.F2S_y(onwmk(da1st, self.kshx_add, 1.0), "cos") + w_zt
+        kx = self.kx[:, None]
+        kyv = ky[None, :]
+        kth1 = self.kth[:, :, 0]
+        d["phix1st"] = F.F2S(-a1st * kx, "sin", "cos") + q["phi2x"]
+        d["phiy1st"] = F.F2S(-a1st * kyv, "cos", "sin") + q["phi2y"]
+        etax = F.F2S(da1st * kx, "sin", "cos")
+        etay = F.F2S(da1st * kyv, "cos", "sin")
+        d["phizt1st"] = F.F2S(da1st * kth1, "cos", "cos") + q["phi2zt"]
+        d["phixx1st"] = F.F2S(-a1st * kx * kx, "cos", "cos") + q["phi2xx"]
+        d["phizz1st"] = F.F2S(a1st * self.k * self.k, "cos", "cos") + q["phi2zz"]
+        phixz = F.F2S(-a1st * kx * kth1, "sin", "cos") + q["phi2xz"]
+        phiyz = F.F2S(-a1st * kyv * kth1, "cos", "sin") + q["phi2yz"]
+        d["etax1st"] = etax - q["phi2xt"] - self.iabsnb * (self.dnux * phiz1st + self.nu * phixz)
+        d["etay1st"] = etay - q["phi2yt"] - self.iabsnb * (self.dnuy * phiz1st + self.nu * phiyz)
+        d["phiz1st"] = phiz1st
+        return d
+
+    def _dpos_1st(self, time):
+        """dposdy_1st and dposdz_1st (wavemaking.f90:313-406): y and z
+        derivatives of the paddle position and their time derivatives."""
+        w = TWOPI * self.freq_w
+        eiwt = np.exp(1j * w * time)
+        ry = self.dposdy_ini * eiwt[None, :]         # (n2, nf)
+        rz = self.pos_ini * eiwt[None, :]
+        g = self.pos_gzed[:, None]
+        dg = self.dpos_gzed[:, None]
+        dy = g * ry.sum(axis=1).real[None, :]
+        dyt = g * (ry * (1j * w)[None, :]).sum(axis=1).real[None, :]
+        dz = dg * rz.sum(axis=1).real[None, :]
+        dzt = dg * (rz * (1j * w)[None, :]).sum(axis=1).real[None, :]
+        return dy, dyt, dz, dzt
+
+    def solveHOS_SWEET_2(self, a2nd, eta2nd, eta1st, a_add_2, time):
+        """solveHOS_SWEET_2 (resol_wmkr.f90:219-329) with phiadd_2nd
+        (resol_wmkr.f90:802-864), no free-wave correction (ifree = 0).
+        Needs the first-order set of the same stage (solveHOS_SWEET_1).
+        Returns da2nd (modes), deta2nd (space), da_add_2 and the second-order
+        additional fields (phi, phix, phiy, phiz, phit) at z = 0."""
+        F = self.fourier
+        n3 = self.n3
+        d = self._d1st
+        alpha, alphat, alphatt = self._alpha
+        pos, dpos, d2pos = self._pos
+        dy, dyt, dz, dzt = self._dpos_1st(time)
+        noramp = -pos * d["phixx_add"] + dy * d["phiy_add"] + dz * d["phiz_add"]
+        dd = np.zeros((self.n3_add, self.n2))
+        dd[:n3] = -alpha * (-pos * d["phixxt_add"] - dpos * d["phixx_add"] + dy * d["phiyt_add"]
+                            + dyt * d["phiy_add"] + dz * d["phizt_add"] + dzt * d["phiz_add"]) \
+            - alphat * noramp
+        dd = self.match_surface_wmk(dd)
+        da_add_2 = F.S2F_add(dd, "cos", "cos") / self.k_add_thk_add
+        ca = np.cos(self.kx_add)[:, None]
+        sa = np.sin(self.kx_add)[:, None]
+        C = self._contract_fs
+        p2 = C(a_add_2 * ca, self.csh_add_x)
+        p2t = C(da_add_2 * ca, self.csh_add_x)
+        p2z = -C(a_add_2 * sa, self.kx_add_csh_add_x)
+        p2x = -C(a_add_2 * ca, self.k_add_sh_add_x)
+        p2y = -C(a_add_2 * ca, self.kycsh_add_x, "sin")
+        phiz2nd = F.F2S(a2nd * self.kth[:, :, 0], "cos", "cos") + p2z
+        deta2 = phiz2nd - d["phix1st"] * d["etax1st"] - d["phiy1st"] * d["etay1st"] + eta1st * d["phizz1st"]
+        da2 = (-eta2nd - p2t - 0.5 * (d["phix1st"] ** 2 + d["phiy1st"] ** 2 + d["phiz1st"] ** 2)
+               - eta1st * d["phizt1st"] - self.iabsnb * self.nu * deta2)
+        da2 = F.S2F(da2, "cos", "cos")
+        return da2, deta2, da_add_2, (p2, p2x, p2y, p2z, p2t)
 
     # --------------------------------------------------------- phiadd_SL
     def phiadd_SL(self, a_add, da_add, eta):
@@ -1052,6 +1225,11 @@ class Tank:
                 state["a1st"], state["eta1st"], state["a_add_1"], time)
             a_tot = state["a_add_1"] + state["a_add_2"] + state["a_add_3"]
             da_tot = d_add1
+            if self.inp["i_wmk"] == 2:
+                da2, deta2, d_add2, _ = self.solveHOS_SWEET_2(
+                    state["a2nd"], state["eta2nd"], state["eta1st"], state["a_add_2"], time)
+                da_tot = d_add1 + d_add2
+                out.update(a2nd=da2, eta2nd=deta2, a_add_2=d_add2)
             phi_add, phix_add, phiy_add, phiz_add, phit_add = self.phiadd_SL(a_tot, da_tot, etark)
             out.update(a1st=da1, eta1st=deta1, a_add_1=d_add1, a_add_ramp=d_ramp)
         else:
@@ -1060,8 +1238,10 @@ class Tank:
             za = np.zeros((self.n3_add, n2))
             out.update(a1st=z.copy(), eta1st=z.copy(), a_add_1=za.copy(), a_add_ramp=za.copy())
         za = np.zeros((self.n3_add, n2))
-        out.update(a_add_2=za.copy(), a_add_3=za.copy(),
-                   a2nd=np.zeros((n1, n2)), eta2nd=np.zeros((n1, n2)))
+        out.setdefault("a_add_2", za.copy())
+        out.setdefault("a2nd", np.zeros((n1, n2)))
+        out.setdefault("eta2nd", np.zeros((n1, n2)))
+        out.update(a_add_3=za.copy())
         self.phi_add = phi_add
         # grad eta . grad phi_add (resol_HOS.f90:534-555)
         self._tick(9)

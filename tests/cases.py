@@ -36,6 +36,31 @@ REF_REGULAR_3D = dict(inp=default_input(xlen=46.4, ylen=29.74, h=5.0, icase=2, a
                                         d_hinge=2.147, iramp=1, Tramp=3.0, T_stop=40.0, iabsnb=1, xabsf=0.8,
                                         coeffabsf=1.0, toler=1e-4, f_out=10.0, idim=1),
                       n1=256, n2=32, n3=16, mHOS=3, p1=3, p2=3)
+REF_IRREG_2D = dict(inp=default_input(xlen=120.0, ylen=100.0, h=5.0, icase=3, file_name="Hs4_Tp10", i_cut=0,
+                                      ibat=2, i_wmk=2, igeom=2, d_hinge=1.0, iramp=0, Tramp=0.0, T_stop=50.0,
+                                      iabsnb=1, xabsf=0.8, coeffabsf=1.0, toler=1e-4, f_out=30.0, idim=1),
+                    n1=512, n2=1, n3=32, mHOS=3, p1=3, p2=1)
 
-ALL = {"reg1d": REG_1D, "reg1d_m5": REG_1D_M5, "reg3d": REG_3D, "slosh": SLOSH, "jonswap1d": JONSWAP_1D,
+
+def write_ref_wave_files(fx, directory, name="Hs4_Tp10"):
+    """The .cfg/.dat wave files of a reference fixture (the layout file2wave
+    reads, wave_def.f90:181-278), rewritten with the stored values."""
+    import os
+    with open(os.path.join(directory, name + ".cfg"), "w") as f:
+        for v in fx["cfg"]:
+            f.write(f" {v} \n")
+    with open(os.path.join(directory, name + ".dat"), "w") as f:
+        for h, fr, a, an, ph in fx["components"]:
+            f.write(f"{int(h)} , {float(fr)!r} , {float(a)!r} , {float(an)!r} , {float(ph)!r} ,\n")
+
+
+# second-order wavemaker (i_wmk = 2), 2-D and 3-D
+REG_1D_W2 = dict(inp=default_input(T_stop=30.0, amp_mono=0.03, nu_mono=0.8, toler=1e-7, f_out=10.0, i_wmk=2,
+                                   iramp=1, Tramp=1.0),
+                 n1=65, n2=1, n3=17, mHOS=3, p1=3, p2=1)
+REG_3D_W2 = dict(inp=default_input(T_stop=20.0, amp_mono=0.02, nu_mono=0.7, theta_mono=20.0, toler=1e-7,
+                                   f_out=4.0, ylen=20.0, i_wmk=2, iramp=1, Tramp=1.0),
+                 n1=33, n2=17, n3=9, mHOS=3, p1=3, p2=3)
+
+ALL = {"reg1d": REG_1D, "reg1d_w2": REG_1D_W2, "reg3d_w2": REG_3D_W2, "reg1d_m5": REG_1D_M5, "reg3d": REG_3D, "slosh": SLOSH, "jonswap1d": JONSWAP_1D,
        "wide3d": WIDE_3D}

@@ -2,12 +2,12 @@
 
 python tests/golden/make_ref_benchmarks.py [REFERENCE_ROOT]
 
-Reads Benchmark/Sloshing/Ref_data/probes.dat and
-Benchmark/Regular_3D/Ref_data/probes.dat (probe records written by the
-reference HOS-NWT, 61d13.5 format) with their prob.inp probe positions, and
-stores the numbers in ref_sloshing.npz and ref_regular3d.npz beside this
-script, together with the run configuration that each file's input echo
-states. The reference tree is only needed to regenerate the fixtures.
+Reads the probe records that the reference HOS-NWT wrote in
+Benchmark/Sloshing, Benchmark/Regular_3D and Benchmark/Irreg_2D
+(Ref_data/*.dat, 61d13.5 format) with their prob.inp probe positions (and
+Irreg_2D's wave file), and stores the numbers in ref_sloshing.npz,
+ref_regular3d.npz and ref_irreg2d.npz beside this script, together with the
+run configuration that each file's input echo states. The reference tree is only needed to regenerate the fixtures.
 """
 import os
 import sys
@@ -47,4 +47,20 @@ if __name__ == "__main__":
     np.savez_compressed(os.path.join(HERE, "ref_regular3d.npz"), records=r,
                         probes=read_xy(os.path.join(bench, "Regular_3D", "prob.inp")),
                         numerics=np.array([256, 32, 16, 3, 3, 3]))
-    print("sloshing", s.shape, "regular_3d", r.shape)
+    # Irreg_2D: the Hs4_Tp10 file wave, second-order wavemaker (i_wmk = 2),
+    # M = 3, 512 modes, 30 Hz output over 50 s; the wave file's components
+    # are stored too, since the run reads them
+    d = os.path.join(bench, "Irreg_2D")
+    g = read_probes(os.path.join(d, "Ref_data", "probes_Hs4_Tp10.dat"))
+    with open(os.path.join(d, "Hs4_Tp10.cfg")) as f:
+        cfg = [ln.strip() for ln in f if ln.strip()]
+    comp = []
+    with open(os.path.join(d, "Hs4_Tp10.dat")) as f:
+        for ln in f:
+            if ln.strip():
+                comp.append([float(t) for t in ln.replace(",", " ").split()])
+    np.savez_compressed(os.path.join(HERE, "ref_irreg2d.npz"), records=g,
+                        probes=read_xy(os.path.join(d, "prob.inp")),
+                        numerics=np.array([512, 1, 32, 3, 3, 1]), cfg=np.array(cfg),
+                        components=np.array(comp))
+    print("sloshing", s.shape, "regular_3d", r.shape, "irreg_2d", g.shape, len(comp))

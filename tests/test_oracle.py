@@ -145,10 +145,11 @@ def _ref_fixture(name):
     return np.load(os.path.join(os.path.dirname(__file__), "golden", name))
 
 
-def _run_records(case, fx, T_end=None):
+def _run_records(case, fx, T_end=None, wave_dir="."):
     from oracle.hos_oracle import Tank
     probes = [tuple(p) for p in fx["probes"]]
-    o = Tank(case["inp"], case["n1"], case["n2"], case["n3"], case["mHOS"], case["p1"], case["p2"], probes=probes)
+    o = Tank(case["inp"], case["n1"], case["n2"], case["n3"], case["mHOS"], case["p1"], case["p2"], probes=probes,
+             wave_files_dir=wave_dir)
     recs = o.run(T_end=T_end)
     return np.array([[r[0] * o.Tscale] + list(np.asarray(r[1]) * o.h) for r in recs])
 
@@ -160,7 +161,7 @@ def test_oracle_matches_reference_sloshing_record():
     got = _run_records(cases.REF_SLOSHING, fx)
     ref = fx["records"]
     assert got.shape == ref.shape
-    assert np.max(np.abs(got[:, 0] - ref[:, 0])) < 1e-9
+    assert np.all(np.abs(got[:, 0] - ref[:, 0]) <= 0.6 * _digit_unit(ref[:, 0]) + 1e-9)
     err = np.abs(got[:, 1:] - ref[:, 1:]) / (_digit_unit(ref[:, 1:]) + 1e-12)
     assert np.max(err[:, [0, 2]]) <= 0.6, np.max(err)
     assert np.max(np.abs(got[:, 2])) < 1e-12  # the node of the mode
@@ -175,6 +176,21 @@ def test_oracle_matches_reference_regular3d_record():
     got = _run_records(case, fx, T_end=1.0)
     ref = fx["records"][:len(got)]
     assert len(got) == 11
-    assert np.max(np.abs(got[:, 0] - ref[:, 0])) < 1e-9
+    assert np.all(np.abs(got[:, 0] - ref[:, 0]) <= 0.6 * _digit_unit(ref[:, 0]) + 1e-9)
+    err = np.abs(got[:, 1:] - ref[:, 1:]) / (_digit_unit(ref[:, 1:]) + 1e-14)
+    assert np.max(err) <= 0.6, np.max(err)
+
+
+def test_oracle_matches_reference_irreg2d_record(tmp_path):
+    """Benchmark/Irreg_2D: a 4348-component file wave with the second-order
+    wavemaker (i_wmk = 2), M = 3 on 512 modes; the first two seconds (61
+    records of the 1502) on the CPU."""
+    fx = _ref_fixture("ref_irreg2d.npz")
+    assert [int(v) for v in fx["numerics"]] == [512, 1, 32, 3, 3, 1]
+    cases.write_ref_wave_files(fx, str(tmp_path))
+    got = _run_records(cases.REF_IRREG_2D, fx, T_end=2.0, wave_dir=str(tmp_path))
+    ref = fx["records"][:len(got)]
+    assert len(got) == 61
+    assert np.all(np.abs(got[:, 0] - ref[:, 0]) <= 0.6 * _digit_unit(ref[:, 0]) + 1e-9)
     err = np.abs(got[:, 1:] - ref[:, 1:]) / (_digit_unit(ref[:, 1:]) + 1e-14)
     assert np.max(err) <= 0.6, np.max(err)
