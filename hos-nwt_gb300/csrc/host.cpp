@@ -65,6 +65,13 @@ static double wave_number_adim(double f, double prec) {
   return w2;
 }
 
+// wave_number_r (linear_wave.f90:119-133): dimensional depth h
+static double wave_number_r(double f, double h, double prec) {
+  const double w2h = (TWOPI * f) * (TWOPI * f) / G * h;
+  if (w2h < std::log(1.7976931348623157e308) - 1.0) return dichoto(xthx, w2h, 0.0, 10000000.0, prec) / h;
+  return (TWOPI * f) * (TWOPI * f) / G;
+}
+
 // TF_adim_new (linear_wave.f90:277-334), hinged and piston branches
 static std::complex<double> transfer_function(const std::string& typ, double k, double hinge) {
   const std::complex<double> I(0.0, 1.0);
@@ -337,6 +344,61 @@ static void wave_init(Wave& w, const std::string& typ, double hinge) {
   }
 }
 
+// ocean_txt2cfg_dat (read_ocean_txt.f90:33-228) for the ECN wave basin
+// (icase 31) and towing tank (32): the fronts of an Edinburgh Designs .txt
+// file as the lines of the .cfg and .dat files the reference writes and then
+// reads back (the .dat values pass through G20.7, 7 significant digits).
+static int ocean_txt2cfg_dat(const std::string& path, int i_cut, double nuc_low, double nuc_high, int icase,
+                             std::vector<std::string>& cfg, std::vector<std::string>& dat) {
+  std::ifstream f(path);
+  if (!f) return 1;
+  std::vector<std::string> lines;
+  std::string t;
+  while (std::getline(f, t)) lines.push_back(t);
+  int rnum = -1, ramp = 0, rcomp = 0, n_front = -1;
+  size_t n_start = 0;
+  auto after = [](const std::string& s, const std::string& key) {
+    std::istringstream is(s.substr(s.find(key) + key.size()));
+    long long v = 0;
+    is >> v;
+    return v;
+  };
+  for (size_t i = 0; i < lines.size(); ++i) {
+    const std::string& s = lines[i];
+    if (s.find("rnumber  =") != std::string::npos) rnum = (int)after(s, "=");
+    if (s.find("ramp     =") != std::string::npos) ramp = (int)after(s, "=");
+    if (s.find("rnumber compression") != std::string::npos) rcomp = (int)after(s, s.substr(0, s.rfind('=') + 1));
+    if (s.find("Wave has ") != std::string::npos) {
+      n_front = (int)after(s, "Wave has ");
+      n_start = i + 2;
+    }
+  }
+  if (rnum < 0 || n_front < 0 || n_start + n_front > lines.size()) return 1;
+  const double clock = 32.0, f_base = clock / std::pow(2.0, rnum);
+  const double f_lo = i_cut == 1 ? nuc_low : 0.0, f_hi = i_cut == 1 ? nuc_high : 100.0;
+  char buf[128];
+  auto F = [&](const char* fmt, double v) { std::snprintf(buf, sizeof buf, fmt, v); return std::string(buf); };
+  cfg = {F("%2.0f", rnum), F("%5.2f", clock), F("%5.2f", icase == 31 ? 5.0 : 2.88), F("%4.0f", ramp), "lin",
+         F("%5.2f", f_lo), F("%6.2f", f_hi), F("%5.2f", icase == 31 ? 30.0 : 5.0), "hinged",
+         F("%6.3f", icase == 31 ? 2.147 : 0.0)};
+  dat.clear();
+  auto g7 = [&](double v) { std::snprintf(buf, sizeof buf, "%.6E", v); return std::string(buf); };
+  for (int j = 0; j < n_front; ++j) {
+    std::istringstream is(lines[n_start + j]);
+    double h, fr, a, ang, ph;
+    is >> h >> fr >> a >> ang >> ph;
+    long long harmo = std::llround(h);
+    if (rcomp) harmo *= rcomp;
+    const double freq = harmo * f_base;
+    if (icase == 31) ph = ph + wave_number_r(freq, 5.0, 1.0e-12) * 29.74 / 2.0 * std::sin(ang);
+    ang = 180.0 * ang / PI;
+    if (a < 1.0e-98) a = 0.0;
+    if (freq >= f_lo && freq <= f_hi)
+      dat.push_back(std::to_string(harmo) + " " + g7(freq) + " " + g7(a) + " " + g7(ang) + " " + g7(ph));
+  }
+  return 0;
+}
+
 static int wave_cfg(Ctx& c, const char* wave_dir) {
   // initialize_wav_cfg (initial_condition.f90:128-310)
   Params& P = c.P;
@@ -361,13 +423,21 @@ static int wave_cfg(Ctx& c, const char* wave_dir) {
       w.angle = {P.theta_mono};
       w.phase = {P.ph_mono};
     }
-  } else if (P.icase == 3) {
+  } else if (P.icase == 3 || P.icase == 31 || P.icase == 32) {
     std::string base = std::string(wave_dir ? wave_dir : ".") + "/" + trim(in.file_name);
-    std::ifstream cf(base + ".cfg");
-    if (!cf) return fail(c, HOSNWT_ERR_IO, "cannot open %s.cfg", base.c_str());
-    std::vector<std::string> cl;
+    std::vector<std::string> cl, dl;  // the .cfg and .dat lines
     std::string s;
-    while (std::getline(cf, s)) cl.push_back(trim(s));
+    if (P.icase == 3) {
+      std::ifstream cf(base + ".cfg");
+      if (!cf) return fail(c, HOSNWT_ERR_IO, "cannot open %s.cfg", base.c_str());
+      while (std::getline(cf, s)) cl.push_back(trim(s));
+      std::ifstream df(base + ".dat");
+      if (!df) return fail(c, HOSNWT_ERR_IO, "cannot open %s.dat", base.c_str());
+      while (std::getline(df, s)) dl.push_back(s);
+    } else {
+      const int rc = ocean_txt2cfg_dat(base + ".txt", in.i_cut, in.nuc_low, in.nuc_high, P.icase, cl, dl);
+      if (rc) return fail(c, HOSNWT_ERR_IO, "cannot read the ocean file %s.txt", base.c_str());
+    }
     if (cl.size() < 10) return fail(c, HOSNWT_ERR_IO, "short .cfg file");
     auto first = [&](int i) { std::istringstream is(cl[i]); std::string t; is >> t; return t; };
     w.rnum = std::atoi(first(0).c_str());
@@ -380,11 +450,9 @@ static int wave_cfg(Ctx& c, const char* wave_dir) {
     w.clock = clock_d * Ts;
     const double cut_lo_n = cut_lo * Ts, cut_hi_n = cut_hi * Ts;
     hinge = hinge_d / w.depth;
-    std::ifstream df(base + ".dat");
-    if (!df) return fail(c, HOSNWT_ERR_IO, "cannot open %s.dat", base.c_str());
     std::vector<int> ha;
     std::vector<double> fa, aa, ga, pa;
-    while (std::getline(df, s)) {
+    for (std::string s : dl) {
       if (trim(s).empty()) continue;
       for (char& ch : s)
         if (ch == ',') ch = ' ';

@@ -154,6 +154,50 @@ def wave_number_adim_r(f, prec):
     return w2
 
 
+def ocean_txt2cfg_dat(path, i_cut, nuc_low, nuc_high, icase):
+    """ocean_txt2cfg_dat (read_ocean_txt.f90:33-228) for the ECN wave basin
+    (icase 31) and towing tank (32): the fronts of an Edinburgh Designs .txt
+    file as the lines of the .cfg and .dat files it writes (the .dat values
+    pass through G20.7, i.e. 7 significant digits)."""
+    with open(path, encoding="latin-1") as f:
+        lines = f.read().splitlines()
+    rnum = ramp = rcomp = n_front = n_start = None
+    for i, t in enumerate(lines):
+        if "rnumber  =" in t:
+            rnum = int(t.split("=")[1].split()[0])
+        if "ramp     =" in t:
+            ramp = int(t.split("=")[1].split()[0])
+        if "rnumber compression" in t:
+            rcomp = int(t.split("=")[-1].split()[0])
+        if "Wave has " in t:
+            n_front = int(t.split("Wave has ")[1].split()[0])
+            n_start = i + 2
+    vals = np.array([[float(v) for v in lines[n_start + j].split()[:5]] for j in range(n_front)])
+    harmo = vals[:, 0].astype(np.int64)
+    ampli, angle, phase = vals[:, 2].copy(), vals[:, 3].copy(), vals[:, 4].copy()
+    if rcomp is not None:
+        harmo = harmo * rcomp
+    clock = 32.0
+    freq = harmo * (clock / 2 ** rnum)
+    if icase == 31:
+        for i in range(n_front):
+            k = wave_number_r(freq[i], 5.0, 1.0e-12)
+            phase[i] = phase[i] + k * 29.74 / 2.0 * math.sin(angle[i])
+    angle = 180.0 * angle / PI
+    f_lo, f_hi = (nuc_low, nuc_high) if i_cut == 1 else (0.0, 100.0)
+    if icase == 31:
+        cfg = [f"{rnum:2d}", f"{clock:5.2f}", f"{5.0:5.2f}", f"{ramp:4d}", "lin", f"{f_lo:5.2f}",
+               f"{f_hi:6.2f}", f"{30.0:5.2f}", "hinged", f"{2.147:6.3f}"]
+    else:
+        cfg = [f"{rnum:2d}", f"{clock:5.2f}", f"{2.88:5.2f}", f"{ramp:4d}", "lin", f"{f_lo:5.2f}",
+               f"{f_hi:6.2f}", f"{5.0:5.2f}", "hinged", f"{0.0:6.3f}"]
+    ampli[ampli < 1.0e-98] = 0.0
+    g7 = lambda v: f"{float(v):.6E}"
+    dat = [f"{int(harmo[i]):5d} {g7(freq[i])} {g7(ampli[i])} {g7(angle[i])} {g7(phase[i])}"
+           for i in range(n_front) if f_lo <= freq[i] <= f_hi]
+    return cfg, dat
+
+
 def wave_number_r(f, h, prec):
     """linear_wave.f90:120-134 (dimensional)."""
     w2h = (TWOPI * f) ** 2 / G * h
@@ -498,10 +542,16 @@ class Tank:
                 angle = np.array([self.theta_mono])
                 phase = np.array([self.ph_mono])
             depth, hinge = h, self.d_hinge
-        elif self.icase == 3:
+        elif self.icase in (3, 31, 32):
             base = os.path.join(self.wave_files_dir, p["file_name"].strip())
-            with open(base + ".cfg") as f:
-                cl = [ln.strip() for ln in f.read().splitlines()]
+            if self.icase == 3:
+                with open(base + ".cfg") as f:
+                    cl = [ln.strip() for ln in f.read().splitlines()]
+                with open(base + ".dat") as f:
+                    dat_lines = f.read().splitlines()
+            else:
+                cl, dat_lines = ocean_txt2cfg_dat(base + ".txt", p["i_cut"], p["nuc_low"], p["nuc_high"],
+                                                  self.icase)
             rnum = int(cl[0].split()[0])
             clock_d = float(cl[1].split()[0].replace("d", "e"))
             depth = float(cl[2].split()[0].replace("d", "e"))
@@ -513,11 +563,7 @@ class Tank:
             clock = clock_d * Ts
             cut_lo_n, cut_hi_n = cut_lo * Ts, cut_hi * Ts
             hinge = hinge_d / depth
-            rows = []
-            with open(base + ".dat") as f:
-                for ln in f:
-                    if ln.strip():
-                        rows.append([t for t in ln.replace(",", " ").split()])
+            rows = [ln.replace(",", " ").split() for ln in dat_lines if ln.strip()]
             harmo_a = np.array([int(r[0]) for r in rows])
             freq_a = np.array([float(r[1]) for r in rows])
             amp_a = np.array([float(r[2]) for r in rows])

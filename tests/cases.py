@@ -42,6 +42,20 @@ REF_IRREG_2D = dict(inp=default_input(xlen=120.0, ylen=100.0, h=5.0, icase=3, fi
                     n1=512, n2=1, n3=32, mHOS=3, p1=3, p2=1)
 
 
+REF_IRREG_3D = dict(inp=default_input(xlen=46.4, ylen=29.74, h=5.0, icase=31, file_name="CAT1__22", i_cut=0,
+                                      ibat=2, i_wmk=2, igeom=2, d_hinge=2.147, iramp=1, Tramp=3.0, T_stop=256.0,
+                                      iabsnb=1, xabsf=0.8, coeffabsf=1.0, toler=1e-4, f_out=10.0, idim=1),
+                    n1=256, n2=32, n3=16, mHOS=3, p1=3, p2=3)
+
+
+def write_ref_txt(fx, directory, name="CAT1__22"):
+    """The Edinburgh Designs .txt wave file of a reference fixture."""
+    import os
+    with open(os.path.join(directory, name + ".txt"), "w", encoding="latin-1") as f:
+        for ln in fx["txt"]:
+            f.write(str(ln) + "\n")
+
+
 def write_ref_wave_files(fx, directory, name="Hs4_Tp10"):
     """The .cfg/.dat wave files of a reference fixture (the layout file2wave
     reads, wave_def.f90:181-278), rewritten with the stored values."""

@@ -3,11 +3,12 @@
 python tests/golden/make_ref_benchmarks.py [REFERENCE_ROOT]
 
 Reads the probe records that the reference HOS-NWT wrote in
-Benchmark/Sloshing, Benchmark/Regular_3D and Benchmark/Irreg_2D
-(Ref_data/*.dat, 61d13.5 format) with their prob.inp probe positions (and
-Irreg_2D's wave file), and stores the numbers in ref_sloshing.npz,
-ref_regular3d.npz and ref_irreg2d.npz beside this script, together with the
-run configuration that each file's input echo states. The reference tree is only needed to regenerate the fixtures.
+Benchmark/Sloshing, Benchmark/Regular_3D, Benchmark/Irreg_2D and
+Benchmark/Irreg_3D (Ref_data/*.dat, 61d13.5 format) with their prob.inp
+probe positions (and the wave files of the irregular runs), and stores them
+in ref_sloshing.npz, ref_regular3d.npz, ref_irreg2d.npz and ref_irreg3d.npz
+beside this script, together with the run configuration that each file's
+input echo states. The reference tree is only needed to regenerate the fixtures.
 """
 import os
 import sys
@@ -63,4 +64,13 @@ if __name__ == "__main__":
                         probes=read_xy(os.path.join(d, "prob.inp")),
                         numerics=np.array([512, 1, 32, 3, 3, 1]), cfg=np.array(cfg),
                         components=np.array(comp))
-    print("sloshing", s.shape, "regular_3d", r.shape, "irreg_2d", g.shape, len(comp))
+    # Irreg_3D: an Edinburgh Designs .txt wave (OCEAN reader, icase 31),
+    # i_wmk = 2, M = 3 on 256 x 32 modes, 10 Hz output over 256 s
+    d = os.path.join(bench, "Irreg_3D")
+    g3 = read_probes(os.path.join(d, "Ref_data", "probes.dat"))
+    with open(os.path.join(d, "CAT1__22.txt"), encoding="latin-1") as f:
+        txt = f.read().splitlines()
+    np.savez_compressed(os.path.join(HERE, "ref_irreg3d.npz"), records=g3,
+                        probes=read_xy(os.path.join(d, "prob.inp")),
+                        numerics=np.array([256, 32, 16, 3, 3, 3]), txt=np.array(txt))
+    print("sloshing", s.shape, "regular_3d", r.shape, "irreg_2d", g.shape, len(comp), "irreg_3d", g3.shape)

@@ -1,8 +1,8 @@
 """The CUDA path against the reference's own result files.
 
-Benchmark/Sloshing, Benchmark/Regular_3D and Benchmark/Irreg_2D ship probe
-records written by the reference HOS-NWT (tests/golden/ref_*.npz, made by
-tests/golden/make_ref_benchmarks.py).  The whole runs (20 s, 40 s, 50 s) go
+Benchmark/Sloshing, Regular_3D, Irreg_2D and Irreg_3D ship probe records
+written by the reference HOS-NWT (tests/golden/ref_*.npz, made by
+tests/golden/make_ref_benchmarks.py).  The whole runs (20 s to 256 s) go
 through the C ABI; every probe value must agree with the reference's record
 within about half a unit of its last printed digit (5 significant digits).
 """
@@ -62,6 +62,19 @@ def test_irreg2d_matches_reference_record(lib, tmp_path):
     fx = _fixture("ref_irreg2d.npz")
     cases.write_ref_wave_files(fx, str(tmp_path))
     got = _records(cases.REF_IRREG_2D, fx, str(tmp_path))
+    ref = fx["records"]
+    assert got.shape == ref.shape, (got.shape, ref.shape)
+    assert np.all(np.abs(got[:, 0] - ref[:, 0]) <= 0.6 * _digit_unit(ref[:, 0]) + 1e-9)
+    err = np.abs(got[:, 1:] - ref[:, 1:]) / (_digit_unit(ref[:, 1:]) + 1e-14)
+    assert np.max(err) <= 0.6, (np.max(err), np.unravel_index(np.argmax(err), err.shape))
+
+
+def test_irreg3d_matches_reference_record(lib, tmp_path):
+    """Edinburgh Designs .txt wave (OCEAN reader, icase 31), second-order
+    wavemaker, M = 3, 256 x 32 modes, 2561 records over 256 s."""
+    fx = _fixture("ref_irreg3d.npz")
+    cases.write_ref_txt(fx, str(tmp_path))
+    got = _records(cases.REF_IRREG_3D, fx, str(tmp_path))
     ref = fx["records"]
     assert got.shape == ref.shape, (got.shape, ref.shape)
     assert np.all(np.abs(got[:, 0] - ref[:, 0]) <= 0.6 * _digit_unit(ref[:, 0]) + 1e-9)

@@ -194,3 +194,18 @@ def test_oracle_matches_reference_irreg2d_record(tmp_path):
     assert np.all(np.abs(got[:, 0] - ref[:, 0]) <= 0.6 * _digit_unit(ref[:, 0]) + 1e-9)
     err = np.abs(got[:, 1:] - ref[:, 1:]) / (_digit_unit(ref[:, 1:]) + 1e-14)
     assert np.max(err) <= 0.6, np.max(err)
+
+
+def test_oracle_matches_reference_irreg3d_record(tmp_path):
+    """Benchmark/Irreg_3D: an Edinburgh Designs .txt wave read by the OCEAN
+    reader (icase 31), i_wmk = 2, M = 3 on 256 x 32 modes; the first second
+    (11 records of the 2561) on the CPU."""
+    fx = _ref_fixture("ref_irreg3d.npz")
+    assert [int(v) for v in fx["numerics"]] == [256, 32, 16, 3, 3, 3]
+    cases.write_ref_txt(fx, str(tmp_path))
+    got = _run_records(cases.REF_IRREG_3D, fx, T_end=1.0, wave_dir=str(tmp_path))
+    ref = fx["records"][:len(got)]
+    assert len(got) == 11
+    assert np.all(np.abs(got[:, 0] - ref[:, 0]) <= 0.6 * _digit_unit(ref[:, 0]) + 1e-9)
+    err = np.abs(got[:, 1:] - ref[:, 1:]) / (_digit_unit(ref[:, 1:]) + 1e-14)
+    assert np.max(err) <= 0.6, np.max(err)
