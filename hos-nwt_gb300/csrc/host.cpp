@@ -601,8 +601,8 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
   if (P.n2 == 1) P.nd2 = 1;
   P.icase = in.icase; P.igeom = in.igeom; P.iramp = in.iramp; P.iabsnb = in.iabsnb;
   P.i_wmk = in.i_wmk; P.ibat = in.ibat;
-  if (P.icase != 1 && P.i_wmk != 1 && P.i_wmk != 2)
-    return fail(c, HOSNWT_ERR_UNSUPPORTED, "only first- and second-order wavemakers (i_wmk = 1, 2) are supported");
+  if (P.icase != 1 && (P.i_wmk < 1 || P.i_wmk > 3))
+    return fail(c, HOSNWT_ERR_UNSUPPORTED, "the wavemaker order i_wmk must be 1, 2 or 3");
   if (P.icase != 1 && P.igeom != 1 && P.igeom != 2)
     return fail(c, HOSNWT_ERR_UNSUPPORTED, "only flap/piston wavemakers (igeom 1, 2) are supported");
   // nondimensionalisation (HOS-NWT.f90:99-119)
@@ -761,8 +761,8 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
   d.kycsh = upload(c, kycsh);
   d.kxcsh = upload(c, kxcsh);
   d.ext = upload(c, extension_matrix(P.n3, n3a, P.l_add, P.delz));
-  if (P.i_wmk == 2) {
-    // second-order wavemaker (d1st_for_2nd, solveHOS_SWEET_2): free-surface
+  if (P.i_wmk >= 2) {
+    // second- and third-order wavemaker (d1st_for_2nd, SWEET_2, SWEET_3): free-surface
     // modes on the wavemaker (HOS-NWT.f90:343-355), [i1 + n1 (i2 + n2 i3)]
     const int n3 = P.n3;
     std::vector<double> kx2c((size_t)n1 * n2 * n3), kyc(kx2c.size()), ks(kx2c.size());

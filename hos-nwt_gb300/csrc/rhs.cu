@@ -829,13 +829,100 @@ __global__ void k_sweet2_fs(Sweet2Fs g, const double* __restrict__ nu, double ia
             iabsnb * nu[i] * deta;
 }
 
+// the wavemaker-grid terms of wmk_3rdorder before their F2S_add
+// (resol_wmkr.f90:962-981): first order -a k_add^2 kthk, -da k_add^2 kthk,
+// a ky kthk, da ky kthk, a kx_add kthk, da kx_add kthk; second order
+// a k_add^2, da k_add^2, -a ky, -da ky, -a kx_add, -da kx_add
+struct AddProd3Out {
+  double* p[12];
+};
+__global__ void k_add_prod3(const double* __restrict__ a1, const double* __restrict__ da1,
+                            const double* __restrict__ a2, const double* __restrict__ da2,
+                            const double* __restrict__ k_add, const double* __restrict__ kthk,
+                            const double* __restrict__ kx_add, const double* __restrict__ ky, int n3a, long long n,
+                            AddProd3Out o) {
+  pdl_wait();
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int i3 = (int)(i % n3a), i2 = (int)(i / n3a);
+  const double ka = k_add[i], kt = kthk[i], y = ky[i2], x = kx_add[i3];
+  const double aa = a1[i], dd = da1[i], bb = a2[i], ee = da2[i];
+  o.p[0][i] = -aa * ka * ka * kt;
+  o.p[1][i] = -dd * ka * ka * kt;
+  o.p[2][i] = aa * y * kt;
+  o.p[3][i] = dd * y * kt;
+  o.p[4][i] = aa * x * kt;
+  o.p[5][i] = dd * x * kt;
+  o.p[6][i] = bb * ka * ka;
+  o.p[7][i] = ee * ka * ka;
+  o.p[8][i] = -bb * y;
+  o.p[9][i] = -ee * y;
+  o.p[10][i] = -bb * x;
+  o.p[11][i] = -ee * x;
+}
+
+// solveHOS_SWEET_3's wavemaker condition (resol_wmkr.f90:370-397), no
+// free-wave correction: one block per i2 sums the frequencies, then rows
+// i3 < n3 of bc3.  X1: the six first-order fields (xxx, xxxt, xy, xyt, xz,
+// xzt; F2S_add, n3_add x n2); X2: the six second-order fields (xx, xxt, y,
+// yt, z, zt) as free-surface part (n3 x n2) plus F2S_add part.
+struct Sweet3Wmk {
+  const double* x1[6];
+  const double* wf[6];
+  const double* wa[6];
+};
+__global__ void k_sweet3_wmk(const double* __restrict__ pos_re, const double* __restrict__ pos_im,
+                             const double* __restrict__ dy_re, const double* __restrict__ dy_im,
+                             const double* __restrict__ freq, const double* __restrict__ eiwt,
+                             const double* __restrict__ gzed, const double* __restrict__ dgzed,
+                             const double* __restrict__ sc, int nf, int n2, int n3, int n3a, Sweet3Wmk W,
+                             double* bc3) {
+  pdl_wait();
+  const int i2 = blockIdx.x;
+  const double a = sc[SC_ALPHA], at = sc[SC_ALPHAT];
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int n = threadIdx.x; n < nf; n += blockDim.x) {
+    const double w = 6.283185307179586476925286766559005768394 * freq[n];
+    const double c = eiwt[2 * n], sn = eiwt[2 * n + 1];
+    const long long q = i2 + (long long)n2 * n;
+    const double pr = pos_re[q], pi = pos_im[q], yr = dy_re[q], yi = dy_im[q];
+    s[0] += pr * c - pi * sn;
+    s[1] += -(pr * sn + pi * c) * w;
+    s[2] += yr * c - yi * sn;
+    s[3] += -(yr * sn + yi * c) * w;
+  }
+  __shared__ double S[4];
+  for (int q = 0; q < 4; ++q) {
+    const double v = block_reduce<0>(s[q]);
+    if (threadIdx.x == 0) S[q] = v;
+    __syncthreads();
+  }
+  for (int i3 = threadIdx.x; i3 < n3; i3 += blockDim.x) {
+    const double g = gzed[i3], dg = dgzed[i3];
+    const double pos = g * S[0], dpos = g * S[1], dy = g * S[2], dyt = g * S[3], dz = dg * S[0], dzt = dg * S[1];
+    const long long wi = i3 + (long long)n3 * i2, ai = i3 + (long long)n3a * i2;
+    const double xxx = W.x1[0][ai], xxxt = W.x1[1][ai], xy = W.x1[2][ai], xyt = W.x1[3][ai];
+    const double xz = W.x1[4][ai], xzt = W.x1[5][ai];
+    const double xx2 = W.wf[0][wi] + W.wa[0][ai], xxt2 = W.wf[1][wi] + W.wa[1][ai];
+    const double y2 = W.wf[2][wi] + W.wa[2][ai], yt2 = W.wf[3][wi] + W.wa[3][ai];
+    const double z2 = W.wf[4][wi] + W.wa[4][ai], zt2 = W.wf[5][wi] + W.wa[5][ai];
+    const double t_a = -a * (-dpos * xx2 - pos * xxt2 + dyt * y2 + dy * yt2 + dzt * z2 + dz * zt2);
+    const double t_at = -at * (-pos * xx2 + dy * y2 + dz * z2);
+    const double t_a2 = -(a * a) * (-(pos * pos) / 2.0 * xxxt - dpos * pos * xxx + dpos * dy * xy + pos * dy * xyt +
+                                    pos * dyt * xy + dpos * dz * xz + pos * dz * xzt + pos * dzt * xz);
+    const double t_aat = -a * at * (-(pos * pos) * xxx + 2.0 * pos * dy * xy + 2.0 * pos * dz * xz);
+    bc3[ai] = t_a + t_at + t_a2 + t_aat;
+  }
+}
+
 // phiadd_SL on a 1-D tank (n2 = 1): the i3 contraction at z = eta.
 // kx_add(i3) = (2 i3 + 1) pi / 4, so cos/sin(kx_add(i3) (eta + 1)) follow
 // from one sincos per chunk start and rotations by 2 phi, phi = pi (eta+1)/4.
 __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
     const double* __restrict__ eta, const double* __restrict__ a1, const double* __restrict__ a2,
     const double* __restrict__ a3, const double* __restrict__ da, const double* __restrict__ da2,
-    const double* __restrict__ kx_add, const double* __restrict__ csh, const double* __restrict__ ksh,
+    const double* __restrict__ da3, const double* __restrict__ kx_add, const double* __restrict__ csh,
+    const double* __restrict__ ksh,
     const double* __restrict__ kxcsh, int n1, int n3a, double* phix, double* phiy, double* phiz, double* phit,
     double* phi) {
   pdl_wait();
@@ -845,7 +932,8 @@ __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
   const int i1 = blockIdx.x * kCx + tx;
   for (int t = threadIdx.x; t < n3a; t += blockDim.x) {
     sa[t] = a1[t] + a2[t] + a3[t];
-    sd[t] = da2 ? da[t] + da2[t] : da[t];  // da_add_1 + da_add_2 (resol_HOS.f90:490)
+    // da_add_1 + da_add_2 + da_add_3 (resol_HOS.f90:490)
+    sd[t] = da3 ? da[t] + da2[t] + da3[t] : (da2 ? da[t] + da2[t] : da[t]);
   }
   __syncthreads();
   const int ch = (n3a + kCy - 1) / kCy;
@@ -888,7 +976,8 @@ __global__ void __launch_bounds__(kCx * kCy) k_phiadd_sl_1d(
 // phiadd_SL (3-D): products Q_q(i1, i3, j2) = a(i3, j2) * T_q(i1, i3, j2)
 __global__ void k_phiadd_q(const double* __restrict__ a1, const double* __restrict__ a2,
                            const double* __restrict__ a3, const double* __restrict__ da,
-                           const double* __restrict__ da2, const double* __restrict__ csh,
+                           const double* __restrict__ da2, const double* __restrict__ da3,
+                           const double* __restrict__ csh,
                            const double* __restrict__ ksh,
                            const double* __restrict__ kycsh, const double* __restrict__ kxcsh,
                            int n1, int n2, int n3a, double* Qt, double* Qx, double* Qy, double* Qz,
@@ -899,7 +988,7 @@ __global__ void k_phiadd_q(const double* __restrict__ a1, const double* __restri
   if (o >= n) return;
   const long long r = o / n1;  // i3 + n3a * j2
   const double a = a1[r] + a2[r] + a3[r];
-  Qt[o] = (da2 ? da[r] + da2[r] : da[r]) * csh[o];
+  Qt[o] = (da3 ? da[r] + da2[r] + da3[r] : (da2 ? da[r] + da2[r] : da[r])) * csh[o];
   Qx[o] = a * ksh[o];
   Qy[o] = a * kycsh[o];
   Qz[o] = a * kxcsh[o];
@@ -1266,6 +1355,11 @@ enum {
   W2_WF = 58,   // the same in space (6)
   W2_PHIX = 64, W2_PHIY, W2_ETAX, W2_ETAY, W2_PHIZT, W2_PHIXX, W2_PHIZZ, W2_PZ,
   W2_BC2 = 72, W2_P2T, W2_P2Z, W2_P2TM, W2_P2ZM, W2_PZ2S, W2_RHS2, W2_A2K,
+  W2_AP3 = 80,   // wavemaker-grid products of wmk_3rdorder (12)
+  W2_WA3 = 92,   // their F2S_add (12)
+  W2_WFM2 = 104, // second-order free-surface modes on the wavemaker, y-modal (6)
+  W2_WF2 = 110,  // the same in space (6)
+  W2_BC3 = 116,
   W2_COUNT
 };
 static_assert(W2_COUNT <= Dev::kW2, "second-order work fields");
@@ -1375,6 +1469,56 @@ void enqueue_sweet2(Ctx& c, Enq& W, const double* y, double* k) {
   W.xf({W.S2F_N(w[W2_RHS2], k + L.off[S_A2ND])});
 }
 
+// wmk_3rdorder and solveHOS_SWEET_3 (resol_wmkr.f90:338-437, 942-1115) on
+// the wavemaker stream after enqueue_sweet2: fills the slope of a_add_3.
+void enqueue_sweet3(Ctx& c, Enq& W, const double* y, double* k) {
+  const Params& P = c.P;
+  const Dev& d = c.d;
+  const StateLayout& L = c.L;
+  const int n1 = P.n1, n2 = P.n2, n3 = P.n3, n3a = P.n3a;
+  const long long nA = (long long)n3a * n2;
+  cudaStream_t sw = W.st;
+  double* const* w = d.w2;
+  AddProd3Out ap{};
+  for (int q = 0; q < 12; ++q) ap.p[q] = w[W2_AP3 + q];
+  W.ew(k_add_prod3, nA, y + L.off[S_AADD1], (const double*)(k + L.off[S_AADD1]), y + L.off[S_AADD2],
+       (const double*)(k + L.off[S_AADD2]), (const double*)d.k_add, (const double*)d.k_add_thk,
+       (const double*)d.kx_add, (const double*)d.ky, n3a, nA, ap);
+  {
+    std::vector<XfReq> rq;
+    for (int q = 0; q < 12; ++q) {
+      const int kind = q % 6;  // cos,cos (0,1) cos,sin (2,3) sin,cos (4,5)
+      rq.push_back(W.R(GRID_ADD, -1, kind >= 4 ? 1 : 0, (kind == 2 || kind == 3) ? 1 : 0, w[W2_AP3 + q], n3a, n3a,
+                       n2, w[W2_WA3 + q], n3a, n3a, n2));
+    }
+    W.xf(rq);
+  }
+  WmkFsOut wo{};
+  for (int q = 0; q < 6; ++q) wo.w[q] = n2 == 1 ? w[W2_WF2 + q] : w[W2_WFM2 + q];
+  launch_pdl(k_wmk_from_fs, dim3(n3, n2), dim3(128), 0, sw, y + L.off[S_A2ND], (const double*)(k + L.off[S_A2ND]),
+             (const double*)d.kx2cshx, (const double*)d.kycshx, (const double*)d.kshx, n1, n2, n3, wo);
+  if (n2 != 1)
+    for (int q = 0; q < 6; ++q)
+      launch_y_f2s(W.tb, w[W2_WFM2 + q], n3, n3, w[W2_WF2 + q], n3, (q == 2 || q == 3) ? 1 : 0, sw);
+  Sweet3Wmk sv{};
+  for (int q = 0; q < 6; ++q) {
+    sv.x1[q] = w[W2_WA3 + q];
+    sv.wf[q] = w[W2_WF2 + q];
+    sv.wa[q] = w[W2_WA3 + 6 + q];
+  }
+  launch_pdl(k_sweet3_wmk, dim3(n2), dim3(128), 0, sw, (const double*)d.pos_re, (const double*)d.pos_im,
+             (const double*)d.dposdy_re, (const double*)d.dposdy_im, (const double*)d.freq_w,
+             (const double*)d.eiwt, (const double*)d.gzed, (const double*)d.dgzed, (const double*)d.sc, c.nf, n2,
+             n3, n3a, sv, w[W2_BC3]);
+  {
+    const int tot = (n3a - n3) * n2;
+    launch_pdl(k_extend, dim3(nblk(tot)), dim3(kEW), 0, sw, w[W2_BC3], (double*)nullptr, d.ext, n2, n3, n3a);
+  }
+  double* kA3 = k + L.off[S_AADD3];
+  W.xf({W.R(GRID_ADD, 1, 0, 0, w[W2_BC3], n3a, n3a, n2, kA3, n3a, n3a, n2)});
+  W.ew(k_div, nA, kA3, (double*)nullptr, (const double*)d.k_add_thk, nA);
+}
+
 void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t st) {
   Enq E(c, st);
   const Params& P = c.P;
@@ -1401,7 +1545,8 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   //    main stream before assembly.
   cudaStream_t sw = c.st2;
   Enq W(c, sw, c.tb2, d.xtmp2, nullptr, 0);
-  const bool wmk2 = has_wavemaker(P) && P.i_wmk == 2;
+  const bool wmk2 = has_wavemaker(P) && P.i_wmk >= 2;
+  const bool wmk3 = has_wavemaker(P) && P.i_wmk == 3;
   cudaEventRecord(c.ev_fork, st);
   cudaStreamWaitEvent(sw, c.ev_fork, 0);
   double* kA1 = k + L.off[S_AADD1];
@@ -1455,20 +1600,20 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
          (const double*)d.nu, (double)P.iabsnb, d.rhs1, kEta1, nN);
     W.xf({W.S2F_N(d.rhs1, kA1st)});
     if (wmk2) enqueue_sweet2(c, W, y, k);
+    if (wmk3) enqueue_sweet3(c, W, y, k);
   } else {
     cudaMemsetAsync(kA1, 0, sizeof(double) * nA, sw);
     cudaMemsetAsync(kAR, 0, sizeof(double) * nA, sw);
     cudaMemsetAsync(kA1st, 0, sizeof(double) * nN, sw);
     cudaMemsetAsync(kEta1, 0, sizeof(double) * nN, sw);
   }
-  // the third-order slope stays zero (i_wmk <= 2); so do the second-order
-  // slopes without a second-order wavemaker
+  // the second- and third-order slopes stay zero below their wavemaker order
   if (!wmk2) {
     cudaMemsetAsync(k + L.off[S_AADD2], 0, sizeof(double) * nA, sw);
     cudaMemsetAsync(k + L.off[S_A2ND], 0, sizeof(double) * nN, sw);
     cudaMemsetAsync(k + L.off[S_ETA2ND], 0, sizeof(double) * nN, sw);
   }
-  cudaMemsetAsync(k + L.off[S_AADD3], 0, sizeof(double) * nA, sw);
+  if (!wmk3) cudaMemsetAsync(k + L.off[S_AADD3], 0, sizeof(double) * nA, sw);
 
   // 2. transform batch A: eta in space, eta / eta_x / eta_y / phis_x / phis_y on
   //    the big grid (phisxy_etaxy) and the order-1 HOS terms F2S_big(a1 kth_ext(j))
@@ -1499,17 +1644,18 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
   //     gradients of phi_add on the big grid (resol_HOS.f90:534-555)
   if (has_wavemaker(P)) {
     const double* kA2 = wmk2 ? k + L.off[S_AADD2] : nullptr;
+    const double* kA3 = wmk3 ? k + L.off[S_AADD3] : nullptr;
     cudaStreamWaitEvent(sw, c.ev_eta, 0);
     const double* aA1 = y + L.off[S_AADD1];
     const double* aA2 = y + L.off[S_AADD2];
     const double* aA3 = y + L.off[S_AADD3];
     if (n2 == 1) {
       launch_pdl(k_phiadd_sl_1d, dim3((n1 + kCx - 1) / kCx), dim3(kCx * kCy), 0, sw, d.eta_sp, aA1, aA2,
-                 aA3, (const double*)kA1, kA2, d.kx_add, d.csh, d.ksh, d.kxcsh, n1, P.n3a, d.phix_add,
+                 aA3, (const double*)kA1, kA2, kA3, d.kx_add, d.csh, d.ksh, d.kxcsh, n1, P.n3a, d.phix_add,
                  d.phiy_add, d.phiz_add, d.phit_add, d.phi_add);
     } else {
       const long long nq = (long long)n1 * P.n3a * n2;
-      W.ew(k_phiadd_q, nq, aA1, aA2, aA3, (const double*)kA1, kA2, (const double*)d.csh,
+      W.ew(k_phiadd_q, nq, aA1, aA2, aA3, (const double*)kA1, kA2, kA3, (const double*)d.csh,
            (const double*)d.ksh, (const double*)d.kycsh, (const double*)d.kxcsh, n1, n2, P.n3a,
            d.Q[0], d.Q[1], d.Q[2], d.Q[3], d.Q[4]);
       const int lines = n1 * P.n3a;

@@ -85,7 +85,7 @@ struct Dev {
   double *kx2cshx = nullptr, *kycshx = nullptr, *kshx = nullptr;  // [i1 + n1 (i2 + n2 i3)], i3 < n3
   double *k_add = nullptr;                                         // n3_add x n2
   double *dnux = nullptr, *dgzed = nullptr, *dposdy_re = nullptr, *dposdy_im = nullptr;
-  static constexpr int kW2 = 80;
+  static constexpr int kW2 = 120;
   double* w2[kW2] = {};  // work fields of the second order, max(n1 n2, n3_add n2) each
   // 3-D phiadd_SL workspace (n1 * n3a * n2 each)
   double *Q[5] = {}, *B[5] = {};

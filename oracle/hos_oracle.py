@@ -426,8 +426,8 @@ class Tank:
                 raise ValueError(f"forbidden value of {name}: {v}")
         if self.p1 > self.M or self.p2 > self.M:
             raise ValueError("p1/p2 higher than M")
-        if self.inp["i_wmk"] not in (1, 2) and self.inp["icase"] != 1:
-            raise NotImplementedError("first- and second-order wavemakers (i_wmk = 1, 2) only")
+        if self.inp["i_wmk"] not in (1, 2, 3) and self.inp["icase"] != 1:
+            raise NotImplementedError("wavemaker orders i_wmk = 1, 2, 3 only")
 
     # ------------------------------------------------------------------ setup
     def _nondim(self):
@@ -1039,10 +1039,15 @@ class Tank:
             self.a1st, self.eta1st, self.a1st_add, self.time)
         self.a_add_ramp = self.a1st_add.copy()
         self.da1st_add = da_add
-        if self.inp["i_wmk"] == 2:
-            _, _, da_add_2, _ = self.solveHOS_SWEET_2(self.a2nd, self.eta2nd, self.eta1st, self.a2nd_add,
-                                                      self.time)
-            da_add = da_add + da_add_2
+        if self.inp["i_wmk"] >= 2:
+            da2nd, _, da_add_2, _ = self.solveHOS_SWEET_2(self.a2nd, self.eta2nd, self.eta1st, self.a2nd_add,
+                                                          self.time)
+            if self.inp["i_wmk"] == 3:
+                da_add_3 = self.solveHOS_SWEET_3(self.a2nd, da2nd, self.a1st_add, da_add, self.a2nd_add,
+                                                 da_add_2, self.time)
+                da_add = da_add + da_add_2 + da_add_3
+            else:
+                da_add = da_add + da_add_2
         out = self.phiadd_SL(self.a1st_add + self.a2nd_add + self.a3rd_add, da_add, self.eta)
         self.phi_add = out[0]
 
@@ -1163,6 +1168,45 @@ class Tank:
         dzt = dg * (rz * (1j * w)[None, :]).sum(axis=1).real[None, :]
         return dy, dyt, dz, dzt
 
+    def solveHOS_SWEET_3(self, a2nd, da2nd, a_add_1, da_add_1, a_add_2, da_add_2, time):
+        """solveHOS_SWEET_3 (resol_wmkr.f90:338-437) with wmk_3rdorder
+        (resol_wmkr.f90:942-1115), no free-wave correction (ifree = 0):
+        the third-order wavemaker condition from the first- and second-order
+        potentials at the paddle.  Returns da_add_3.  (phiadd_3rd's fields
+        are not read by the right-hand side.)"""
+        F = self.fourier
+        n3 = self.n3
+        ka, kthk = self.k_add, self.k_add_thk_add
+        ky = self.ky[None, :]
+        kxa = self.kx_add[:, None]
+        xxx = F.F2S_add(-a_add_1 * ka * ka * kthk, "cos", "cos")[:n3]
+        xxxt = F.F2S_add(-da_add_1 * ka * ka * kthk, "cos", "cos")[:n3]
+        xy = F.F2S_add(a_add_1 * ky * kthk, "cos", "sin")[:n3]
+        xyt = F.F2S_add(da_add_1 * ky * kthk, "cos", "sin")[:n3]
+        xz = F.F2S_add(a_add_1 * kxa * kthk, "sin", "cos")[:n3]
+        xzt = F.F2S_add(da_add_1 * kxa * kthk, "sin", "cos")[:n3]
+
+        def onwmk(a, tab, sign):
+            return sign * np.einsum("ij,ijk->kj", a, tab)
+        xx2 = F.F2S_y(onwmk(a2nd, self.kx2cshx_add, -1.0), "cos") + F.F2S_add(a_add_2 * ka * ka, "cos", "cos")[:n3]
+        xxt2 = F.F2S_y(onwmk(da2nd, self.kx2cshx_add, -1.0), "cos") + F.F2S_add(da_add_2 * ka * ka, "cos", "cos")[:n3]
+        y2 = F.F2S_y(onwmk(a2nd, self.kycshx_add, -1.0), "sin") + F.F2S_add(-a_add_2 * ky, "cos", "sin")[:n3]
+        yt2 = F.F2S_y(onwmk(da2nd, self.kycshx_add, -1.0), "sin") + F.F2S_add(-da_add_2 * ky, "cos", "sin")[:n3]
+        z2 = F.F2S_y(onwmk(a2nd, self.kshx_add, 1.0), "cos") + F.F2S_add(-a_add_2 * kxa, "sin", "cos")[:n3]
+        zt2 = F.F2S_y(onwmk(da2nd, self.kshx_add, 1.0), "cos") + F.F2S_add(-da_add_2 * kxa, "sin", "cos")[:n3]
+        alpha, alphat, _ = self._alpha
+        pos, dpos, _ = self._pos
+        dy, dyt, dz, dzt = self._dpos_1st(time)
+        a_alpha = -alpha * (-dpos * xx2 - pos * xxt2 + dyt * y2 + dy * yt2 + dzt * z2 + dz * zt2)
+        a_alphat = -alphat * (-pos * xx2 + dy * y2 + dz * z2)
+        a_alpha2 = -alpha ** 2 * (-(pos ** 2) / 2.0 * xxxt - dpos * pos * xxx + dpos * dy * xy + pos * dy * xyt
+                                  + pos * dyt * xy + dpos * dz * xz + pos * dz * xzt + pos * dzt * xz)
+        a_aat = -alpha * alphat * (-pos ** 2 * xxx + 2.0 * pos * dy * xy + 2.0 * pos * dz * xz)
+        dd = np.zeros((self.n3_add, self.n2))
+        dd[:n3] = a_alpha + a_alphat + a_alpha2 + a_aat
+        dd = self.match_surface_wmk(dd)
+        return F.S2F_add(dd, "cos", "cos") / kthk
+
     def solveHOS_SWEET_2(self, a2nd, eta2nd, eta1st, a_add_2, time):
         """solveHOS_SWEET_2 (resol_wmkr.f90:219-329) with phiadd_2nd
         (resol_wmkr.f90:802-864), no free-wave correction (ifree = 0).
@@ -1271,11 +1315,16 @@ class Tank:
                 state["a1st"], state["eta1st"], state["a_add_1"], time)
             a_tot = state["a_add_1"] + state["a_add_2"] + state["a_add_3"]
             da_tot = d_add1
-            if self.inp["i_wmk"] == 2:
+            if self.inp["i_wmk"] >= 2:
                 da2, deta2, d_add2, _ = self.solveHOS_SWEET_2(
                     state["a2nd"], state["eta2nd"], state["eta1st"], state["a_add_2"], time)
                 da_tot = d_add1 + d_add2
                 out.update(a2nd=da2, eta2nd=deta2, a_add_2=d_add2)
+                if self.inp["i_wmk"] == 3:
+                    d_add3 = self.solveHOS_SWEET_3(state["a2nd"], da2, state["a_add_1"], d_add1,
+                                                   state["a_add_2"], d_add2, time)
+                    da_tot = d_add1 + d_add2 + d_add3
+                    out.update(a_add_3=d_add3)
             phi_add, phix_add, phiy_add, phiz_add, phit_add = self.phiadd_SL(a_tot, da_tot, etark)
             out.update(a1st=da1, eta1st=deta1, a_add_1=d_add1, a_add_ramp=d_ramp)
         else:
@@ -1287,7 +1336,7 @@ class Tank:
         out.setdefault("a_add_2", za.copy())
         out.setdefault("a2nd", np.zeros((n1, n2)))
         out.setdefault("eta2nd", np.zeros((n1, n2)))
-        out.update(a_add_3=za.copy())
+        out.setdefault("a_add_3", za.copy())
         self.phi_add = phi_add
         # grad eta . grad phi_add (resol_HOS.f90:534-555)
         self._tick(9)

@@ -76,5 +76,9 @@ REG_3D_W2 = dict(inp=default_input(T_stop=20.0, amp_mono=0.02, nu_mono=0.7, thet
                                    f_out=4.0, ylen=20.0, i_wmk=2, iramp=1, Tramp=1.0),
                  n1=33, n2=17, n3=9, mHOS=3, p1=3, p2=3)
 
-ALL = {"reg1d": REG_1D, "reg1d_w2": REG_1D_W2, "reg3d_w2": REG_3D_W2, "reg1d_m5": REG_1D_M5, "reg3d": REG_3D, "slosh": SLOSH, "jonswap1d": JONSWAP_1D,
+REG_1D_W3 = dict(REG_1D_W2, inp=dict(REG_1D_W2["inp"], i_wmk=3))
+REG_3D_W3 = dict(REG_3D_W2, inp=dict(REG_3D_W2["inp"], i_wmk=3))
+
+ALL = {"reg1d": REG_1D, "reg1d_w2": REG_1D_W2, "reg3d_w2": REG_3D_W2, "reg1d_w3": REG_1D_W3,
+       "reg3d_w3": REG_3D_W3, "reg1d_m5": REG_1D_M5, "reg3d": REG_3D, "slosh": SLOSH, "jonswap1d": JONSWAP_1D,
        "wide3d": WIDE_3D}

@@ -69,15 +69,17 @@ def _state(o, rng, amp=1e-3):
              a_add_3=np.zeros((n3a, n2)), a1st=amp * rng.standard_normal((n1, n2)) * decay,
              eta1st=amp * rng.standard_normal((n1, n2)) * decay, a2nd=np.zeros((n1, n2)),
              eta2nd=np.zeros((n1, n2)))
-    if o.inp["i_wmk"] == 2:
+    if o.inp["i_wmk"] >= 2:
         y["a_add_2"] = 0.1 * amp * rng.standard_normal((n3a, n2)) * da
         y["a2nd"] = 0.1 * amp * rng.standard_normal((n1, n2)) * decay
         y["eta2nd"] = 0.1 * amp * rng.standard_normal((n1, n2)) * decay
+    if o.inp["i_wmk"] == 3:
+        y["a_add_3"] = 0.01 * amp * rng.standard_normal((n3a, n2)) * da
     return y
 
 
 @pytest.mark.parametrize("name", ["reg1d", "reg1d_m5", "reg3d", "slosh", "jonswap1d", "wide3d", "reg1d_w2",
-                                  "reg3d_w2"])
+                                  "reg3d_w2", "reg1d_w3", "reg3d_w3"])
 def test_solveHOS2(lib, name):
     case = cases.ALL[name]
     g = _gtank(case)
@@ -96,7 +98,7 @@ def test_solveHOS2(lib, name):
             assert _rel(arr, r) < 1e-10, (key, _rel(arr, r))
 
 
-@pytest.mark.parametrize("name", ["reg1d", "reg3d", "slosh", "reg1d_w2", "reg3d_w2"])
+@pytest.mark.parametrize("name", ["reg1d", "reg3d", "slosh", "reg1d_w2", "reg3d_w2", "reg1d_w3", "reg3d_w3"])
 def test_runge4_adapt2(lib, name):
     case = cases.ALL[name]
     o = _otank(case)
@@ -125,7 +127,7 @@ def _zero_state(o):
     return [np.zeros((n1, n2)), np.zeros((n1, n2))] + [np.zeros((n3a, n2))] * 4 + [np.zeros((n1, n2))] * 4
 
 
-@pytest.mark.parametrize("name", ["reg1d", "jonswap1d", "reg3d", "reg1d_w2", "reg3d_w2"])
+@pytest.mark.parametrize("name", ["reg1d", "jonswap1d", "reg3d", "reg1d_w2", "reg3d_w2", "reg1d_w3", "reg3d_w3"])
 def test_time_loop_probes(lib, name):
     case = dict(cases.ALL[name])
     inp = dict(case["inp"])
