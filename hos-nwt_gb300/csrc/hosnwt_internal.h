@@ -217,6 +217,12 @@ struct Tables {
   const double* q_add;
 };
 
+// FP64 FMAs of the transform passes launched from this host thread since
+// the counter was last reset (the algorithm's own count: terms times
+// outputs, as the launch helpers pick them).  The host reads it around the
+// capture of a step graph.
+extern thread_local double g_xform_fmas;
+
 // FP64 FMA throughput of the current device in GFLOP/s.
 double measure_fp64_peak_gflops();
 

@@ -968,7 +968,9 @@ static int build_step_graph(Ctx& c) {
   if (cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return cuda_check(c, "begin capture");
   cudaMemcpyAsync(c.d.sc + SC_T0, c.d.host_sc + SC_T0, 2 * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  const double f0 = g_xform_fmas;
   enqueue_step(c, c.st);
+  c.fmas_per_step = g_xform_fmas - f0;
   if (cudaStreamEndCapture(c.st, &g) != cudaSuccess) return cuda_check(c, "end capture");
   size_t nn = 0;
   cudaGraphGetNodes(g, nullptr, &nn);
@@ -1054,6 +1056,7 @@ extern "C" int hosnwt_get_info(const hosnwt_ctx* h, hosnwt_info* info) {
   info->n_rhs = c.n_rhs;
   info->kernels_per_step = c.kernels_per_step;
   info->device_ms = c.dev_ms;
+  info->fmas_per_step = c.fmas_per_step;
   return HOSNWT_OK;
 }
 

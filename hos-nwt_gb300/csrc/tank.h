@@ -135,6 +135,7 @@ struct Ctx {
   int endramp = 0;
   long long n_rhs = 0;
   int kernels_per_step = 0;
+  double fmas_per_step = 0.0;     // FP64 FMAs of the transforms in one step graph
   double dev_ms = 0.0;            // device time of steps and accepts (CUDA events)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int nparts = 0;

@@ -513,8 +513,9 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
 //   sin-kind: y_k = sum_j2 [cos(pi j2 k/D) S(j2,k) + sin(pi j2 k/D) C(j2,k)]
 // with C, S = sum_j1 w_j x_j cos / sin(pi j1 k / A), which depend on k only
 // through k mod 2A (C even, S odd about A).  Pass 1 computes C, S for
-// k' = 0..A; pass 2 combines them.  Work: 2 (A+1) nin + 2 B nout FMAs
-// instead of about nin * nout / 2 for the direct sum.
+// k' = 0..A; pass 2 combines them.  Work: about (A+2) nin + 2 B nout FMAs
+// (B nout when outputs pair up, see pass 2) instead of about nin * nout / 2
+// for the direct sum.
 //
 // Both passes first issue all of their global loads (inputs, partial sums
 // and twiddles staged in shared memory), then run FMA loops over shared
@@ -545,99 +546,122 @@ __device__ __forceinline__ double ld_cluster(const double* local, unsigned rank)
   return v;
 }
 
-// pass 1: cluster = (job, line, group of kpc consecutive k'); CTA r of the
-// cluster sums j1 in its slice of [0, K).  Threads own (k', part, j2) items
-// with j2 fastest: staged inputs are read without bank conflicts and the j1
-// twiddles are broadcast.
+// pass 1: cluster = (job, line, group of kpc consecutive k' <= A/2); CTA r
+// of the cluster sums j1 in its slice of [0, K).  The even and odd j1 terms
+// are summed apart: cos / sin(pi j1 (A - k') / A) = +-(-1)^j1 cos / sin(pi
+// j1 k' / A), so the same four sums give C, S at k' and at A - k' and half
+// of the k' are computed.  Threads own (k', part, j2) items with j2
+// fastest: staged inputs are read without bank conflicts and the j1
+// twiddles are broadcast.  Slices hold an even number of j1 (Kc2), so a
+// local index has the parity of its global j1.
+__host__ __device__ inline int p1_half(int A) { return A / 2; }
+__host__ __device__ inline int p1_slice(int K, int ncl) { return (((K + ncl - 1) / ncl) + 1) & ~1; }
+
 template <int NJ>
 __global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatchT<NJ> b, int kpc, int ncl) {
   extern __shared__ double sm1[];
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const AxisJob& J = b.job[jb];
-  const int A = J.A, B = J.B, D = J.D, D4 = 4 * D;
-  const int ngrp = (A + 1 + kpc - 1) / kpc;
+  const int A = J.A, B = J.B, D = J.D, D4 = 4 * D, H = p1_half(A);
+  const int ngrp = (H + 1 + kpc - 1) / kpc;
   const int local = (blockIdx.x - b.start[jb]) / ncl;
   const unsigned rank = ncl > 1 ? cluster_rank() : 0u;
   const int line = local / ngrp;
   const int kp0 = (local - line * ngrp) * kpc;
-  const int nkp = min(kpc, A + 1 - kp0);
+  const int nkp = min(kpc, H + 1 - kp0);
   const int j_end = min(J.jhi, J.nin);  // terms j in [jlo, j_end)
   const int K = (j_end + B - 1) / B;
-  const int Kc = (K + ncl - 1) / ncl;
+  const int Kc = p1_slice(K, ncl);
   const int ja1 = min(K, (int)rank * Kc), Kl = min(K, ja1 + Kc) - ja1;
-  double* fin = sm1;                // kpc * B (C, S) of this CTA's slice
-  double* xs = fin + 2 * kpc * B;   // Kl * B weighted inputs, zero outside the sum
+  const int Klp = (Kl + 1) & ~1;    // padded to whole (even, odd) pairs
+  double* fin = sm1;                // kpc * B (C, S, C', S') of this CTA's slice
+  double* xs = fin + 4 * kpc * B;   // Kc * B weighted inputs, zero outside the sum
   double* tc = xs + Kc * B;         // kpc * Kc cos(pi j1 k' / A)
   double* ts = tc + kpc * Kc;       // kpc * Kc sin(pi j1 k' / A)
   double* red = ts + kpc * Kc;      // partial sums of the items
   const double* __restrict__ x = J.in + (long long)line * J.in_sl;
   const double* __restrict__ wr = J.win ? J.win + (long long)line * J.win_sl : nullptr;
   auto stage_twiddles = [&]() {
-    for (int t = threadIdx.x; t < nkp * Kl; t += kP1Threads) {
-      const int kpl = t / Kl, j1 = ja1 + t - kpl * Kl;
-      // pi j1 k' / A = pi (2 B j1 k') / (2 D); both factors below 4D
-      const unsigned step = (2u * (unsigned)B * (unsigned)(kp0 + kpl)) % (unsigned)D4;
-      const int m = (int)((step * (unsigned)j1) % (unsigned)D4);
-      tc[kpl * Kc + j1 - ja1] = twiddle(J.q, D, m);
-      ts[kpl * Kc + j1 - ja1] = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
+    for (int t = threadIdx.x; t < nkp * Klp; t += kP1Threads) {
+      const int kpl = t / Klp, jl = t - kpl * Klp;
+      double c = 0.0, sn = 0.0;
+      if (jl < Kl) {
+        // pi j1 k' / A = pi (2 B j1 k') / (2 D); both factors below 4D
+        const unsigned step = (2u * (unsigned)B * (unsigned)(kp0 + kpl)) % (unsigned)D4;
+        const int m = (int)((step * (unsigned)(ja1 + jl)) % (unsigned)D4);
+        c = twiddle(J.q, D, m);
+        sn = twiddle(J.q, D, m >= D ? m - D : m + 3 * D);
+      }
+      tc[kpl * Kc + jl] = c;
+      ts[kpl * Kc + jl] = sn;
     }
   };
   if (b.early) stage_twiddles();
   pdl_wait();
   if (!b.early) stage_twiddles();
-  for (int t = threadIdx.x; t < Kl * B; t += kP1Threads) {
+  for (int t = threadIdx.x; t < Klp * B; t += kP1Threads) {
     const int j = ja1 * B + t;
     double v = 0.0;
-    if (j >= J.jlo && j < j_end) {
+    if (t < Kl * B && j >= J.jlo && j < j_end) {
       const double w = (j == 0) ? J.w0 : ((j == J.N - 1) ? J.wl : J.wm);
       v = w * in_at(x, J.in_sk, wr, j);
     }
     xs[t] = v;
   }
   __syncthreads();
-  const int P = max(1, kP1Threads / (nkp * B));  // parts splitting the j1 sum
+  const int P = max(1, kP1Threads / (nkp * B));  // parts splitting the j1 pair sum
   const int nitem = nkp * P * B;
+  const int npair = Klp / 2;
   for (int it = threadIdx.x; it < nitem; it += kP1Threads) {
     const int j2 = it % B, r = it / B;
     const int part = r % P, kpl = r / P;
     const double* tcp = tc + kpl * Kc;
     const double* tsp = ts + kpl * Kc;
-    double c = 0.0, s = 0.0;
-#pragma unroll 4
-    for (int j1 = part; j1 < Kl; j1 += P) {
-      const double v = xs[j1 * B + j2];
-      c = fma(v, tcp[j1], c);
-      s = fma(v, tsp[j1], s);
+    double ce = 0.0, se = 0.0, co = 0.0, so = 0.0;
+#pragma unroll 2
+    for (int q = part; q < npair; q += P) {
+      const double v0 = xs[(2 * q) * B + j2], v1 = xs[(2 * q + 1) * B + j2];
+      ce = fma(v0, tcp[2 * q], ce);
+      se = fma(v0, tsp[2 * q], se);
+      co = fma(v1, tcp[2 * q + 1], co);
+      so = fma(v1, tsp[2 * q + 1], so);
     }
-    red[2 * it] = c;
-    red[2 * it + 1] = s;
+    red[4 * it] = ce + co;      // C(k')
+    red[4 * it + 1] = se + so;  // S(k')
+    red[4 * it + 2] = ce - co;  // C(A - k')
+    red[4 * it + 3] = so - se;  // S(A - k')
   }
   __syncthreads();
   for (int t = threadIdx.x; t < nkp * B; t += kP1Threads) {
     const int j2 = t % B, kpl = t / B;
-    double c = 0.0, s = 0.0;
+    double f[4] = {0.0, 0.0, 0.0, 0.0};
     for (int part = 0; part < P; ++part) {
       const int it = (kpl * P + part) * B + j2;
-      c += red[2 * it];
-      s += red[2 * it + 1];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) f[u] += red[4 * it + u];
     }
-    fin[2 * t] = c;
-    fin[2 * t + 1] = s;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) fin[4 * t + u] = f[u];
   }
   if (ncl > 1) cluster_sync_all();
   else __syncthreads();
   if (rank == 0) {
     for (int t = threadIdx.x; t < nkp * B; t += kP1Threads) {
-      double c = fin[2 * t], s = fin[2 * t + 1];
-      for (int r = 1; r < ncl; ++r) {
-        c += ld_cluster(fin + 2 * t, (unsigned)r);
-        s += ld_cluster(fin + 2 * t + 1, (unsigned)r);
+      double f[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) f[u] = fin[4 * t + u];
+      for (int r = 1; r < ncl; ++r)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) f[u] += ld_cluster(fin + 4 * t + u, (unsigned)r);
+      const int j2 = t % B, kp = kp0 + t / B;
+      double* cs = J.cs + (((long long)line * B + j2) * (A + 1)) * 2;
+      cs[2 * kp] = f[0];
+      cs[2 * kp + 1] = f[1];
+      if (A - kp != kp) {
+        cs[2 * (A - kp)] = f[2];
+        cs[2 * (A - kp) + 1] = f[3];
       }
-      const int j2 = t % B, kpl = t / B;
-      double* cs = J.cs + (((long long)line * B + j2) * (A + 1) + kp0 + kpl) * 2;
-      cs[0] = c;
-      cs[1] = s;
     }
   }
   if (ncl > 1) cluster_sync_all();  // remote reads done before any CTA exits
@@ -647,21 +671,45 @@ __global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatchT<N
 // its slice of [0, B).  The slice's twiddles cos/sin(pi j2 k / D) are staged
 // first; lanes own outputs (their C, S loads are contiguous), warps split
 // the slice and are combined in a fixed order.
+//
+// Paired jobs (mode 1: B even, every output wanted): with B even, (-1)^j =
+// (-1)^j2, so y(D - k) = +-sum_j2 (-1)^j2 T_j2(k) for the terms T_j2(k) of
+// y(k).  Lanes own k <= D/2; warps (and cluster slices, of even length)
+// hold j2 of one parity, and the even and odd sums E, O give y(k) = E + O
+// and y(D - k) = E - O (cos kind) or O - E (sin kind).
+__host__ __device__ inline int p2_slice(int B, int ncl, bool paired) {
+  const int c = (B + ncl - 1) / ncl;
+  return (paired && ncl > 1) ? ((c + 1) & ~1) : c;
+}
+__host__ __device__ inline int p2_lanes(const AxisJob& J) { return J.mode == 1 ? J.D / 2 + 1 : J.nout; }
+
+__device__ __forceinline__ void p2_put(const AxisJob& J, const AccEpi& acc, int line, int k, double y) {
+  if (k >= J.nout) return;
+  const bool on = k >= J.klo && k < J.khi;
+  const long long e = (long long)line * J.out_sl + (long long)k * J.out_sk;
+  const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
+  const double v = on ? y * sc * J.gscale : 0.0;
+  J.out[e] = v;
+  if (J.epi) acc_epilogue(acc, e, v);
+}
+
 template <int NJ>
 __global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatchT<NJ> b, int ncl) {
   extern __shared__ double sm2[];
   __shared__ double red[kP2Warps][32];
-  __shared__ double fin[32];
+  __shared__ double fin[2][32];
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const AxisJob& J = b.job[jb];
   const int A = J.A, B = J.B, D = J.D, D4 = 4 * D;
-  const int nkb = (J.nout + 31) / 32;
+  const bool paired = J.mode == 1;
+  const int nlane = p2_lanes(J);
+  const int nkb = (nlane + 31) / 32;
   const int local = (blockIdx.x - b.start[jb]) / ncl;
   const unsigned rank = ncl > 1 ? cluster_rank() : 0u;
   const int line = local / nkb;
   const int k0 = (local - line * nkb) * 32;
-  const int Bc = (B + ncl - 1) / ncl;
+  const int Bc = p2_slice(B, ncl, paired);
   const int ja2 = min(B, (int)rank * Bc), Bl = min(B, ja2 + Bc) - ja2;
   auto stage_twiddles = [&]() {
     for (int t = threadIdx.x; t < Bl * 32; t += kP2Threads) {
@@ -677,7 +725,7 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatchT<N
   if (!b.early) stage_twiddles();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int k = k0 + lane;
-  const bool on = k < J.nout && k >= J.klo && k < J.khi;
+  const bool on = paired ? k < nlane : (k < J.nout && k >= J.klo && k < J.khi);
   int kp = k % (2 * A);
   double ssign = 1.0;
   if (kp > A) {
@@ -723,21 +771,38 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2(const AxisBatchT<N
   red[warp][lane] = acc;
   __syncthreads();
   if (warp == 0) {
-    double y = 0.0;
+    if (paired) {
+      // warps of even index hold even j2 (kP2Warps and ja2 are even)
+      double e = 0.0, o = 0.0;
 #pragma unroll
-    for (int w = 0; w < kP2Warps; ++w) y += red[w][lane];
-    fin[lane] = y;
+      for (int w = 0; w < kP2Warps; w += 2) {
+        e += red[w][lane];
+        o += red[w + 1][lane];
+      }
+      fin[0][lane] = e;
+      fin[1][lane] = o;
+    } else {
+      double y = 0.0;
+#pragma unroll
+      for (int w = 0; w < kP2Warps; ++w) y += red[w][lane];
+      fin[0][lane] = y;
+    }
   }
   if (ncl > 1) cluster_sync_all();
   else __syncthreads();
-  if (rank == 0 && warp == 0 && k < J.nout) {
-    double y = fin[lane];
-    for (int r = 1; r < ncl; ++r) y += ld_cluster(fin + lane, (unsigned)r);
-    double* out = J.out + (long long)line * J.out_sl + (long long)k * J.out_sk;
-    const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
-    const double v = on ? y * sc * J.gscale : 0.0;
-    *out = v;
-    if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, v);
+  if (rank == 0 && warp == 0) {
+    double y = fin[0][lane];
+    for (int r = 1; r < ncl; ++r) y += ld_cluster(&fin[0][lane], (unsigned)r);
+    if (paired) {
+      double o = fin[1][lane];
+      for (int r = 1; r < ncl; ++r) o += ld_cluster(&fin[1][lane], (unsigned)r);
+      if (k < nlane) {
+        p2_put(J, b.acc, line, k, y + o);
+        if (D - k != k) p2_put(J, b.acc, line, D - k, is_sin ? o - y : y - o);
+      }
+    } else if (k < J.nout) {
+      p2_put(J, b.acc, line, k, on ? y : 0.0);
+    }
   }
   if (ncl > 1) cluster_sync_all();  // remote reads done before any CTA exits
 }
@@ -753,7 +818,9 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2_lines(const AxisBa
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const AxisJob& J = b.job[jb];
   const int A = J.A, B = J.B, D = J.D, D4 = 4 * D;
-  const int nkb = (J.nout + 31) / 32;
+  const bool paired = J.mode == 1;
+  const int nlane = p2_lanes(J);
+  const int nkb = (nlane + 31) / 32;
   const int local = blockIdx.x - b.start[jb];
   const int kb = local % nkb;
   const int l0 = (local / nkb) * lpc;
@@ -772,7 +839,7 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2_lines(const AxisBa
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int k = k0 + lane;
-  const bool on = k < J.nout && k >= J.klo && k < J.khi;
+  const bool on = paired ? k < nlane : (k < J.nout && k >= J.klo && k < J.khi);
   int kp = k % (2 * A);
   double ssign = 1.0;
   if (kp > A) {
@@ -780,27 +847,33 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2_lines(const AxisBa
     ssign = -1.0;
   }
   const bool is_sin = (J.off != 0);
-  const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
   const double2* tw = reinterpret_cast<const double2*>(sm2) + lane;
   const int l1 = min(J.nlines, l0 + lpc);
   for (int line = l0 + warp; line < l1; line += kP2Warps) {
     const double* cs = J.cs + ((long long)line * B * (A + 1) + kp) * 2;
-    double acc = 0.0;
+    double ae = 0.0, ao = 0.0;  // even, odd j2 (paired jobs; else all in ae)
     if (on) {
 #pragma unroll 4
       for (int j2 = 0; j2 < B; ++j2) {
         const long long o = (long long)j2 * (A + 1) * 2;
         const double C = __ldcg(cs + o), S = ssign * __ldcg(cs + o + 1);
         const double2 t = tw[j2 * 32];
-        if (is_sin) acc = fma(t.x, S, fma(t.y, C, acc));
-        else acc = fma(t.x, C, fma(-t.y, S, acc));
+        if (paired && (j2 & 1)) {  // j2 is warp-uniform
+          if (is_sin) ao = fma(t.x, S, fma(t.y, C, ao));
+          else ao = fma(t.x, C, fma(-t.y, S, ao));
+        } else {
+          if (is_sin) ae = fma(t.x, S, fma(t.y, C, ae));
+          else ae = fma(t.x, C, fma(-t.y, S, ae));
+        }
       }
     }
-    if (k < J.nout) {
-      double* out = J.out + (long long)line * J.out_sl + (long long)k * J.out_sk;
-      const double v = on ? acc * sc * J.gscale : 0.0;
-      *out = v;
-      if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, v);
+    if (paired) {
+      if (k < nlane) {
+        p2_put(J, b.acc, line, k, ae + ao);
+        if (D - k != k) p2_put(J, b.acc, line, D - k, is_sin ? ao - ae : ae - ao);
+      }
+    } else {
+      p2_put(J, b.acc, line, k, on ? ae : 0.0);
     }
   }
 }
@@ -1018,8 +1091,14 @@ int axis_kind(int grid_axis_is_z, int dir, int cs) {
   return cs ? K_S1_F2S : K_C1_F2S;
 }
 
-// Choose D = A * B minimising the two-level work 2 (A+1) nin + 2 B nout;
-// A = 0 when the direct sum (about nin * nout / 2 FMAs) is cheaper.
+// FMAs of a two-level pass pair on one line: pass 1 folds k' about A/2,
+// pass 2 pairs outputs k, D - k when B is even and every output is wanted
+double x_two_level_cost(int A, int B, int D, int nin, int nout) {
+  const bool paired = (B % 2 == 0) && nout == D + 1;
+  return 2.0 * (A / 2 + 1) * (double)nin + 2.0 * B * (paired ? (double)(D / 2 + 1) : (double)nout);
+}
+// Choose D = A * B minimising the two-level work x_two_level_cost; A = 0
+// when the direct sum (about nin * nout / 2 FMAs) is cheaper.
 void pick_factors(int D, int nin, int nout, int* Aout, int* Bout) {
   *Aout = *Bout = 0;
   const double direct = 0.5 * (double)nin * (double)nout;
@@ -1028,7 +1107,7 @@ void pick_factors(int D, int nin, int nout, int* Aout, int* Bout) {
     if (D % A) continue;
     const int B = D / A;
     if (B < 2 || B > 256) continue;  // pass 2 stages B x 32 twiddle pairs
-    const double cost = 2.0 * (A + 1) * (double)nin + 2.0 * B * (double)nout;
+    const double cost = x_two_level_cost(A, B, D, nin, nout);
     if (cost < best) {
       best = cost;
       *Aout = A;
@@ -1066,14 +1145,14 @@ void allow_smem(K kern) {
 size_t pass1_smem(const AxisJob& J, int kpc, int ncl) {
   const int j_end = std::min(J.jhi, J.nin);
   const int K = (j_end + J.B - 1) / J.B;
-  const int Kc = (K + ncl - 1) / ncl;
-  const int nkp = std::min(kpc, J.A + 1);
+  const int Kc = p1_slice(K, ncl);
+  const int nkp = std::min(kpc, p1_half(J.A) + 1);
   const int items = std::max(kP1Threads, nkp * J.B);
   return sizeof(double) *
-         (2 * (size_t)kpc * J.B + (size_t)Kc * J.B + 2 * (size_t)kpc * Kc + 2 * (size_t)items);
+         (4 * (size_t)kpc * J.B + (size_t)Kc * J.B + 2 * (size_t)kpc * Kc + 4 * (size_t)items);
 }
 size_t pass2_smem(const AxisJob& J, int ncl) {
-  return sizeof(double) * 2 * 32 * (size_t)((J.B + ncl - 1) / ncl);
+  return sizeof(double) * 2 * 32 * (size_t)p2_slice(J.B, ncl, J.mode == 1);
 }
 
 // Cluster size: split a CTA's sum only while its FP64 work (`fmas`, at about
@@ -1086,8 +1165,18 @@ int pick_cluster(long long units, long long fmas, int terms, int nsm) {
   return ncl;
 }
 
+// FMAs of a two-level pass pair on one line
+double two_level_fmas(const AxisJob& J) {
+  return x_two_level_cost(J.A, J.B, J.D, std::min(J.nin, J.N), J.nout);
+}
+// the y passes (ytl_pass1/2) run the unfolded sums
+double y_two_level_fmas(const AxisJob& J) {
+  return 2.0 * (J.A + 1) * (double)std::min(J.nin, J.N) + 2.0 * J.B * (double)J.nout;
+}
+
 void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
   b.early = early ? 1 : 0;
+  for (int i = 0; i < b.njobs; ++i) g_xform_fmas += (double)b.job[i].nlines * two_level_fmas(b.job[i]);
   static bool attr_set = false;
   if (!attr_set) {
     for (int nj : {1, 2, 4, 8, kMaxJobs})
@@ -1104,7 +1193,7 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
   int kmin = 1 << 30;
   for (int i = 0; i < b.njobs; ++i) {
     const AxisJob& J = b.job[i];
-    rows += (long long)J.nlines * (J.A + 1);
+    rows += (long long)J.nlines * (p1_half(J.A) + 1);
     const int K = (std::min(J.jhi, J.nin) + J.B - 1) / J.B;
     kmin = std::min(kmin, K);
     kbmax = std::max(kbmax, (long long)K * J.B);
@@ -1121,7 +1210,7 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
   int total = 0;
   for (int i = 0; i < b.njobs; ++i) {
     b.start[i] = total;
-    total += b.job[i].nlines * ((b.job[i].A + 1 + kpc - 1) / kpc) * ncl1;
+    total += b.job[i].nlines * ((p1_half(b.job[i].A) + 1 + kpc - 1) / kpc) * ncl1;
   }
   b.start[b.njobs] = total;
   if (total > 0)
@@ -1141,12 +1230,12 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
       attr_l = true;
     }
     long long blocks = 0;
-    for (int i = 0; i < b.njobs; ++i) blocks += (long long)b.job[i].nlines * ((b.job[i].nout + 31) / 32);
+    for (int i = 0; i < b.njobs; ++i) blocks += (long long)b.job[i].nlines * ((p2_lanes(b.job[i]) + 31) / 32);
     const int lpc = (int)std::min<long long>(16, std::max<long long>(4, blocks / (4LL * std::max(nsm, 1))));
     total = 0;
     for (int i = 0; i < b.njobs; ++i) {
       b.start[i] = total;
-      total += ((b.job[i].nlines + lpc - 1) / lpc) * ((b.job[i].nout + 31) / 32);
+      total += ((b.job[i].nlines + lpc - 1) / lpc) * ((p2_lanes(b.job[i]) + 31) / 32);
       smem2 = std::max(smem2, pass2_smem(b.job[i], 1));
     }
     b.start[b.njobs] = total;
@@ -1161,7 +1250,7 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
   long long blocks = 0;
   int bmin = 1 << 30, bmax = 0;
   for (int i = 0; i < b.njobs; ++i) {
-    blocks += (long long)b.job[i].nlines * ((b.job[i].nout + 31) / 32);
+    blocks += (long long)b.job[i].nlines * ((p2_lanes(b.job[i]) + 31) / 32);
     bmin = std::min(bmin, b.job[i].B);
     bmax = std::max(bmax, b.job[i].B);
   }
@@ -1169,7 +1258,7 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
   total = 0;
   for (int i = 0; i < b.njobs; ++i) {
     b.start[i] = total;
-    total += b.job[i].nlines * ((b.job[i].nout + 31) / 32) * ncl2;
+    total += b.job[i].nlines * ((p2_lanes(b.job[i]) + 31) / 32) * ncl2;
     smem2 = std::max(smem2, pass2_smem(b.job[i], ncl2));
   }
   b.start[b.njobs] = total;
@@ -1240,6 +1329,7 @@ void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
     }
     J.nchunk = nchunk;
     J.chunk = chunk;
+    g_xform_fmas += (double)J.nlines * J.nlane * std::max(J.tb - J.ta, 1);
     b.start[i] = total;
     total += J.nlines * J.ntile * J.nchunk;
   }
@@ -1282,6 +1372,7 @@ void pick_factors_y(int D, int nin, int nout, int* Aout, int* Bout) {
 
 void launch_ytl(AxisBatch& b, bool early, cudaStream_t st) {
   b.early = early ? 1 : 0;
+  for (int i = 0; i < b.njobs; ++i) g_xform_fmas += (double)b.job[i].nlines * y_two_level_fmas(b.job[i]);
   static bool attr_set = false;
   if (!attr_set) {
     for (int nj : {1, 2, 4, 8, kMaxJobs})
@@ -1360,6 +1451,10 @@ void launch_batch_y(AxisBatch& in, const Tables& tb, cudaStream_t st) {
     } else if (c1s1 && J.nin >= J.N && J.nout <= J.D / 2 + 1 && J.D >= 4 && J.w0 == J.wl) {
       J.mode = 2;
     }
+    {
+      const int nin = std::min(std::min(J.jhi, J.nin), J.N) - J.jlo;
+      g_xform_fmas += (double)J.nlines * J.nlane * (J.mode == 2 ? (J.D + 1) / 2 : std::max(nin, 1));
+    }
     b.start[i] = total;
     const int nlb = (J.nlines + kYThreads - 1) / kYThreads;
     total += nlb * ((J.nlane + kYR - 1) / kYR);
@@ -1373,6 +1468,8 @@ void launch_batch_y(AxisBatch& in, const Tables& tb, cudaStream_t st) {
 }
 
 }  // namespace
+
+thread_local double g_xform_fmas = 0.0;
 
 std::vector<double> quarter_table(int D) {
   std::vector<double> q(D + 1);
@@ -1477,6 +1574,7 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
       if (A > 0 && cs_used + need <= tb.cs_cap) {
         J.A = A;
         J.B = B;
+        J.mode = (B % 2 == 0 && J.nout == J.N) ? 1 : 0;  // pass 2 pairs k, D - k
         J.cs = tb.cs + cs_used;
         cs_used += need;
         b2.job[b2.njobs++] = J;

@@ -76,6 +76,8 @@ typedef struct hosnwt_info {
   int kernels_per_step;    /* kernel launches in one RK4(5) step graph */
   double device_ms;        /* device time of all steps and accepts so far
                               (CUDA events on the context's stream) */
+  double fmas_per_step;    /* FP64 FMAs of the transform passes in one step
+                              graph (terms x outputs of the algorithm run) */
 } hosnwt_info;
 
 typedef struct hosnwt_ctx hosnwt_ctx;
