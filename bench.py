@@ -421,6 +421,31 @@ def run_3d(args):
     print(json.dumps(line), flush=True)
 
 
+def run_profile_step(args, w):
+    """One step of a tank between cudaProfilerStart / cudaProfilerStop, after
+    `--warmup` untimed steps, for `ncu --profile-from-start off`: the capture
+    then holds exactly the kernels of one step graph and its accept."""
+    import torch
+    import hosnwt
+    tank = hosnwt.Tank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
+                       probes=w["probes"], wave_dir=w["wave_dir"])
+    info = tank.info()
+    h = info["delt"]
+    for _ in range(args.warmup):
+        tank.step(h)
+        tank.accept(h)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    tank.step(h)
+    tank.accept(h)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"profile_step": w["name"], "kernels_per_step": info["kernels_per_step"],
+                      "fmas_per_step": info["fmas_per_step"], "n1": info["n1"], "n2": info["n2"],
+                      "nd1": info["nd1"], "nd2": info["nd2"]}), flush=True)
+    tank.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,7 +454,16 @@ def main():
     ap.add_argument("--impl", default="cuda", choices=("cuda", "reference"))
     ap.add_argument("--workload", default="irregular_2d", choices=("irregular_2d", "ensemble", "directional_3d"))
     ap.add_argument("--sim-seconds", type=float, default=1.0, help="ensemble: simulated seconds per tank")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="run one step inside a cudaProfilerStart/Stop range (for ncu) and exit")
     args = ap.parse_args()
+    if args.profile_step:
+        with tempfile.TemporaryDirectory() as tmp:
+            if args.workload == "directional_3d":
+                run_profile_step(args, workloads.directional_3d(tmp))
+            else:
+                run_profile_step(args, workloads.irregular_2d(tmp))
+        return
     if args.workload == "ensemble":
         run_ensemble(args)
         return

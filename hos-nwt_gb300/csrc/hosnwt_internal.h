@@ -102,8 +102,9 @@ struct AxisJob {
   double w0, wm, wl;         // weights for j == 0, interior j, j == N-1
   double s0, sm, sl;         // scales for k == 0, interior k, k == N-1
   double gscale;
-  const double* win;         // optional input weights (first pass only):
-  long long win_sl;          //   input j of line l is multiplied by win[j + l * win_sl]
+  const double* win;         // optional input weights (first pass only): input j
+  long long win_sl;          //   of line l is multiplied by win[j * win_sk + l * win_sl]
+  long long win_sk;
   const double* q;           // quarter-wave table cos(pi*m/(2D)), m = 0..D
   const double* ty;          // y passes: twiddle rows [j * ldy + k], k <= D/2 (or null)
   int ldy;

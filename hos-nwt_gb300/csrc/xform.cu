@@ -34,9 +34,9 @@ __device__ __forceinline__ int mod4d(long long v, int D4) {
 
 // input j of a first-pass line, times the optional weight
 __device__ __forceinline__ double in_at(const double* __restrict__ x, long long sk,
-                                       const double* __restrict__ w, int j) {
+                                       const double* __restrict__ w, long long wsk, int j) {
   const double v = __ldg(x + (long long)j * sk);
-  return w ? v * __ldg(w + j) : v;
+  return w ? v * __ldg(w + (long long)j * wsk) : v;
 }
 
 constexpr int kXThreads = 256;   // 8 warps
@@ -100,13 +100,13 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatchT<
     if (J.mode == 2) {
       for (int t = threadIdx.x; t < sb - sa; t += kXThreads) {
         const int j = sa + t;
-        const double xa = in_at(x, sk, wr, j);
-        const double xb = in_at(x, sk, wr, D - j);
+        const double xa = in_at(x, sk, wr, J.win_sk, j);
+        const double xb = in_at(x, sk, wr, J.win_sk, D - j);
         su[t] = xa + xb;
         sv[t] = xa - xb;
       }
     } else {
-      for (int t = threadIdx.x; t < sb - sa; t += kXThreads) su[t] = in_at(x, sk, wr, sa + t);
+      for (int t = threadIdx.x; t < sb - sa; t += kXThreads) su[t] = in_at(x, sk, wr, J.win_sk, sa + t);
     }
     __syncthreads();
     const int len = sb - sa;
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatchT<
     const int j_end = min(J.jhi, J.nin);
     if (J.mode == 2) {
       if (J.jlo == 0) {  // pair (0, D) with the end weight
-        const double xa = in_at(x, sk, wr, 0), xb = in_at(x, sk, wr, D);
+        const double xa = in_at(x, sk, wr, J.win_sk, 0), xb = in_at(x, sk, wr, J.win_sk, D);
         const double t = ((k & 1) == 0) ? xa + xb : xa - xb;
         e = fma(J.w0 * t, twiddle_s(q, D, mod4d((long long)J.bj * kk + J.off, D4)), e);
       }
@@ -169,18 +169,18 @@ __global__ void __launch_bounds__(kXThreads) axis_pass_lanes_k(const AxisBatchT<
         const int jm = D / 2;
         if (jm >= J.jlo && jm < J.jhi && jm > 0) {
           const int mm = mod4d((long long)(J.aj * jm + J.bj) * kk + J.off, D4);
-          e = fma(J.wm * in_at(x, sk, wr, jm), twiddle_s(q, D, mm), e);
+          e = fma(J.wm * in_at(x, sk, wr, J.win_sk, jm), twiddle_s(q, D, mm), e);
         }
       }
     } else {
       if (J.jlo == 0 && 0 < j_end) {
         const int mm = mod4d((long long)J.bj * kk + J.off, D4);
-        e = fma(J.w0 * in_at(x, sk, wr, 0), twiddle_s(q, D, mm), e);
+        e = fma(J.w0 * in_at(x, sk, wr, J.win_sk, 0), twiddle_s(q, D, mm), e);
       }
       const int jl = J.N - 1;
       if (jl > 0 && jl >= J.jlo && jl < j_end) {
         const int mm = mod4d((long long)(J.aj * jl + J.bj) * kk + J.off, D4);
-        const double t = J.wl * in_at(x, sk, wr, jl) * twiddle_s(q, D, mm);
+        const double t = J.wl * in_at(x, sk, wr, J.win_sk, jl) * twiddle_s(q, D, mm);
         if (J.mode == 1 && (jl & 1)) o += t;
         else e += t;
       }
@@ -288,6 +288,9 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
   const int D = J.D, D4 = 4 * D;
   const double* __restrict__ x = J.in + (long long)line * J.in_sl;
   const long long sk = J.in_sk;
+  // input weights (a y pass that runs first reads them along y)
+  const double* __restrict__ wr = J.win ? J.win + (long long)line * J.win_sl : nullptr;
+  auto X = [&](int j) { return in_at(x, sk, wr, J.win_sk, j); };
   const int j_end = min(J.jhi, J.nin);
   const bool is_sin = (J.off != 0);
   double* out = J.out + (long long)line * J.out_sl;
@@ -321,14 +324,14 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
     const int a1 = min(j_end, J.N - 1);
     int j = a0;
     if (j < a1 && (j & 1)) {
-      const double v = __ldg(x + (long long)j * sk);
+      const double v = X(j);
       row8(T + j * ld, t);
 #pragma unroll
       for (int r = 0; r < kYR; ++r) O[r] = fma(v, t[r], O[r]);
       ++j;
     }
     for (; j + 1 < a1; j += 2) {
-      const double v0 = __ldg(x + (long long)j * sk), v1 = __ldg(x + (long long)(j + 1) * sk);
+      const double v0 = X(j), v1 = X(j + 1);
       double t1[kYR];
       row8(T + j * ld, t);
       row8(T + (j + 1) * ld, t1);
@@ -339,7 +342,7 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
       }
     }
     if (j < a1) {
-      const double v = __ldg(x + (long long)j * sk);
+      const double v = X(j);
       row8(T + j * ld, t);
 #pragma unroll
       for (int r = 0; r < kYR; ++r) E[r] = fma(v, t[r], E[r]);
@@ -352,9 +355,9 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
       const int k = k0 + r;
       if (k >= J.nlane) break;
       double e = J.wm * E[r], o = J.wm * O[r];
-      if (J.jlo == 0 && 0 < j_end) e = fma(J.w0 * __ldg(x), t0[r], e);
+      if (J.jlo == 0 && 0 < j_end) e = fma(J.w0 * X(0), t0[r], e);
       if (D >= J.jlo && D < j_end) {
-        const double tt = J.wl * __ldg(x + (long long)D * sk) * tD[r];
+        const double tt = J.wl * X(D) * tD[r];
         if (D & 1) o += tt;
         else e += tt;
       }
@@ -369,7 +372,7 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
     for (int r = 0; r < kYR; ++r) acc[r] = 0.0;
     const int pe = (D + 1) / 2;  // interior pairs j < D - j
     for (int j = 1; j < pe; ++j) {
-      const double xa = __ldg(x + (long long)j * sk), xb = __ldg(x + (long long)(D - j) * sk);
+      const double xa = X(j), xb = X(D - j);
       const double u = xa + xb, v = xa - xb;
       row8(T + j * ld, t);
 #pragma unroll
@@ -387,12 +390,12 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
       if (k >= J.nlane) break;
       double tt = J.wm * acc[r];
       if (J.jlo == 0) {
-        const double xa = __ldg(x), xb = __ldg(x + (long long)D * sk);
+        const double xa = X(0), xb = X(D);
         tt = fma(J.w0 * (((k & 1) == 0) ? xa + xb : xa - xb), t0[r], tt);
       }
       if ((D & 1) == 0) {
         const int jm = D / 2;
-        if (jm >= J.jlo && jm < J.jhi) tt = fma(J.wm * __ldg(x + (long long)jm * sk), tm[r], tt);
+        if (jm >= J.jlo && jm < J.jhi) tt = fma(J.wm * X(jm), tm[r], tt);
       }
       put(k, tt);
     }
@@ -403,7 +406,7 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
     const int a1 = min(j_end, J.N - 1);
     int j = a0;
     if (j < a1 && (j & 1)) {
-      const double v = __ldg(x + (long long)j * sk);
+      const double v = X(j);
 #pragma unroll
       for (int r = 0; r < kYR; ++r) {
         O[r] = fma(v, twiddle(J.q, D, m[r]), O[r]);
@@ -412,7 +415,7 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
       ++j;
     }
     for (; j + 1 < a1; j += 2) {
-      const double v0 = __ldg(x + (long long)j * sk), v1 = __ldg(x + (long long)(j + 1) * sk);
+      const double v0 = X(j), v1 = X(j + 1);
 #pragma unroll
       for (int r = 0; r < kYR; ++r) {
         E[r] = fma(v0, twiddle(J.q, D, m[r]), E[r]);
@@ -422,7 +425,7 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
       }
     }
     if (j < a1) {
-      const double v = __ldg(x + (long long)j * sk);
+      const double v = X(j);
 #pragma unroll
       for (int r = 0; r < kYR; ++r) E[r] = fma(v, twiddle(J.q, D, m[r]), E[r]);
     }
@@ -431,9 +434,9 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
       const int k = k0 + r;
       if (k >= J.nlane) break;
       double e = J.wm * E[r], o = J.wm * O[r];
-      if (J.jlo == 0 && 0 < j_end) e = fma(J.w0 * __ldg(x), twiddle(J.q, D, mod4d(J.off, D4)), e);
+      if (J.jlo == 0 && 0 < j_end) e = fma(J.w0 * X(0), twiddle(J.q, D, mod4d(J.off, D4)), e);
       if (D >= J.jlo && D < j_end) {
-        const double t = J.wl * __ldg(x + (long long)D * sk) *
+        const double t = J.wl * X(D) *
                          twiddle(J.q, D, mod4d((long long)2 * D * k + J.off, D4));
         if (D & 1) o += t;
         else e += t;
@@ -448,7 +451,7 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
     // cos: even k pairs with u; sin: even k pairs with v
     const int pe = (D + 1) / 2;  // interior pairs j < D - j
     for (int j = 1; j < pe; ++j) {
-      const double xa = __ldg(x + (long long)j * sk), xb = __ldg(x + (long long)(D - j) * sk);
+      const double xa = X(j), xb = X(D - j);
       const double u = xa + xb, v = xa - xb;
 #pragma unroll
       for (int r = 0; r < kYR; ++r) {
@@ -463,13 +466,13 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
       if (k >= J.nlane) break;
       double t = J.wm * acc[r];
       if (J.jlo == 0) {  // the end pair (0, D) with the end weight
-        const double xa = __ldg(x), xb = __ldg(x + (long long)D * sk);
+        const double xa = X(0), xb = X(D);
         t = fma(J.w0 * (((k & 1) == 0) ? xa + xb : xa - xb), twiddle(J.q, D, mod4d(J.off, D4)), t);
       }
       if ((D & 1) == 0) {
         const int jm = D / 2;
         if (jm >= J.jlo && jm < J.jhi)
-          t = fma(J.wm * __ldg(x + (long long)jm * sk),
+          t = fma(J.wm * X(jm),
                   twiddle(J.q, D, mod4d((long long)2 * jm * k + J.off, D4)), t);
       }
       put(k, t);
@@ -480,7 +483,7 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
     for (int r = 0; r < kYR; ++r) acc[r] = 0.0;
     const int a1 = min(j_end, J.N - 1);
     for (int j = a0; j < a1; ++j) {
-      const double v = __ldg(x + (long long)j * sk);
+      const double v = X(j);
 #pragma unroll
       for (int r = 0; r < kYR; ++r) {
         acc[r] = fma(v, twiddle(J.q, D, m[r]), acc[r]);
@@ -495,12 +498,12 @@ __global__ void __launch_bounds__(kYThreads) axis_pass_lanes_line(const AxisBatc
       const int kk = J.ak * k + J.bk;
       if (J.jlo == 0 && 0 < j_end) {
         const int mm = mod4d((long long)J.bj * kk + J.off, D4);
-        t = fma(J.w0 * __ldg(x), twiddle(J.q, D, mm), t);
+        t = fma(J.w0 * X(0), twiddle(J.q, D, mm), t);
       }
       const int jl = J.N - 1;
       if (jl > 0 && jl >= J.jlo && jl < j_end) {
         const int mm = mod4d((long long)(J.aj * jl + J.bj) * kk + J.off, D4);
-        t = fma(J.wl * __ldg(x + (long long)jl * sk), twiddle(J.q, D, mm), t);
+        t = fma(J.wl * X(jl), twiddle(J.q, D, mm), t);
       }
       put(k, t);
     }
@@ -605,7 +608,7 @@ __global__ void __launch_bounds__(kP1Threads) two_level_pass1(const AxisBatchT<N
     double v = 0.0;
     if (t < Kl * B && j >= J.jlo && j < j_end) {
       const double w = (j == 0) ? J.w0 : ((j == J.N - 1) ? J.wl : J.wm);
-      v = w * in_at(x, J.in_sk, wr, j);
+      v = w * in_at(x, J.in_sk, wr, J.win_sk, j);
     }
     xs[t] = v;
   }
@@ -883,33 +886,37 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2_lines(const AxisBa
 // every load and store is coalesced and every twiddle is warp-uniform.
 // The partial sums are stored [((j2 (A+1) + k') 2 + {C, S}) nlines + line].
 constexpr int kYT = 128;   // lines per CTA
-constexpr int kYKP = 18;   // k' per pass-1 CTA (accumulator pairs per thread)
+constexpr int kYKF = 9;    // k' <= A/2 per pass-1 CTA (four accumulators each)
 constexpr int kYQ = 20;    // outputs of one k' class per pass-2 thread
+constexpr int kYH = 12;    // outputs k <= D/2 of one class per thread (paired jobs)
 
-// pass 1: CTA = (job, k' chunk, j2, block of kYT lines)
+// pass 1: CTA = (job, k' chunk, j2, block of kYT lines).  As in the x pass,
+// the even and odd j1 terms are summed apart, which gives C, S at k' and at
+// A - k' from the same sums: only k' <= A/2 are computed.
 template <int NJ>
 __global__ void __launch_bounds__(kYT) ytl_pass1(const AxisBatchT<NJ> b) {
   extern __shared__ double smy[];
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const AxisJob& J = b.job[jb];
-  const int A = J.A, B = J.B, D = J.D, D4 = 4 * D;
-  const int nkc = (A + 1 + kYKP - 1) / kYKP;
+  const int A = J.A, B = J.B, D = J.D, D4 = 4 * D, H = A / 2;
+  const int nkc = (H + 1 + kYKF - 1) / kYKF;
   int local = blockIdx.x - b.start[jb];
   const int kc = local % nkc;
   local /= nkc;
   const int j2 = local % B;
   const int lb = local / B;
-  const int kp0 = kc * kYKP, nkp = min(kYKP, A + 1 - kp0);
+  const int kp0 = kc * kYKF, nkp = min(kYKF, H + 1 - kp0);
   const int j_end = min(J.jhi, J.nin);
   const int K = (j_end + B - 1) / B;
-  double* tc = smy;               // K x kYKP cos(pi j1 k' / A)
-  double* ts = tc + K * kYKP;     // K x kYKP sin(pi j1 k' / A)
+  const int Kp = (K + 1) & ~1;    // whole (even, odd) pairs
+  double* tc = smy;               // Kp x kYKF cos(pi j1 k' / A), zero beyond K
+  double* ts = tc + Kp * kYKF;    // Kp x kYKF sin(pi j1 k' / A)
   auto stage = [&]() {
-    for (int t = threadIdx.x; t < K * kYKP; t += kYT) {
-      const int j1 = t / kYKP, kpl = t - j1 * kYKP;
+    for (int t = threadIdx.x; t < Kp * kYKF; t += kYT) {
+      const int j1 = t / kYKF, kpl = t - j1 * kYKF;
       double c = 0.0, sn = 0.0;
-      if (kpl < nkp) {
+      if (kpl < nkp && j1 < K) {
         const unsigned step = (2u * (unsigned)B * (unsigned)(kp0 + kpl)) % (unsigned)D4;
         const int m = (int)((step * (unsigned)j1) % (unsigned)D4);
         c = twiddle(J.q, D, m);
@@ -926,27 +933,43 @@ __global__ void __launch_bounds__(kYT) ytl_pass1(const AxisBatchT<NJ> b) {
   const int line = lb * kYT + threadIdx.x;
   if (line >= J.nlines) return;
   const double* __restrict__ x = J.in + (long long)line * J.in_sl;
-  double c[kYKP], sn[kYKP];
+  const double* __restrict__ wr = J.win ? J.win + (long long)line * J.win_sl : nullptr;
+  double ce[kYKF], co[kYKF], se[kYKF], so[kYKF];
 #pragma unroll
-  for (int r = 0; r < kYKP; ++r) c[r] = sn[r] = 0.0;
-  for (int j1 = 0; j1 < K; ++j1) {
-    const int j = B * j1 + j2;
-    if (j < J.jlo || j >= j_end) continue;
-    const double w = (j == 0) ? J.w0 : ((j == J.N - 1) ? J.wl : J.wm);
-    const double v = w * __ldg(x + (long long)j * J.in_sk);
+  for (int r = 0; r < kYKF; ++r) ce[r] = co[r] = se[r] = so[r] = 0.0;
+  for (int j1 = 0; j1 < K; j1 += 2) {
+    const int j = B * j1 + j2, jo = j + B;
+    double v0 = 0.0, v1 = 0.0;
+    if (j >= J.jlo && j < j_end) {
+      const double w = (j == 0) ? J.w0 : ((j == J.N - 1) ? J.wl : J.wm);
+      v0 = w * in_at(x, J.in_sk, wr, J.win_sk, j);
+    }
+    if (j1 + 1 < K && jo >= J.jlo && jo < j_end) {
+      const double w = (jo == J.N - 1) ? J.wl : J.wm;
+      v1 = w * in_at(x, J.in_sk, wr, J.win_sk, jo);
+    }
+    const double* t0 = tc + j1 * kYKF;
+    const double* s0 = ts + j1 * kYKF;
 #pragma unroll
-    for (int r = 0; r < kYKP; ++r) {
-      c[r] = fma(v, tc[j1 * kYKP + r], c[r]);
-      sn[r] = fma(v, ts[j1 * kYKP + r], sn[r]);
+    for (int r = 0; r < kYKF; ++r) {
+      ce[r] = fma(v0, t0[r], ce[r]);
+      se[r] = fma(v0, s0[r], se[r]);
+      co[r] = fma(v1, t0[kYKF + r], co[r]);
+      so[r] = fma(v1, s0[kYKF + r], so[r]);
     }
   }
   const long long nl = J.nlines;
-  double* o = J.cs + ((long long)j2 * (A + 1) + kp0) * 2 * nl + line;
+  double* o = J.cs + (long long)j2 * (A + 1) * 2 * nl + line;
 #pragma unroll
-  for (int r = 0; r < kYKP; ++r) {
+  for (int r = 0; r < kYKF; ++r) {
     if (r < nkp) {
-      o[(2 * r) * nl] = c[r];
-      o[(2 * r + 1) * nl] = sn[r];
+      const int kp = kp0 + r;
+      o[(2 * kp) * nl] = ce[r] + co[r];
+      o[(2 * kp + 1) * nl] = se[r] + so[r];
+      if (A - kp != kp) {
+        o[(2 * (A - kp)) * nl] = ce[r] - co[r];
+        o[(2 * (A - kp) + 1) * nl] = so[r] - se[r];
+      }
     }
   }
 }
@@ -959,10 +982,23 @@ __device__ __forceinline__ int ytl_k(int o, int A, int kp, bool pair) {
   return (o & 1) ? 2 * A * (q + 1) - kp : 2 * A * q + kp;
 }
 
+__device__ __forceinline__ void ytl_put(const AxisJob& J, const AccEpi& acc, int line, int k, double y) {
+  if (k >= J.nout) return;
+  const bool on = k >= J.klo && k < J.khi;
+  const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
+  const double v = on ? y * sc * J.gscale : 0.0;
+  const long long e = (long long)line * J.out_sl + (long long)k * J.out_sk;
+  J.out[e] = v;
+  if (J.epi) acc_epilogue(acc, e, v);
+}
+
 // pass 2: CTA = (job, k', block of kYT lines); each C, S value is read once
-// and feeds every output of its class
+// and feeds every output of its class.  Paired jobs (mode 1: B even, every
+// output wanted): outputs k and D - k are in the same class, and with B
+// even y(D - k) = +-sum_j2 (-1)^j2 T_j2(k); the thread sums even and odd j2
+// apart for the class's outputs k <= D/2 and writes both.
 template <int NJ>
-__global__ void __launch_bounds__(kYT) ytl_pass2(const AxisBatchT<NJ> b) {
+__global__ void __launch_bounds__(kYT, 1) ytl_pass2(const AxisBatchT<NJ> b) {
   extern __shared__ double smy[];
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
@@ -972,6 +1008,7 @@ __global__ void __launch_bounds__(kYT) ytl_pass2(const AxisBatchT<NJ> b) {
   const int kp = local % (A + 1);
   const int lb = local / (A + 1);
   const bool pair = kp > 0 && kp < A;
+  const bool paired = J.mode == 1;
   double* tw = smy;  // B x kYQ (cos, sin)(pi j2 k / D)
   auto stage = [&]() {
     for (int t = threadIdx.x; t < B * kYQ; t += kYT) {
@@ -999,6 +1036,45 @@ __global__ void __launch_bounds__(kYT) ytl_pass2(const AxisBatchT<NJ> b) {
   // outputs of this class below nout (uniform over the CTA)
   int nq = 0;
   while (nq < kYQ && ytl_k(nq, A, kp, pair) < J.nout) ++nq;
+  if (paired) {
+    int nc = 0;  // outputs k <= D/2 (the class's outputs increase with oi)
+    while (nc < nq && nc < kYH && ytl_k(nc, A, kp, pair) <= D / 2) ++nc;
+    double ae[kYH], ao[kYH];
+#pragma unroll
+    for (int oi = 0; oi < kYH; ++oi) ae[oi] = ao[oi] = 0.0;
+    for (int j2 = 0; j2 < B; j2 += 2) {
+      const long long base = (long long)j2 * (A + 1) * 2 * nl;
+      const long long step = (long long)(A + 1) * 2 * nl;
+      const double C0 = __ldcg(cs + base), S0 = __ldcg(cs + base + nl);
+      const double C1 = __ldcg(cs + base + step), S1 = __ldcg(cs + base + step + nl);
+      const double2* t0 = reinterpret_cast<const double2*>(tw) + j2 * kYQ;
+      const double2* t1 = t0 + kYQ;
+#pragma unroll
+      for (int oi = 0; oi < kYH; ++oi) {
+        if (oi < nc) {
+          const bool neg = pair && (oi & 1);
+          const double Sa = neg ? -S0 : S0, Sb = neg ? -S1 : S1;
+          const double2 w0 = t0[oi], w1 = t1[oi];
+          if (is_sin) {
+            ae[oi] = fma(w0.x, Sa, fma(w0.y, C0, ae[oi]));
+            ao[oi] = fma(w1.x, Sb, fma(w1.y, C1, ao[oi]));
+          } else {
+            ae[oi] = fma(w0.x, C0, fma(-w0.y, Sa, ae[oi]));
+            ao[oi] = fma(w1.x, C1, fma(-w1.y, Sb, ao[oi]));
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int oi = 0; oi < kYH; ++oi) {
+      if (oi < nc) {
+        const int k = ytl_k(oi, A, kp, pair);
+        ytl_put(J, b.acc, line, k, ae[oi] + ao[oi]);
+        if (D - k != k) ytl_put(J, b.acc, line, D - k, is_sin ? ao[oi] - ae[oi] : ae[oi] - ao[oi]);
+      }
+    }
+    return;
+  }
   double acc[kYQ];
 #pragma unroll
   for (int oi = 0; oi < kYQ; ++oi) acc[oi] = 0.0;
@@ -1016,17 +1092,10 @@ __global__ void __launch_bounds__(kYT) ytl_pass2(const AxisBatchT<NJ> b) {
       }
     }
   }
-  double* out = J.out + (long long)line * J.out_sl;
 #pragma unroll
   for (int oi = 0; oi < kYQ; ++oi) {
     const int k = ytl_k(oi, A, kp, pair);
-    if (k < J.nout) {
-      const bool on = k >= J.klo && k < J.khi;
-      const double sc = (k == 0) ? J.s0 : ((k == J.N - 1) ? J.sl : J.sm);
-      const double v = on ? acc[oi] * sc * J.gscale : 0.0;
-      out[(long long)k * J.out_sk] = v;
-      if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, v);
-    }
+    if (oi < nq) ytl_put(J, b.acc, line, k, acc[oi]);
   }
 }
 
@@ -1169,9 +1238,15 @@ int pick_cluster(long long units, long long fmas, int terms, int nsm) {
 double two_level_fmas(const AxisJob& J) {
   return x_two_level_cost(J.A, J.B, J.D, std::min(J.nin, J.N), J.nout);
 }
-// the y passes (ytl_pass1/2) run the unfolded sums
+// the y passes (ytl_pass1/2) fold and pair the same way (pairing when the
+// job's mode is 1)
 double y_two_level_fmas(const AxisJob& J) {
-  return 2.0 * (J.A + 1) * (double)std::min(J.nin, J.N) + 2.0 * J.B * (double)J.nout;
+  return 2.0 * (J.A / 2 + 1) * (double)std::min(J.nin, J.N) +
+         2.0 * J.B * (J.mode == 1 ? (double)(J.D / 2 + 1) : (double)J.nout);
+}
+// outputs k <= D/2 of one k' class of a y pass are at most this many
+bool ytl_can_pair(int D, int A, int B, int nout, int N) {
+  return B % 2 == 0 && nout == N && 2 * ((D / 2) / (2 * A)) + 2 <= kYH;
 }
 
 void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
@@ -1361,7 +1436,8 @@ void pick_factors_y(int D, int nin, int nout, int* Aout, int* Bout) {
     const int B = D / A;
     if (B < 2 || B > 256) continue;
     if (2 * ((nout + 2 * A - 1) / (2 * A)) + 1 > kYQ) continue;
-    const double cost = 2.0 * (A + 1) * (double)nin + 2.0 * B * (double)nout;
+    const bool paired = ytl_can_pair(D, A, B, nout, D + 1);
+    const double cost = 2.0 * (A / 2 + 1) * (double)nin + 2.0 * B * (paired ? (double)(D / 2 + 1) : (double)nout);
     if (cost < best) {
       best = cost;
       *Aout = A;
@@ -1389,8 +1465,8 @@ void launch_ytl(AxisBatch& b, bool early, cudaStream_t st) {
     const int nlb = (J.nlines + kYT - 1) / kYT;
     const int K = (std::min(J.jhi, J.nin) + J.B - 1) / J.B;
     b.start[i] = total;
-    total += nlb * J.B * ((J.A + 1 + kYKP - 1) / kYKP);
-    smem1 = std::max(smem1, sizeof(double) * 2 * (size_t)K * kYKP);
+    total += nlb * J.B * ((J.A / 2 + 1 + kYKF - 1) / kYKF);
+    smem1 = std::max(smem1, sizeof(double) * 2 * (size_t)((K + 1) & ~1) * kYKF);
     smem2 = std::max(smem2, sizeof(double) * 2 * (size_t)J.B * kYQ);
   }
   b.start[b.njobs] = total;
@@ -1429,6 +1505,7 @@ void launch_batch_y(AxisBatch& in, const Tables& tb, cudaStream_t st) {
       if (A > 0 && cs_used + need <= tb.cs_cap) {
         J.A = A;
         J.B = B;
+        J.mode = ytl_can_pair(J.D, A, B, J.nout, J.N) ? 1 : 0;
         J.cs = tb.cs + cs_used;
         cs_used += need;
         b2.job[b2.njobs++] = J;
@@ -1498,13 +1575,19 @@ std::vector<double> y_twiddle_rows(int N, bool sin_kind, int* ld) {
   return t;
 }
 
-void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* const* tmp,
-                       cudaStream_t st) {
+namespace {
+
+// The passes of the requests idx[0..n), along x then y.  The first pass
+// applies the input weights, the last the scale and the accumulation
+// epilogue; tmp[idx[i]] holds the intermediate.
+void launch_ordered(const XfReq* reqs, const int* idx, int n, const Tables& tb, double* const* tmp,
+                    cudaStream_t st) {
   AxisBatch bx{}, by{};
   bx.njobs = by.njobs = 0;
-  for (int r = 0; r < nreq; ++r)
-    if (reqs[r].acc) bx.acc = by.acc = *reqs[r].acc;
-  for (int r = 0; r < nreq; ++r) {
+  for (int i = 0; i < n; ++i)
+    if (reqs[idx[i]].acc) bx.acc = by.acc = *reqs[idx[i]].acc;
+  for (int i = 0; i < n; ++i) {
+    const int r = idx[i];
     const XfReq& R = reqs[r];
     int Nx, Ny;
     const double *qx, *qy;
@@ -1516,48 +1599,53 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
     // x (or z) pass
     AxisJob& X = bx.job[bx.njobs++];
     set_kind(X, axis_kind(zaxis, R.dir, R.csx), Nx, qx);
+    X.nin = R.nin1;
+    X.nout = R.nout1;
+    X.out_sk = 1;
+    X.win_sk = 1;
+    if (!twod) {
+      X.in = R.in;
+      X.in_sk = 1;
+      X.in_sl = R.in_ld;
+      X.win = R.win;
+      X.win_sl = R.win_ld;
+      X.nlines = 1;
+      X.out = R.out;
+      X.out_sl = R.out_ld;
+      X.gscale = R.scale;
+      X.epi = R.acc ? 1 : 0;
+      continue;
+    }
+    AxisJob& Y = by.job[by.njobs++];
+    set_kind(Y, axis_kind(false, R.dir, R.csy), Ny, qy);
+    Y.ty = (R.grid == GRID_BIG) ? tb.ty_nd2[R.csy ? 1 : 0] : tb.ty_n2[R.csy ? 1 : 0];
+    Y.ldy = (R.grid == GRID_BIG) ? tb.ldy_nd2 : tb.ldy_n2;
+    Y.nin = R.nin2;
+    Y.nout = R.nout2;
+    Y.out_sl = 1;
+    // The y-sin plans zero the boundary columns of the input and output
+    // (fourier_FFTW.f90:282-285, 296-299): the x pass skips the lines beyond
+    // the input's extent.
     X.in = R.in;
     X.in_sk = 1;
     X.in_sl = R.in_ld;
     X.win = R.win;
     X.win_sl = R.win_ld;
-    X.nin = R.nin1;
-    X.gscale = twod ? 1.0 : R.scale;
-    X.epi = (!twod && R.acc) ? 1 : 0;
-    if (twod) {
-      // the y-sin plans zero the boundary columns of the input and output
-      // (fourier_FFTW.f90:282-285, 296-299): skip those lines here
-      X.nlines = R.nin2;
-      X.nout = R.nout1;
-      X.out = tmp[r];
-      X.out_sk = 1;
-      X.out_sl = R.nout1;
-    } else {
-      X.nlines = 1;
-      X.nout = R.nout1;
-      X.out = R.out;
-      X.out_sk = 1;
-      X.out_sl = R.out_ld;
-    }
-    if (twod) {
-      AxisJob& Y = by.job[by.njobs++];
-      set_kind(Y, axis_kind(false, R.dir, R.csy), Ny, qy);
-      Y.epi = R.acc ? 1 : 0;
-      Y.ty = (R.grid == GRID_BIG) ? tb.ty_nd2[R.csy ? 1 : 0] : tb.ty_n2[R.csy ? 1 : 0];
-      Y.ldy = (R.grid == GRID_BIG) ? tb.ldy_nd2 : tb.ldy_n2;
-      Y.in = tmp[r];
-      Y.in_sk = R.nout1;
-      Y.in_sl = 1;
-      Y.nin = R.nin2;
-      Y.nlines = R.nout1;
-      Y.nout = R.nout2;
-      Y.out = R.out;
-      Y.out_sk = R.out_ld;
-      Y.out_sl = 1;
-      Y.gscale = R.scale;
-    }
+    X.nlines = R.nin2;
+    X.out = tmp[r];
+    X.out_sl = R.nout1;
+    X.gscale = 1.0;
+    X.epi = 0;
+    Y.in = tmp[r];
+    Y.in_sk = R.nout1;
+    Y.in_sl = 1;
+    Y.nlines = R.nout1;
+    Y.out = R.out;
+    Y.out_sk = R.out_ld;
+    Y.gscale = R.scale;
+    Y.epi = R.acc ? 1 : 0;
   }
-  // two-level passes for the jobs whose length factors well
+  // two-level passes for the x jobs whose length factors well
   AxisBatch b2{}, bd{};
   b2.njobs = bd.njobs = 0;
   b2.acc = bd.acc = bx.acc;
@@ -1586,6 +1674,18 @@ void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* co
   if (b2.njobs) launch_two_level(b2, tb.nsm, tb.q_const, st);
   if (bd.njobs) launch_batch_x(bd, tb, st);
   if (by.njobs) launch_batch_y(by, tb, st);
+}
+
+}  // namespace
+
+void launch_transforms(const XfReq* reqs, int nreq, const Tables& tb, double* const* tmp,
+                       cudaStream_t st) {
+  // x then y for every request.  (Running the y pass first, where it takes
+  // fewer FMAs, was measured slower on the 3-D big grid: the x pass over
+  // the extra lines runs at a lower FP64 rate than the y pass it saves.)
+  int idx[kMaxJobs];
+  for (int r = 0; r < nreq; ++r) idx[r] = r;
+  launch_ordered(reqs, idx, nreq, tb, tmp, st);
 }
 
 namespace {
