@@ -446,6 +446,25 @@ def run_profile_step(args, w):
     tank.close()
 
 
+def run_profile_roofline(args, w):
+    """The roofline batch of run_cuda (four FOURIER_2_SPACE_BIG of n1 modes,
+    one launch of its pass pair) inside a cudaProfilerStart / Stop range, for
+    `ncu --profile-from-start off -k regex:two_level_pass -c 2`."""
+    import torch
+    import hosnwt
+    tank = hosnwt.Tank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
+                       probes=w["probes"], wave_dir=w["wave_dir"])
+    info = tank.info()
+    n1, nd1 = info["n1"], info["nd1"]
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    tank.time_transform("big", -1, "cos", "cos", (n1, 1), (nd1, 1), batch=4, nrep=1)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"profile_roofline": w["name"], "n1": n1, "nd1": nd1}), flush=True)
+    tank.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -456,7 +475,13 @@ def main():
     ap.add_argument("--sim-seconds", type=float, default=1.0, help="ensemble: simulated seconds per tank")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one step inside a cudaProfilerStart/Stop range (for ncu) and exit")
+    ap.add_argument("--profile-roofline", action="store_true",
+                    help="run the roofline transform batch once inside a cudaProfilerStart/Stop range and exit")
     args = ap.parse_args()
+    if args.profile_roofline:
+        with tempfile.TemporaryDirectory() as tmp:
+            run_profile_roofline(args, workloads.irregular_2d(tmp))
+        return
     if args.profile_step:
         with tempfile.TemporaryDirectory() as tmp:
             if args.workload == "directional_3d":
