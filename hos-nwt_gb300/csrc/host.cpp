@@ -869,7 +869,13 @@ int alloc_device(Ctx& c) {
   d.ys = dalloc<double>(c, S);
   for (int s = 0; s < 5; ++s) d.k[s] = dalloc<double>(c, S);
   d.ynew = dalloc<double>(c, S);
-  for (double** p : {&d.eta, &d.phis, &d.deta, &d.eta_c, &d.phis_c, &d.deta_c, &d.etam, &d.phim,
+  // eta, phis (and eta_c, phis_c) are adjacent, so that the drop-in step
+  // moves them in one copy each way
+  d.eta = dalloc<double>(c, 2 * nN);
+  d.phis = d.eta + nN;
+  d.eta_c = dalloc<double>(c, 2 * nN);
+  d.phis_c = d.eta_c + nN;
+  for (double** p : {&d.deta, &d.deta_c, &d.etam, &d.phim,
                      &d.eta_sp, &d.w_eta_x, &d.w_eta_y, &d.w_phi_x, &d.w_phi_y, &d.phix_add,
                      &d.phiy_add, &d.phiz_add, &d.phit_add, &d.phi_add, &d.phit_add1, &d.phiz_add1, &d.a1k,
                      &d.phiz1st, &d.rhs1, &d.X1, &d.X2, &d.X3, &d.det, &d.dph, &d.NL1, &d.NL2,
@@ -914,6 +920,11 @@ int alloc_device(Ctx& c) {
   d.counter = dalloc<unsigned int>(c, 16);
   if (cudaMallocHost((void**)&d.host_sc, SC_COUNT * sizeof(double)) != cudaSuccess) return 1;
   std::memset(d.host_sc, 0, SC_COUNT * sizeof(double));
+  // staging of the drop-in step: eta, phis, the eight arrays from a_add_1
+  // on (their order in the state vector), and the error estimate
+  if (cudaMallocHost((void**)&d.host_io, (2 * nN + (S - (size_t)c.L.off[S_AADD1]) + 1) * sizeof(double)) !=
+      cudaSuccess)
+    return 1;
   for (void* p : c.allocs)
     if (!p) return 1;
   return 0;
@@ -930,6 +941,8 @@ void free_device(Ctx& c) {
   c.allocs.clear();
   if (c.d.host_sc) cudaFreeHost(c.d.host_sc);
   c.d.host_sc = nullptr;
+  if (c.d.host_io) cudaFreeHost(c.d.host_io);
+  c.d.host_io = nullptr;
   for (cudaEvent_t e : {c.ev_fork, c.ev_eta, c.ev_join, c.ev_pow, c.ev_acc, c.ev_dl})
     if (e) cudaEventDestroy(e);
   c.ev_fork = c.ev_eta = c.ev_join = c.ev_pow = c.ev_acc = c.ev_dl = nullptr;
@@ -1070,18 +1083,26 @@ static void timed_collect(Ctx& c) {
   if (cudaEventElapsedTime(&ms, c.ev0, c.ev1) == cudaSuccess) c.dev_ms += ms;
 }
 
-static int run_step(Ctx& c, double t_o, double h_loc, double* err) {
+// Launch one step graph; the error estimate lands in host_sc[SC_ERR] when
+// the stream reaches it.
+static int launch_step(Ctx& c, double t_o, double h_loc) {
   if (!c.step_graph) return HOSNWT_ERR_ARG;
   c.d.host_sc[SC_T0] = t_o;
   c.d.host_sc[SC_H] = h_loc;
   timed_begin(c);
   if (cudaGraphLaunch(c.step_graph, c.st) != cudaSuccess) return cuda_check(c, "graph launch");
   timed_end(c);
-  double e = 0.0;
-  cudaMemcpyAsync(&e, c.d.sc + SC_ERR, sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaMemcpyAsync(c.d.host_sc + SC_ERR, c.d.sc + SC_ERR, sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  return HOSNWT_OK;
+}
+
+static int run_step(Ctx& c, double t_o, double h_loc, double* err) {
+  const int rc = launch_step(c, t_o, h_loc);
+  if (rc) return rc;
   if (cudaStreamSynchronize(c.st) != cudaSuccess) return cuda_check(c, "step");
   timed_collect(c);
   c.n_rhs += 5;
+  const double e = c.d.host_sc[SC_ERR];
   if (err) *err = e;
   if (!std::isfinite(e)) {
     c.err = "non-finite error estimate";
@@ -1123,19 +1144,38 @@ extern "C" int hosnwt_runge4_adapt2(hosnwt_ctx* h, double t_o, double* eta, doub
   Ctx& c = h->c;
   const StateLayout& L = c.L;
   const size_t nN = (size_t)c.P.n1 * c.P.n2, nA = (size_t)c.P.n3a * c.P.n2;
-  double* const arr[10] = {nullptr, nullptr, a_add_rk_1, a_add_rk_2, a_add_rkramp, a_add_rk_3, a1st, eta1st, a2nd, eta2nd};
+  double* const arr[10] = {eta, phis, a_add_rk_1, a_add_rk_2, a_add_rkramp, a_add_rk_3, a1st, eta1st, a2nd, eta2nd};
   const size_t sz[10] = {nN, nN, nA, nA, nA, nA, nN, nN, nN, nN};
-  cudaMemcpyAsync(c.d.eta, eta, nN * sizeof(double), cudaMemcpyHostToDevice, c.st);
-  cudaMemcpyAsync(c.d.phis, phis, nN * sizeof(double), cudaMemcpyHostToDevice, c.st);
-  for (int a = 2; a < 10; ++a)
-    cudaMemcpyAsync(c.d.y0 + L.off[a], arr[a], sz[a] * sizeof(double), cudaMemcpyHostToDevice, c.st);
-  int rc = run_step(c, t_o, h_loc, err);
-  if (rc != HOSNWT_OK && rc != HOSNWT_ERR_NAN) return rc;
-  cudaMemcpyAsync(eta, c.d.eta_c, nN * sizeof(double), cudaMemcpyDeviceToHost, c.st);
-  cudaMemcpyAsync(phis, c.d.phis_c, nN * sizeof(double), cudaMemcpyDeviceToHost, c.st);
-  for (int a = 2; a < 10; ++a)
-    cudaMemcpyAsync(arr[a], c.d.ynew + L.off[a], sz[a] * sizeof(double), cudaMemcpyDeviceToHost, c.st);
-  cudaStreamSynchronize(c.st);
+  // one pinned staging buffer, two copies each way, one synchronisation:
+  // [eta | phis] and the state vector from a_add_1 on are contiguous on the
+  // device, in the order of the arguments
+  double* io = c.d.host_io;
+  size_t o = 0;
+  for (int a = 0; a < 10; ++a) {
+    std::memcpy(io + o, arr[a], sz[a] * sizeof(double));
+    o += sz[a];
+  }
+  const size_t ntail = o - 2 * nN;
+  cudaMemcpyAsync(c.d.eta, io, 2 * nN * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  cudaMemcpyAsync(c.d.y0 + L.off[S_AADD1], io + 2 * nN, ntail * sizeof(double), cudaMemcpyHostToDevice, c.st);
+  int rc = launch_step(c, t_o, h_loc);
+  if (rc) return rc;
+  cudaMemcpyAsync(io, c.d.eta_c, 2 * nN * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  cudaMemcpyAsync(io + 2 * nN, c.d.ynew + L.off[S_AADD1], ntail * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) return cuda_check(c, "runge4_adapt2");
+  timed_collect(c);
+  c.n_rhs += 5;
+  o = 0;
+  for (int a = 0; a < 10; ++a) {
+    std::memcpy(arr[a], io + o, sz[a] * sizeof(double));
+    o += sz[a];
+  }
+  const double e = c.d.host_sc[SC_ERR];
+  *err = e;
+  if (!std::isfinite(e)) {
+    c.err = "non-finite error estimate";
+    rc = HOSNWT_ERR_NAN;
+  }
   const int rc2 = cuda_check(c, "runge4_adapt2");
   return rc2 ? rc2 : rc;
 }

@@ -1997,8 +1997,8 @@ void enqueue_accept(Ctx& c, bool end_ramp, cudaStream_t st) {
   const StateLayout& L = c.L;
   const long long nN = (long long)c.P.n1 * c.P.n2;
   cudaMemcpyAsync(d.y0, d.ynew, sizeof(double) * L.size, cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(d.eta, d.eta_c, sizeof(double) * nN, cudaMemcpyDeviceToDevice, st);
-  cudaMemcpyAsync(d.phis, d.phis_c, sizeof(double) * nN, cudaMemcpyDeviceToDevice, st);
+  // eta, phis are adjacent, and so are eta_c, phis_c
+  cudaMemcpyAsync(d.eta, d.eta_c, sizeof(double) * 2 * nN, cudaMemcpyDeviceToDevice, st);
   cudaMemcpyAsync(d.deta, d.deta_c, sizeof(double) * nN, cudaMemcpyDeviceToDevice, st);
   if (end_ramp) {
     const long long nA = (long long)c.P.n3a * c.P.n2;

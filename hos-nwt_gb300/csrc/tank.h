@@ -102,6 +102,7 @@ struct Dev {
   unsigned int *counter = nullptr;
   double *probe_out = nullptr;
   double *host_sc = nullptr;    // pinned mirror of the scalar slots
+  double *host_io = nullptr;    // pinned staging of hosnwt_runge4_adapt2's arrays
 };
 
 struct Ctx {
