@@ -102,6 +102,10 @@ def load_library(path=LIB_PATH):
     lib.hosnwt_check_slope.argtypes = [vp, P(ctypes.c_int)]
     lib.hosnwt_transform_noalloc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    vp8 = ctypes.c_void_p
+    ll = ctypes.c_longlong
+    ci = ctypes.c_int
+    lib.hosnwt_tc_gemm_bf16.argtypes = [vp8, ll, vp8, ll, vp8, ll, ci, ci, ci, ci, vp8, ci, vp8, vp8, vp8]
     _lib = lib
     return lib
 
@@ -351,3 +355,25 @@ class Tank:
             delt, _, _ = self.advance(time_next, delt)
             self.check_slope()
         return recs
+
+
+def tc_gemm(A, B, bias=None, act=0, Dadd=None, out=None, out_bf16=False, err=None, stream=0):
+    """hosnwt_tc_gemm_bf16 on CUDA tensors: act(A B^T + bias + Dadd) with A
+    (M x K) and B (N x K) BF16 row-major (row strides A.stride(0),
+    B.stride(0)), FP32 accumulation; returns D (M x N, FP32 or BF16).  `err`
+    is an optional int32 CUDA tensor of one element that the kernel sets to
+    1 if one of its waits timed out."""
+    import torch
+    M, K = A.shape
+    N = B.shape[0]
+    if out is None:
+        out = torch.empty((M, N), dtype=torch.bfloat16 if out_bf16 else torch.float32, device=A.device)
+    if err is None:
+        err = torch.zeros(1, dtype=torch.int32, device=A.device)
+    rc = load_library().hosnwt_tc_gemm_bf16(
+        A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(0), out.data_ptr(), out.stride(0),
+        1 if out.dtype == torch.bfloat16 else 0, M, N, K, bias.data_ptr() if bias is not None else None,
+        int(act), Dadd.data_ptr() if Dadd is not None else None, err.data_ptr(), stream)
+    if rc != HOSNWT_OK:
+        raise HosError(f"hosnwt_tc_gemm_bf16 failed ({ERRORS.get(rc, rc)})")
+    return out

@@ -203,6 +203,18 @@ int hosnwt_transform_noalloc(int dir, int cs, int n, int nlines, const double* i
 int hosnwt_advance_many(hosnwt_ctx* const* ctxs, int n, const double* time_next,
                         double* h_rk);
 
+/* Tensor-core contraction of the surrogate (tc_gemm.cu), on device
+ * pointers: D = act(A B^T + bias + Dadd) with A (M x K, row stride lda) and
+ * B (N x K, row stride ldb) in BF16, FP32 accumulation, D FP32 (d_bf16 = 0)
+ * or BF16 (row stride ldd); bias (N) and Dadd (FP32, M x N, row stride ldd)
+ * may be null; act 0 = none, 1 = GELU (tanh form).  K, lda and ldb must be
+ * multiples of 8 and A, B 16-byte aligned.  *err (device) is set to 1 if a
+ * wait inside the kernel timed out.  Asynchronous on `stream` (a
+ * cudaStream_t, null for the default stream). */
+int hosnwt_tc_gemm_bf16(const void* A, long long lda, const void* B, long long ldb, void* D, long long ldd,
+                        int d_bf16, int M, int N, int K, const float* bias, int act, const float* Dadd,
+                        unsigned* err, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
