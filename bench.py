@@ -343,19 +343,38 @@ def run_ensemble(args):
     """Pattern 2: 64 independent 2-D tanks of uneven n1 / M, advanced by the
     same simulated time one after another and then all together
     (hosnwt_advance_many, one stream per tank).  Reports aggregate simulated
-    tank-seconds per wall-second of both and their ratio."""
+    tank-seconds per wall-second of both and their ratio.  Under torchrun
+    the tanks are split into contiguous cost-balanced blocks, one per rank
+    (ensemble.shard); the ranks exchange nothing while the tanks run, and
+    the wall times are the maximum over ranks (strong scaling: the ensemble
+    is fixed as ranks are added)."""
     import torch
     import hosnwt
-    specs = workloads.ensemble()
+    import ensemble
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device (the product has no CPU path)")
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    all_specs = workloads.ensemble()
+    sim_s = args.sim_seconds
+    start, stop = ensemble.shard(all_specs, rank, world, sim_s)
+    specs = all_specs[start:stop]
     tanks = [hosnwt.Tank(s["inp"], s["n1"], 1, s["n3"], s["mHOS"], s["p1"], 1, probes=s["probes"])
              for s in specs]
-    sim_s = args.sim_seconds
     infos = [t.info() for t in tanks]
     # warm-up: every tank a short stretch alone
     h = [i["delt"] for i in infos]
     for k, t in enumerate(tanks):
         h[k], _, _ = t.advance(0.05 / infos[k]["Tscale"], h[k])
     torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
     t0 = time.perf_counter()
     steps0 = sum(t.info()["n_rhs"] for t in tanks)
     for k, t in enumerate(tanks):
@@ -365,9 +384,12 @@ def run_ensemble(args):
     seq = time.perf_counter() - t0
     steps_seq = sum(t.info()["n_rhs"] for t in tanks) - steps0
     n_mid = [t.info()["n_rhs"] for t in tanks]
+    if dist is not None:
+        dist.barrier()
     t0 = time.perf_counter()
     tn = [t.info()["time_cur"] + sim_s / t.info()["Tscale"] for t in tanks]
-    h = list(hosnwt.advance_many(tanks, tn, h))
+    if tanks:
+        h = list(hosnwt.advance_many(tanks, tn, h))
     torch.cuda.synchronize()
     bat = time.perf_counter() - t0
     steps_bat = sum(t.info()["n_rhs"] for t in tanks) - steps0 - steps_seq
@@ -375,21 +397,42 @@ def run_ensemble(args):
     # transform FMAs of its step graph
     n_end = [t.info()["n_rhs"] for t in tanks]
     fmas_bat = sum((n_end[k] - n_mid[k]) // 5 * tanks[k].info()["fmas_per_step"] for k in range(len(tanks)))
+    summaries = [{"tank": start + k, "n1": specs[k]["n1"], "mHOS": specs[k]["mHOS"],
+                  "time_s": t.info()["time_cur"] * t.info()["Tscale"], "rhs": n_end[k]}
+                 for k, t in enumerate(tanks)]
+    if dist is not None:
+        v = torch.tensor([seq, bat, float(fmas_bat), float(steps_seq), float(steps_bat)], device="cuda",
+                         dtype=torch.float64)
+        mx = v.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(v, op=dist.ReduceOp.SUM)
+        seq, bat = float(mx[0]), float(mx[1])
+        fmas_bat, steps_seq, steps_bat = float(v[2]), int(v[3]), int(v[4])
+    gathered = ensemble.gather_summaries(summaries, start, len(all_specs))
     fp64_peak = hosnwt.fp64_peak_gflops()
-    line = {"metric": "ensemble tank-sim-s/wall-s (64 independent 2-D tanks)", "value": len(tanks) * sim_s / bat,
-            "unit": "tank-sim-s/wall-s", "n_gpus": 1, "higher_is_better": True, "dtype": "f64",
-            "data": "synthetic",
-            "config": {"workload": "ensemble: 64 x 2-D JONSWAP tanks, n1 in {129..2049}, M in {3,5,7}, p1=M, "
-                                   "tol 1e-7, per-tank adaptive dt", "sim_seconds_per_tank": sim_s},
-            "sequential_value": len(tanks) * sim_s / seq, "batched_over_sequential": seq / bat,
-            "rk_steps": {"sequential": steps_seq // 5, "batched": steps_bat // 5},
-            "wall_s": {"sequential": seq, "batched": bat},
-            "fp64_batched": {"transform_fmas": fmas_bat, "achieved_gflops": 2.0 * fmas_bat / bat / 1e9,
-                             "peak_gflops": fp64_peak, "frac": 2.0 * fmas_bat / bat / 1e9 / fp64_peak,
-                             "note": "the transform FMAs alone; the batched run is bound by the FP64 "
-                                     "pipes, so its ratio to the sequential run is capped by how "
-                                     "much FP64 work the sequential tanks leave idle"}}
-    print(json.dumps(line), flush=True)
+    if rank == 0:
+        n_all = len(all_specs)
+        line = {"metric": "ensemble tank-sim-s/wall-s (64 independent 2-D tanks)", "value": n_all * sim_s / bat,
+                "unit": "tank-sim-s/wall-s", "n_gpus": world, "higher_is_better": True, "dtype": "f64",
+                "scaling": "strong", "data": "synthetic",
+                "config": {"workload": "ensemble: 64 x 2-D JONSWAP tanks, n1 in {129..2049}, M in {3,5,7}, "
+                                       "p1=M, tol 1e-7, per-tank adaptive dt", "sim_seconds_per_tank": sim_s,
+                           "parallelism": f"tank blocks over {world} rank(s), no collective while running"},
+                "sequential_value": n_all * sim_s / seq, "batched_over_sequential": seq / bat,
+                "rk_steps": {"sequential": steps_seq // 5, "batched": steps_bat // 5},
+                "wall_s": {"sequential": seq, "batched": bat},
+                "tanks_reported": sum(1 for s in gathered if s is not None),
+                "fp64_batched": {"transform_fmas": fmas_bat, "achieved_gflops": 2.0 * fmas_bat / bat / 1e9,
+                                 "peak_gflops": fp64_peak * world,
+                                 "frac": 2.0 * fmas_bat / bat / 1e9 / (fp64_peak * world),
+                                 "note": "the transform FMAs alone; the batched run is bound by the FP64 "
+                                         "pipes, so its ratio to the sequential run is capped by how "
+                                         "much FP64 work the sequential tanks leave idle"}}
+        print(json.dumps(line), flush=True)
+    for t in tanks:
+        t.close()
+    if dist is not None:
+        dist.destroy_process_group()
 
 
 def run_3d(args):
