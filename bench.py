@@ -107,6 +107,73 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+class NvmlClocks:
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml,
+    read-only queries) every few milliseconds in a thread, so that a timed
+    region of tens of milliseconds still gets samples under load."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index=0, period_s=0.002):
+        self.index, self.period = index, period_s
+        self.sm, self.reasons, self.max_mhz = [], set(), None
+        self.lib = None
+
+    def __enter__(self):
+        import ctypes
+        try:
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return self
+            h = ctypes.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(self.index), ctypes.byref(h)) != 0:
+                lib.nvmlShutdown()
+                return self
+            mx = ctypes.c_uint()
+            if lib.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            self.lib, self.h = lib, h
+            self.get_reasons = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+            self.stop = threading.Event()
+            self.t = threading.Thread(target=self._run, daemon=True)
+            self.t.start()
+        except Exception:
+            self.lib = None
+        return self
+
+    def _run(self):
+        import ctypes
+        c, r = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop.is_set():
+            if self.lib.nvmlDeviceGetClockInfo(self.h, 1, ctypes.byref(c)) == 0:  # NVML_CLOCK_SM
+                self.sm.append(float(c.value))
+            if self.get_reasons(self.h, ctypes.byref(r)) == 0:
+                for bit, name in self.REASONS.items():
+                    if r.value & bit:
+                        self.reasons.add(name)
+            self.stop.wait(self.period)
+
+    def __exit__(self, *a):
+        if self.lib is not None:
+            self.stop.set()
+            self.t.join(timeout=5)
+            self.lib.nvmlShutdown()
+
+
+def _clocks(smi, nv):
+    """Clock record of the timed region: the NVML samples (dense) with the
+    nvidia-smi ones (200 ms apart) as a cross-check."""
+    out = smi.summary()
+    if nv.sm:
+        out = {"sm_mhz": statistics.median(nv.sm), "sm_max_mhz": nv.max_mhz or out.get("sm_max_mhz"),
+               "reasons": sorted(set(out.get("reasons", [])) - {"unavailable"} | nv.reasons),
+               "samples": len(nv.sm), "source": "nvml every 2 ms",
+               "nvidia_smi": {"sm_mhz": out.get("sm_mhz"), "samples": out.get("samples", 0)}}
+    return out
+
+
 def _measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -142,10 +209,17 @@ def _fp64_step(fmas, ms, peak_gflops):
             "frac": g / peak_gflops}
 
 
+def _fused_pass():
+    """The library runs 2-D x passes as one fused kernel when
+    HOSNWT_FUSED_PASS=1, else as the two-launch pass pair."""
+    return os.environ.get("HOSNWT_FUSED_PASS", "0")[:1] == "1"
+
+
 def _profile_traffic():
-    """Per-launch DRAM traffic of the dominant kernels from the committed ncu
-    summary (profiles/two_level_passes_irregular_2d.md), if present."""
-    p = os.path.join(ROOT, "profiles", "two_level_passes_irregular_2d.md")
+    """Per-launch DRAM traffic of the roofline batch's kernels from the
+    committed ncu summary of the pass the library runs, if present."""
+    name = "two_level_fused_irregular_2d.md" if _fused_pass() else "two_level_passes_irregular_2d.md"
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -234,12 +308,9 @@ def run_cuda(args, w):
     h = info["delt"]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    # roofline of the dominant kernels: the two passes of the big-grid
-    # transforms (a batch of four FOURIER_2_SPACE_BIG of extended n1 modes,
-    # the shape of the HOS order loop), replayed back to back in a CUDA
-    # graph.  Timed first, so that the first two_level_pass1/2 launches of
-    # this process (the warm-up of this measurement) are the ones an ncu
-    # capture with -s 0 -c 2 profiles.
+    # roofline of the dominant kernels: the big-grid transform passes (a
+    # batch of four FOURIER_2_SPACE_BIG of extended n1 modes, the shape of
+    # the HOS order loop), replayed back to back in a CUDA graph.
     n1, nd1 = info["n1"], info["nd1"]
     ms_tl = tank.time_transform("big", -1, "cos", "cos", (n1, 1), (nd1, 1), batch=4, nrep=50)
 
@@ -254,7 +325,7 @@ def run_cuda(args, w):
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    with ClockSampler(local) as clk, NvmlClocks(local) as nv:
         ms0 = tank.info()["device_ms"]
         wall0 = time.perf_counter()
         for _ in range(args.steps):
@@ -318,13 +389,14 @@ def run_cuda(args, w):
                         "d2h_bytes_per_step": io_bytes},
                 "gpu_launches": info["kernels_per_step"] * args.steps + 4 * args.steps,
                 "fp64_step": _fp64_step(info["fmas_per_step"], dev_ms / args.steps, fp64_peak),
-                "clocks": clk.summary(),
+                "clocks": _clocks(clk, nv),
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_src,
-                             "kernel": "two_level_pass1 + two_level_pass2 (4 x FOURIER_2_SPACE_BIG of n1 modes)",
+                             "kernel": ("two_level_fused" if _fused_pass() else "two_level_pass1 + two_level_pass2")
+                                       + " (4 x FOURIER_2_SPACE_BIG of n1 modes)",
                              "ms_per_launch": ms,
-                             "timing": "pass pair of the batch, 50 replays in one CUDA graph (L2 warm)",
+                             "timing": "the batch's transform launches, 50 replays in one CUDA graph (L2 warm)",
                              "fp64": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64_peak,
                                       "frac": fp64_achieved / fp64_peak,
                                       "note": "FMAs of the two-level algorithm actually run; the "
@@ -464,6 +536,106 @@ def run_3d(args):
     print(json.dumps(line), flush=True)
 
 
+GEMM_SHAPES = [
+    # (name, M, N, K)
+    ("square 8192^3 (tensor-bound)", 8192, 8192, 8192),
+    ("surrogate channel mix on the 2052 x 1028 dealiased grid (32 -> 32 channels)", 2052 * 1028, 32, 32),
+    ("surrogate truncated x transform as a contraction (1028 x 32 lines, 64 modes, 2052 points "
+     "zero-padded to K = 2056, the multiple of 8 that TMA row strides need)", 1028 * 32, 64, 2056),
+]
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), float(d.get("bf16_tflops", 1900.0)), "of measured"
+    return 6800.0, 1900.0, "of fallback"
+
+
+def run_tc_gemm(args):
+    """The surrogate's tensor-core contraction (tc_gemm.cu: TMA, tcgen05.mma,
+    TMEM accumulator) on its shapes: D = A B^T with A (M x K), B (N x K)
+    BF16, FP32 accumulate, FP32 out; CUDA events on the launching stream,
+    `--steps` launches after `--warmup`.  Beside it, torch.matmul (cuBLAS)
+    on the same BF16 operands, for reference only."""
+    import torch
+    import hosnwt
+    hbm, bf16, src = _peaks()
+    st = torch.cuda.current_stream()
+    rows = []
+    for name, M, N, K in GEMM_SHAPES:
+        g = torch.Generator(device="cuda").manual_seed(M + N + K)
+        A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+        B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+        D = torch.empty(M, N, device="cuda", dtype=torch.float32)
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+        def ours():
+            hosnwt.tc_gemm(A, B, out=D, err=err, stream=st.cuda_stream)
+
+        def cublas():
+            torch.matmul(A, B.T)
+
+        res = {}
+        for tag, fn in (("tc_gemm", ours), ("cublas", cublas)):
+            for _ in range(max(3, args.warmup)):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(args.steps):
+                fn()
+            e1.record(st)
+            torch.cuda.synchronize()
+            res[tag] = e0.elapsed_time(e1) / args.steps
+        assert int(err.item()) == 0, "tc_gemm: a wait timed out"
+        ref = (A[:256].float() @ B.float().T)
+        assert (D[:256] - ref).abs().max().item() <= 1e-5 * (A[:256].float().abs() @ B.float().abs().T).max().item()
+        flops = 2.0 * M * N * K
+        alg_bytes = 2.0 * (M * K + N * K) + 4.0 * M * N
+        ai = flops / alg_bytes
+        ms = res["tc_gemm"]
+        tflops = flops / (ms * 1e-3) / 1e12
+        gbs = alg_bytes / (ms * 1e-3) / 1e9
+        tensor_bound = ai > bf16 * 1e3 / hbm
+        rows.append({"shape": name, "M": M, "N": N, "K": K, "ms": ms, "tflops": tflops, "gbs": gbs,
+                     "bound": "tensor" if tensor_bound else "hbm",
+                     "frac": tflops / bf16 if tensor_bound else gbs / hbm,
+                     "cublas_ms": res["cublas"],
+                     "cublas_note": "torch.matmul, BF16 out"})
+        del A, B, D
+        torch.cuda.empty_cache()
+    print(json.dumps({"metric": "tc_gemm throughput (surrogate contractions)", "unit": "TFLOP/s | GB/s",
+                      "peaks": {"bf16_tflops": bf16, "hbm_gbs": hbm, "source": src},
+                      "steps": args.steps, "warmup": args.warmup, "dtype": "bf16 in, f32 accumulate",
+                      "shapes": rows}), flush=True)
+
+
+def run_profile_gemm(args):
+    """One tc_gemm launch per shape of GEMM_SHAPES between cudaProfilerStart
+    and cudaProfilerStop, for `ncu --profile-from-start off -k regex:k_tc_gemm`."""
+    import torch
+    import hosnwt
+    st = torch.cuda.current_stream()
+    ops = []
+    for name, M, N, K in GEMM_SHAPES:
+        A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+        B = torch.randn(N, K, device="cuda").to(torch.bfloat16)
+        D = torch.empty(M, N, device="cuda", dtype=torch.float32)
+        ops.append((A, B, D))
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    for A, B, D in ops:
+        hosnwt.tc_gemm(A, B, out=D, err=err, stream=st.cuda_stream)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    assert int(err.item()) == 0
+    print(json.dumps({"profile_gemm": [s[0] for s in GEMM_SHAPES]}), flush=True)
+
+
 def run_profile_step(args, w):
     """One step of a tank between cudaProfilerStart / cudaProfilerStop, after
     `--warmup` untimed steps, for `ncu --profile-from-start off`: the capture
@@ -490,9 +662,10 @@ def run_profile_step(args, w):
 
 
 def run_profile_roofline(args, w):
-    """The roofline batch of run_cuda (four FOURIER_2_SPACE_BIG of n1 modes,
-    one launch of its pass pair) inside a cudaProfilerStart / Stop range, for
-    `ncu --profile-from-start off -k regex:two_level_pass -c 2`."""
+    """The roofline batch of run_cuda (four FOURIER_2_SPACE_BIG of n1 modes:
+    the two-launch pass pair, or one two_level_fused launch under
+    HOSNWT_FUSED_PASS=1) inside a cudaProfilerStart / Stop range, for
+    `ncu --profile-from-start off -k regex:two_level`."""
     import torch
     import hosnwt
     tank = hosnwt.Tank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
@@ -514,13 +687,16 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cuda", choices=("cuda", "reference"))
-    ap.add_argument("--workload", default="irregular_2d", choices=("irregular_2d", "ensemble", "directional_3d"))
+    ap.add_argument("--workload", default="irregular_2d", choices=("irregular_2d", "ensemble", "directional_3d", "tc_gemm"))
     ap.add_argument("--sim-seconds", type=float, default=1.0, help="ensemble: simulated seconds per tank")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one step inside a cudaProfilerStart/Stop range (for ncu) and exit")
     ap.add_argument("--profile-roofline", action="store_true",
                     help="run the roofline transform batch once inside a cudaProfilerStart/Stop range and exit")
     args = ap.parse_args()
+    if args.workload == "tc_gemm":
+        run_profile_gemm(args) if args.profile_step else run_tc_gemm(args)
+        return
     if args.profile_roofline:
         with tempfile.TemporaryDirectory() as tmp:
             run_profile_roofline(args, workloads.irregular_2d(tmp))

@@ -224,6 +224,14 @@ struct Tables {
 // capture of a step graph.
 extern thread_local double g_xform_fmas;
 
+// With HOSNWT_FUSED_PASS=1 in the environment (read once when the library
+// loads), x passes of few lines (2-D tanks) run both two-level passes in one
+// kernel (two_level_fused) instead of two launches.  Off by default: on
+// GB300 the single transform is faster but a whole 2-D step is not, and an
+// ensemble of tanks is slower (the fused CTAs repeat table staging and
+// pass 1).
+extern const bool g_fused_enabled;
+
 // FP64 FMA throughput of the current device in GFLOP/s.
 double measure_fp64_peak_gflops();
 

@@ -1601,19 +1601,10 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
     W.xf({W.S2F_N(d.rhs1, kA1st)});
     if (wmk2) enqueue_sweet2(c, W, y, k);
     if (wmk3) enqueue_sweet3(c, W, y, k);
-  } else {
-    cudaMemsetAsync(kA1, 0, sizeof(double) * nA, sw);
-    cudaMemsetAsync(kAR, 0, sizeof(double) * nA, sw);
-    cudaMemsetAsync(kA1st, 0, sizeof(double) * nN, sw);
-    cudaMemsetAsync(kEta1, 0, sizeof(double) * nN, sw);
   }
-  // the second- and third-order slopes stay zero below their wavemaker order
-  if (!wmk2) {
-    cudaMemsetAsync(k + L.off[S_AADD2], 0, sizeof(double) * nA, sw);
-    cudaMemsetAsync(k + L.off[S_A2ND], 0, sizeof(double) * nN, sw);
-    cudaMemsetAsync(k + L.off[S_ETA2ND], 0, sizeof(double) * nN, sw);
-  }
-  if (!wmk3) cudaMemsetAsync(k + L.off[S_AADD3], 0, sizeof(double) * nA, sw);
+  // Slopes of the wavemaker arrays that this tank never forms (no wavemaker;
+  // orders above i_wmk) stay zero: the slope buffers are zero-filled when
+  // they are allocated and only the branches above write those parts.
 
   // 2. transform batch A: eta in space, eta / eta_x / eta_y / phis_x / phis_y on
   //    the big grid (phisxy_etaxy) and the order-1 HOS terms F2S_big(a1 kth_ext(j))
@@ -1634,10 +1625,8 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
                               d.kth_ext + (long long)nd1 * nd2 * (j - 1), nd1));
     E.xf(rq);
     cudaEventRecord(c.ev_eta, st);
-    if (n2 == 1) {
-      cudaMemsetAsync(d.etay, 0, sizeof(double) * nB, st);
-      cudaMemsetAsync(d.phisy, 0, sizeof(double) * nB, st);
-    }
+    // in 2-D tanks eta_y and phis_y stay zero: their buffers are zero-filled
+    // when allocated and only the y-gradient transforms above write them
   }
   // 5b. wavemaker branch, second part: phiadd_SL with the total additional
   //     amplitudes at z = eta (needs eta in space from batch A) and the
@@ -1669,13 +1658,9 @@ void enqueue_rhs(Ctx& c, const double* y, double* k, bool rk_mode, cudaStream_t 
            (const double*)d.B[3], (const double*)d.B[4], n1, n2, P.n3a, d.phix_add, d.phiy_add,
            d.phiz_add, d.phit_add, d.phi_add);
     }
-  } else {
-    cudaMemsetAsync(d.phix_add, 0, sizeof(double) * nN, sw);
-    cudaMemsetAsync(d.phiy_add, 0, sizeof(double) * nN, sw);
-    cudaMemsetAsync(d.phiz_add, 0, sizeof(double) * nN, sw);
-    cudaMemsetAsync(d.phit_add, 0, sizeof(double) * nN, sw);
-    cudaMemsetAsync(d.phi_add, 0, sizeof(double) * nN, sw);
   }
+  // without a wavemaker phi_add and its derivatives stay zero (zero-filled
+  // at allocation, written only by the phiadd_SL kernels above)
   W.xf({W.S2F_N(d.phix_add, d.pmode[0]), W.S2F_N(d.phiy_add, d.pmode[1]),
         W.S2F_N(d.phiz_add, d.pmode[2])});
   W.xf({W.F2S_B(d.pmode[0], n1, n1, n2, d.pxe), W.F2S_B(d.pmode[1], n1, n1, n2, d.pye),

@@ -13,6 +13,7 @@
 // warp-uniform twiddles) and several outputs per thread.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <type_traits>
 
 #include "hosnwt_internal.h"
@@ -881,6 +882,202 @@ __global__ void __launch_bounds__(kP2Threads) two_level_pass2_lines(const AxisBa
   }
 }
 
+// Fused two-level pass for launches with few lines (the x passes of 2-D
+// tanks).  The outputs k whose folded class k' (k mod 2A, reflected about
+// A) is g or A - g need the pass-1 values C, S at those two k' only, and
+// pass 1 gives both from one even/odd j1 sum.  So one CTA per (job, line,
+// class pair g <= A/2, output split u) computes C, S of its pair into
+// shared memory and then the outputs of its pair: both passes in one
+// launch, no partial sums through global memory, and no communication
+// between CTAs.  A half-period cos table is staged whole in shared memory
+// (before griddepcontrol.wait when it is constant).  With nsplit > 1 the
+// outputs of a pair are dealt round-robin to nsplit CTAs, each of which
+// repeats the (short) pass 1.
+constexpr int kFThreads = 256;
+constexpr int kFWarps = kFThreads / 32;
+
+// distinct residues k mod 2A of class pair g, ascending: {g, A-g, A+g, 2A-g}
+__host__ __device__ inline int fused_residues(int A, int g, int* r) {
+  if (g == 0) { r[0] = 0; r[1] = A; return 2; }
+  if (2 * g == A) { r[0] = g; r[1] = A + g; return 2; }
+  r[0] = g; r[1] = A - g; r[2] = A + g; r[3] = 2 * A - g;
+  return 4;
+}
+// residue i of fused_residues(A, g, .), without an indexed local array
+__host__ __device__ inline int fused_residue(int A, int g, int i) {
+  if (g == 0) return i == 0 ? 0 : A;
+  if (2 * g == A) return i == 0 ? g : A + g;
+  return i == 0 ? g : (i == 1 ? A - g : (i == 2 ? A + g : 2 * A - g));
+}
+// number of outputs k < nlane in class pair g
+__host__ __device__ inline int fused_slots(int A, int g, int nlane) {
+  int r[4];
+  const int nr = fused_residues(A, g, r);
+  const int per = nlane / (2 * A), rem = nlane - per * 2 * A;
+  int n = per * nr;
+  for (int i = 0; i < nr; ++i) n += r[i] < rem ? 1 : 0;
+  return n;
+}
+// j2 parts of pass 2 for nsb blocks of 32 outputs (even: parts keep the
+// parity of j2, which paired outputs need)
+__host__ __device__ inline int fused_parts(int nsb) {
+  if (nsb <= 0 || nsb >= kFWarps) return 2;
+  const int p = (kFWarps / nsb) & ~1;
+  return p < 2 ? 2 : p;
+}
+__host__ __device__ inline int fused_p1_parts(int B) { return B >= kFThreads ? 1 : kFThreads / B; }
+
+template <int NJ>
+__global__ void __launch_bounds__(kFThreads) two_level_fused(const AxisBatchT<NJ> b, int nsplit) {
+  extern __shared__ double smf[];
+  int jb = 0;
+  while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
+  const AxisJob& J = b.job[jb];
+  const int A = J.A, B = J.B, D = J.D, D2 = 2 * D, D4 = 4 * D, H = A / 2;
+  const int local = blockIdx.x - b.start[jb];
+  const int line = local / ((H + 1) * nsplit);
+  const int rem = local - line * (H + 1) * nsplit;
+  const int g = rem / nsplit, u = rem - g * nsplit;
+  const bool paired = J.mode == 1;
+  const bool is_sin = (J.off != 0);
+  const int nlane = paired ? D / 2 + 1 : J.nout;
+  const int j_end = min(J.jhi, J.nin);
+  const int K = (j_end + B - 1) / B;
+  const int Klp = (K + 1) & ~1;
+  // FP64 work on this GPU is scarce (about 2 operations per clock per SM),
+  // so the inner loops issue FMAs only: the table covers a half period, so
+  // a lookup needs no sign change, and signs and weights are applied to
+  // the few sums, not to the terms.
+  double* qh = smf;                 // 2D + 1: cos(pi m / (2D)), m = 0..2D
+  double* xs = qh + (D2 + 1);       // Klp * B inputs, zero outside the sum
+  double* csm = xs + Klp * B;       // B x {C(g), S(g), C(A-g), S(A-g)}
+  double* red = csm + 4 * B;        // partial sums of both passes
+  auto stage_table = [&]() {
+    // cos(pi m/(2D)) = -cos(pi (2D - m)/(2D)): the sign bit is flipped as an
+    // integer
+    for (int t = threadIdx.x; t <= D2; t += kFThreads)
+      qh[t] = t <= D ? __ldg(J.q + t)
+                     : __longlong_as_double(__double_as_longlong(__ldg(J.q + (D2 - t))) ^ (1LL << 63));
+  };
+  auto cosm = [&](int m) { return qh[m <= D2 ? m : D4 - m]; };                 // m in [0, 4D)
+  auto sinm = [&](int m) { return cosm(m >= D ? m - D : m + 3 * D); };
+  if (b.early) stage_table();
+  pdl_wait();
+  if (!b.early) stage_table();
+  const double* __restrict__ x = J.in + (long long)line * J.in_sl;
+  const double* __restrict__ wr = J.win ? J.win + (long long)line * J.win_sl : nullptr;
+  // interior inputs enter with weight wm, applied to the sums below; the two
+  // end points carry w0 / wm and wl / wm
+  const double e0 = J.w0 / J.wm, el = J.wl / J.wm;
+  for (int t = threadIdx.x; t < Klp * B; t += kFThreads) {
+    double v = 0.0;
+    if (t >= J.jlo && t < j_end) {
+      v = wr ? __ldg(x + (long long)t * J.in_sk) * __ldg(wr + (long long)t * J.win_sk)
+             : __ldg(x + (long long)t * J.in_sk);
+      if (t == 0) v *= e0;
+      else if (t == J.N - 1) v *= el;
+    }
+    xs[t] = v;
+  }
+  __syncthreads();
+  // pass 1: items (j2, part); part sums the j1 pairs q = part, part + P1, ...
+  const int P1 = fused_p1_parts(B);
+  const int npair = Klp / 2;
+  {
+    const int stp = (int)((2LL * B * g) % D4);                      // angle index of j1 = 1
+    const int inc = (int)((2LL * stp * (long long)P1) % D4);        // j1 -> j1 + 2 P1
+    for (int it = threadIdx.x; it < P1 * B; it += kFThreads) {
+      const int j2 = it % B, part = it / B;
+      double ce = 0.0, se = 0.0, co = 0.0, so = 0.0;
+      int m = (int)((2LL * stp * (long long)part) % D4);           // j1 = 2 part
+      for (int q = part; q < npair; q += P1) {
+        int m1 = m + stp;
+        if (m1 >= D4) m1 -= D4;
+        const double v0 = xs[(2 * q) * B + j2], v1 = xs[(2 * q + 1) * B + j2];
+        ce = fma(v0, cosm(m), ce);
+        se = fma(v0, sinm(m), se);
+        co = fma(v1, cosm(m1), co);
+        so = fma(v1, sinm(m1), so);
+        m += inc;
+        if (m >= D4) m -= D4;
+      }
+      red[4 * it] = ce + co;      // C(g)
+      red[4 * it + 1] = se + so;  // S(g)
+      red[4 * it + 2] = ce - co;  // C(A - g)
+      red[4 * it + 3] = so - se;  // S(A - g)
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < B; t += kFThreads) {
+    double f[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int part = 0; part < P1; ++part)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) f[v] += red[4 * (part * B + t) + v];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) csm[4 * t + v] = f[v] * J.wm;
+  }
+  __syncthreads();
+  // pass 2: this CTA's outputs are the slots s = t nsplit + u of the pair
+  const int nr = (g == 0 || 2 * g == A) ? 2 : 4;
+  const int nslot = fused_slots(A, g, nlane);
+  const int nu = nslot > u ? (nslot - u + nsplit - 1) / nsplit : 0;
+  const int nsb = (nu + 31) / 32;
+  const int P = fused_parts(nsb);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int item = warp; item < nsb * P; item += kFWarps) {
+    const int sb = item / P, p = item - sb * P;
+    const int t = sb * 32 + lane;
+    double y = 0.0;
+    if (t < nu) {
+      const int s = t * nsplit + u;
+      const int k = 2 * A * (s / nr) + fused_residue(A, g, s % nr);
+      int kp = k % (2 * A);
+      double ssign = 1.0;
+      if (kp > A) { kp = 2 * A - kp; ssign = -1.0; }
+      const double* cp = csm + (kp == g ? 0 : 2);
+      int m = (int)((2LL * p * k) % D4);
+      const int inc = (int)((2LL * P * k) % D4);
+      // cos kind: y = sum cw C - ssign sum sw S; sin kind: y = ssign sum cw S + sum sw C
+      double a1 = 0.0, a2 = 0.0;
+      if (is_sin) {
+        for (int j2 = p; j2 < B; j2 += P) {
+          a1 = fma(cosm(m), cp[4 * j2 + 1], a1);
+          a2 = fma(sinm(m), cp[4 * j2], a2);
+          m += inc;
+          if (m >= D4) m -= D4;
+        }
+        y = fma(ssign, a1, a2);
+      } else {
+        for (int j2 = p; j2 < B; j2 += P) {
+          a1 = fma(cosm(m), cp[4 * j2], a1);
+          a2 = fma(sinm(m), cp[4 * j2 + 1], a2);
+          m += inc;
+          if (m >= D4) m -= D4;
+        }
+        y = fma(-ssign, a2, a1);
+      }
+    }
+    red[item * 32 + lane] = y;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nu; t += kFThreads) {
+    const int sb = t >> 5, ln = t & 31;
+    double e = 0.0, o = 0.0;
+    for (int p = 0; p < P; p += 2) {
+      e += red[(sb * P + p) * 32 + ln];
+      o += red[(sb * P + p + 1) * 32 + ln];
+    }
+    const int s = t * nsplit + u;
+    const int k = 2 * A * (s / nr) + fused_residue(A, g, s % nr);
+    if (paired) {
+      p2_put(J, b.acc, line, k, e + o);
+      if (D - k != k) p2_put(J, b.acc, line, D - k, is_sin ? o - e : e - o);
+    } else {
+      p2_put(J, b.acc, line, k, e + o);
+    }
+  }
+}
+
 // Two-level y passes (REDFT00 / RODFT00 along a strided axis, lines
 // contiguous): the same split as above, with lanes owning lines so that
 // every load and store is coalesced and every twiddle is warp-uniform.
@@ -1345,6 +1542,63 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
     });
 }
 
+// Shared memory of the fused pass for job J with nsplit CTAs per class pair.
+size_t fused_smem(const AxisJob& J, int nsplit) {
+  const int j_end = std::min(J.jhi, J.nin);
+  const int K = (j_end + J.B - 1) / J.B;
+  const int Klp = (K + 1) & ~1;
+  const int nlane = J.mode == 1 ? J.D / 2 + 1 : J.nout;
+  size_t red = (size_t)4 * fused_p1_parts(J.B) * J.B;
+  for (int g = 0; g <= J.A / 2; ++g) {
+    const int nslot = fused_slots(J.A, g, nlane);
+    const int nu = (nslot + nsplit - 1) / nsplit;
+    const int nsb = (nu + 31) / 32;
+    red = std::max(red, (size_t)nsb * fused_parts(nsb) * 32);
+  }
+  return sizeof(double) * (2 * (size_t)J.D + 1 + (size_t)Klp * J.B + 4 * (size_t)J.B + red);
+}
+
+// The fused pass serves x-pass batches whose jobs have few lines in all
+// (2-D tanks) and no accumulation epilogue, when its shared memory fits;
+// returns false (launching nothing) otherwise.
+bool launch_two_level_fused(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
+  if (!g_fused_enabled) return false;
+  long long units = 0;
+  for (int i = 0; i < b.njobs; ++i) {
+    const AxisJob& J = b.job[i];
+    if (J.epi || J.A < 2 || J.wm == 0.0) return false;
+    units += (long long)J.nlines * (J.A / 2 + 1);
+  }
+  if (units == 0 || units > 4LL * std::max(nsm, 1)) return false;
+  // a small launch spreads each pair's outputs over up to 4 CTAs
+  const int nsplit = (int)std::max<long long>(1, std::min<long long>(4, std::max(nsm, 1) / units));
+  size_t smem = 0;
+  for (int i = 0; i < b.njobs; ++i) smem = std::max(smem, fused_smem(b.job[i], nsplit));
+  if (smem > 200 * 1024) return false;
+  static bool attr_set = false;
+  if (!attr_set) {
+    for (int nj : {1, 2, 4, 8, kMaxJobs})
+      with_capacity(nj, [&](auto c) { allow_smem(two_level_fused<decltype(c)::value>); });
+    attr_set = true;
+  }
+  b.early = early ? 1 : 0;
+  int total = 0;
+  for (int i = 0; i < b.njobs; ++i) {
+    const AxisJob& J = b.job[i];
+    b.start[i] = total;
+    total += J.nlines * (J.A / 2 + 1) * nsplit;
+    // pass 1 runs once per CTA of a pair
+    g_xform_fmas += (double)J.nlines * (two_level_fmas(J) +
+                                        (nsplit - 1) * 2.0 * (J.A / 2 + 1) * std::min(J.nin, J.N));
+  }
+  b.start[b.njobs] = total;
+  with_capacity(b.njobs, [&](auto c) {
+    constexpr int NJ = decltype(c)::value;
+    launch_pdl(two_level_fused<NJ>, dim3(total), dim3(kFThreads), smem, st, shrink<NJ>(b), nsplit);
+  });
+  return true;
+}
+
 // Decide the symmetry mode and the split of every x-pass job, then launch.
 void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
   b.early = tb.q_const ? 1 : 0;
@@ -1547,6 +1801,10 @@ void launch_batch_y(AxisBatch& in, const Tables& tb, cudaStream_t st) {
 }  // namespace
 
 thread_local double g_xform_fmas = 0.0;
+const bool g_fused_enabled = [] {
+  const char* e = std::getenv("HOSNWT_FUSED_PASS");
+  return e && e[0] == '1';
+}();
 
 std::vector<double> quarter_table(int D) {
   std::vector<double> q(D + 1);
@@ -1671,7 +1929,8 @@ void launch_ordered(const XfReq* reqs, const int* idx, int n, const Tables& tb, 
     }
     bd.job[bd.njobs++] = J;
   }
-  if (b2.njobs) launch_two_level(b2, tb.nsm, tb.q_const, st);
+  if (b2.njobs && !launch_two_level_fused(b2, tb.nsm, tb.q_const, st))
+    launch_two_level(b2, tb.nsm, tb.q_const, st);
   if (bd.njobs) launch_batch_x(bd, tb, st);
   if (by.njobs) launch_batch_y(by, tb, st);
 }
