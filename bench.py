@@ -16,6 +16,10 @@ replica tank (the path does not shard); value = total steps/s.
 
 --impl reference times the CPU restatement of the reference (the oracle:
 numpy/scipy FP64, single thread like the Fortran reference) on the same tank.
+
+Other workloads (--workload): regular_2d (the 2-D regular-wave tank, n1 =
+257, M = 3), directional_3d (513 x 257, M = 5), ensemble (64 independent
+2-D tanks), tc_gemm (the surrogate's tensor-core contraction).
 """
 from __future__ import annotations
 
@@ -43,13 +47,21 @@ METRIC = "RK4(5) steps/s (sim-s/wall-s reported alongside)"
 UNIT = "steps/s"
 
 
+WORKLOAD_TEXT = {
+    "irregular_2d": "irregular_2d: 2-D JONSWAP tank 50 m x 5 m, flap, 512 components, "
+                    "n1=1025 n3=65 M=5 p1=5, RK4(5) tol 1e-7",
+    "regular_2d": "regular_2d: 2-D regular wave T=1.0 s H=0.05 m, tank 50 m x 5 m, flap hinged 2.0 m above "
+                  "the bottom, 3 s ramp, n1=257 n3=33 M=3 p1=3, RK4(5) tol 1e-7",
+}
+
+
 def _workload_config(w, info=None):
-    cfg = {"workload": "irregular_2d: 2-D JONSWAP tank 50 m x 5 m, flap, 512 components, "
-                       "n1=1025 n3=65 M=5 p1=5, RK4(5) tol 1e-7",
+    cfg = {"workload": WORKLOAD_TEXT[w["name"]],
            "n1": w["n1"], "n3": w["n3"], "mHOS": w["mHOS"], "p1": w["p1"],
-           "wave_components": 512, "seed": 513,
            "l2": "flushed between steps (256 MiB write outside the timed events)",
            "parallelism": "replicas"}
+    if w["name"] == "irregular_2d":
+        cfg.update({"wave_components": 512, "seed": 513})
     if info is not None:
         cfg["nd1"] = info["nd1"]
         cfg["dt_nondim"] = info["delt"]
@@ -248,7 +260,7 @@ def cpu_baseline(w, budget_s=15.0, max_steps=400):
         n += 1
     el = time.perf_counter() - t0
     return {"value": n / el, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{n} RK4(5) steps of the irregular_2d tank (n1=1025, M=5) with the numpy/scipy "
+            "sample": f"{n} RK4(5) steps of the {w['name']} tank (n1={w['n1']}, M={w['mHOS']}) with the numpy/scipy "
                       f"oracle, {el:.1f} s on one host core"}
 
 
@@ -376,7 +388,7 @@ def run_cuda(args, w):
     fp64_peak = hosnwt.fp64_peak_gflops()
     fp64_flops = 2.0 * _two_level_fmas(nd1 - 1, n1, nd1) * 4
     fp64_achieved = fp64_flops / (ms * 1e-3) / 1e9
-    traffic = _profile_traffic()
+    traffic = _profile_traffic() if w["name"] == "irregular_2d" else None
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -687,7 +699,7 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cuda", choices=("cuda", "reference"))
-    ap.add_argument("--workload", default="irregular_2d", choices=("irregular_2d", "ensemble", "directional_3d", "tc_gemm"))
+    ap.add_argument("--workload", default="irregular_2d", choices=("irregular_2d", "regular_2d", "ensemble", "directional_3d", "tc_gemm"))
     ap.add_argument("--sim-seconds", type=float, default=1.0, help="ensemble: simulated seconds per tank")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one step inside a cudaProfilerStart/Stop range (for ncu) and exit")
@@ -715,7 +727,7 @@ def main():
         run_3d(args)
         return
     with tempfile.TemporaryDirectory() as tmp:
-        w = workloads.irregular_2d(tmp)
+        w = workloads.regular_2d() if args.workload == "regular_2d" else workloads.irregular_2d(tmp)
         if args.impl == "reference":
             run_reference(args, w)
         else:

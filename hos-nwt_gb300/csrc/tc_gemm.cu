@@ -227,27 +227,35 @@ __global__ void __launch_bounds__(kThreads, 1)
       if (!ready) (void)mbar_wait(&done_bar, 0u);
     }
   } else {
-    const int row = m0 + warp * 32 + lane;
+    // Every MMA has completed, so the stage ring is free: each warp passes
+    // its 32 accumulator rows through a 32 x 16 shared-memory tile (rows
+    // padded to 17 words: conflict-free both ways) so that a half-warp then
+    // reads, combines and stores 16 consecutive columns of one row.
+    float* tile = reinterpret_cast<float*>(base) + warp * (32 * 17);
+    const int half = lane >> 4, cl = lane & 15;
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 16) {
       float v[16];
       tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-      if (row < g.M) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int col = n0 + c0 + i;
-          if (col < g.N) {
-            float x = v[i];
-            if (g.bias) x += g.bias[col];
-            if (g.Dadd) x += g.Dadd[(long long)row * g.ldd + col];
-            if (g.act == 1) x = gelu(x);
-            if (g.d_bf16)
-              ((__nv_bfloat16*)g.D)[(long long)row * g.ldd + col] = __float2bfloat16(x);
-            else
-              ((float*)g.D)[(long long)row * g.ldd + col] = x;
-          }
+      for (int i = 0; i < 16; ++i) tile[lane * 17 + i] = v[i];
+      __syncwarp();
+      const int col = n0 + c0 + cl;
+      const float bcol = (g.bias && col < g.N) ? g.bias[col] : 0.0f;
+#pragma unroll 4
+      for (int r = half; r < 32; r += 2) {
+        const int row = m0 + warp * 32 + r;
+        if (row < g.M && col < g.N) {
+          float x = tile[r * 17 + cl] + bcol;
+          if (g.Dadd) x += g.Dadd[(long long)row * g.ldd + col];
+          if (g.act == 1) x = gelu(x);
+          if (g.d_bf16)
+            ((__nv_bfloat16*)g.D)[(long long)row * g.ldd + col] = __float2bfloat16(x);
+          else
+            ((float*)g.D)[(long long)row * g.ldd + col] = x;
         }
       }
+      __syncwarp();
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
