@@ -648,6 +648,87 @@ def run_profile_gemm(args):
     print(json.dumps({"profile_gemm": [s[0] for s in GEMM_SHAPES]}), flush=True)
 
 
+def run_surrogate(args):
+    """The surrogate for the orders 4..7 of W (pattern 4), offline: a 2-D
+    irregular tank (n1 = 513, M = 7, p1 = 7) runs on the plain FP64 GPU
+    path; snapshots of eta, phizm(1..3) and phizm(4..7) (hosnwt_hos_terms)
+    are taken every 0.1 s from 5 to 45 s of one wave realisation (seed 513)
+    for training and from 20 to 40 s of another (seed 600) for testing.  A
+    4-layer, 32-channel FNO with 64 cosine modes is trained on the tensor
+    cores (BF16 in, FP32 accumulate) and its held-out error is reported,
+    relative to the orders 4..7 part and to the whole W."""
+    import torch
+    import hosnwt
+    import surrogate
+
+    def make(seed, tmp):
+        w = workloads.irregular_2d(tmp, seed=seed, n1=513, n3=33, mHOS=7, p1=7, T_stop=60.0)
+        return hosnwt.Tank(w["inp"], w["n1"], 1, w["n3"], w["mHOS"], w["p1"], 1, probes=w["probes"],
+                           wave_dir=w["wave_dir"])
+
+    t0 = time.perf_counter()
+    with tempfile.TemporaryDirectory() as tmp:
+        tank = make(513, tmp)
+    nd = tank.info()["nd1"]
+    Xtr, Ytr, Wtr, _ = surrogate.collect(tank, 5.0, 45.0, 0.1, tank.info()["delt"])
+    # plain M = 7 step time on this tank (device-resident, CUDA events)
+    h = tank.info()["delt"]
+    for _ in range(3):
+        tank.step(h)
+    torch.cuda.synchronize()
+    ms0 = tank.info()["device_ms"]
+    for _ in range(20):
+        tank.step(h)
+    step_ms = (tank.info()["device_ms"] - ms0) / 20
+    tank.close()
+    with tempfile.TemporaryDirectory() as tmp:
+        tank = make(600, tmp)
+    Xte, Yte, Wte, _ = surrogate.collect(tank, 20.0, 40.0, 0.1, tank.info()["delt"])
+    tank.close()
+    t_collect = time.perf_counter() - t0
+    model = surrogate.build_fno(nd)
+    iters = max(args.steps, 1) * 40
+    losses, t_train, sc = surrogate.train(model, Xtr, Ytr, iters=iters, batch=32, lr=3e-3)
+    pred = surrogate.predict(model, Xte, sc)
+    err = pred - Yte
+    rel_hi = float(np.linalg.norm(err) / np.linalg.norm(Yte))
+    rel_w = float(np.linalg.norm(err) / np.linalg.norm(Wte))
+    share = float(np.linalg.norm(Yte) / np.linalg.norm(Wte))
+    per_snap = np.linalg.norm(err, axis=1) / np.maximum(np.linalg.norm(Wte, axis=1), 1e-300)
+    # inference time of one field and of the five of an RK4(5) step
+    xs, ys = sc
+    times = {}
+    for b in (1, 5):
+        Xt = torch.tensor(Xte[:b] / xs, dtype=torch.float32, device="cuda")
+        with torch.no_grad():
+            for _ in range(3):
+                model(Xt)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(20):
+                model(Xt)
+            e1.record()
+            torch.cuda.synchronize()
+        times[b] = e0.elapsed_time(e1) / 20
+    surrogate.check_kernel_flags()
+    print(json.dumps({
+        "metric": "surrogate (orders 4..7 of W): held-out relative error", "value": rel_hi,
+        "unit": "||pred - W_4..7|| / ||W_4..7||", "higher_is_better": False, "dtype": "bf16 in, f32 accumulate",
+        "data": "synthetic: snapshots of the plain FP64 GPU solver",
+        "config": {"workload": "surrogate: 2-D irregular JONSWAP tank, n1=513 n3=33 M=7 p1=7, Hs=0.10 m Tp=1.4 s; "
+                               "train seed 513 t=5..45 s, test seed 600 t=20..40 s, every 0.1 s",
+                   "nd1": nd, "fno": "4 layers, 32 channels, 64 cosine modes", "train_iters": iters, "batch": 32},
+        "snapshots": {"train": int(Xtr.shape[0]), "test": int(Xte.shape[0])},
+        "error_relative_to_W": rel_w, "orders_4_7_share_of_W": share,
+        "per_snapshot_error_relative_to_W": {"median": float(np.median(per_snap)), "max": float(np.max(per_snap))},
+        "loss": {"first10": float(np.mean(losses[:10])), "last10": float(np.mean(losses[-10:]))},
+        "seconds": {"collect": t_collect, "train": t_train},
+        "inference_ms": {"one_field": times[1], "five_fields": times[5]},
+        "plain_m7_step_ms": step_ms,
+        "note": "offline: the surrogate is not used inside the time loop"}), flush=True)
+
+
 def run_profile_step(args, w):
     """One step of a tank between cudaProfilerStart / cudaProfilerStop, after
     `--warmup` untimed steps, for `ncu --profile-from-start off`: the capture
@@ -699,7 +780,8 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cuda", choices=("cuda", "reference"))
-    ap.add_argument("--workload", default="irregular_2d", choices=("irregular_2d", "regular_2d", "ensemble", "directional_3d", "tc_gemm"))
+    ap.add_argument("--workload", default="irregular_2d", choices=("irregular_2d", "regular_2d", "ensemble", "directional_3d", "tc_gemm",
+                                                   "surrogate"))
     ap.add_argument("--sim-seconds", type=float, default=1.0, help="ensemble: simulated seconds per tank")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one step inside a cudaProfilerStart/Stop range (for ncu) and exit")
@@ -708,6 +790,9 @@ def main():
     args = ap.parse_args()
     if args.workload == "tc_gemm":
         run_profile_gemm(args) if args.profile_step else run_tc_gemm(args)
+        return
+    if args.workload == "surrogate":
+        run_surrogate(args)
         return
     if args.profile_roofline:
         with tempfile.TemporaryDirectory() as tmp:

@@ -1582,6 +1582,21 @@ extern "C" int hosnwt_solveHOS2(hosnwt_ctx* h, const double* const* y, double* c
   return cuda_check(c, "solveHOS2");
 }
 
+extern "C" int hosnwt_hos_terms(hosnwt_ctx* h, double* eta_big, double* phizm) {
+  if (!h || !eta_big || !phizm) return HOSNWT_ERR_ARG;
+  Ctx& c = h->c;
+  const size_t nB = (size_t)c.P.nd1 * c.P.nd2;
+  if (c.n_rhs == 0) return fail(c, HOSNWT_ERR_ARG, "hos_terms: no right-hand side has been evaluated");
+  // the scratch fields of the last right-hand side enqueued on this context
+  cudaStreamSynchronize(c.st);
+  cudaMemcpyAsync(eta_big, c.d.etapm[0], nB * sizeof(double), cudaMemcpyDeviceToHost, c.st);
+  for (int m = 1; m <= c.P.M; ++m)
+    cudaMemcpyAsync(phizm + (size_t)(m - 1) * nB, c.d.phizm[m], nB * sizeof(double), cudaMemcpyDeviceToHost,
+                    c.st);
+  cudaStreamSynchronize(c.st);
+  return cuda_check(c, "hos_terms");
+}
+
 extern "C" int hosnwt_transform(hosnwt_ctx* h, int grid, int dir, int csx, int csy, const double* in,
                                 double* out) {
   if (!h || !in || !out || grid < 0 || grid > 2 || (dir != 1 && dir != -1)) return HOSNWT_ERR_ARG;

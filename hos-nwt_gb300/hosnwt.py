@@ -94,6 +94,7 @@ def load_library(path=LIB_PATH):
     lib.hosnwt_solveHOS2.argtypes = [vp, P(dp), P(dp), ctypes.c_double, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_double]
     lib.hosnwt_transform.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp, dp]
+    lib.hosnwt_hos_terms.argtypes = [vp, dp, dp]
     lib.hosnwt_advance_many.argtypes = [P(vp), ctypes.c_int, dp, dp]
     lib.hosnwt_time_transform.argtypes = [vp] + [ctypes.c_int] * 10 + [dp]
     lib.hosnwt_fp64_peak.argtypes = [dp]
@@ -255,6 +256,18 @@ class Tank:
         self._check(rc, "solveHOS2")
         return ks
 
+    def hos_terms(self):
+        """eta on the dealiased grid and the M vertical-velocity terms
+        phizm(:,:,1..M) of the last right-hand side evaluated on this tank
+        (hosnwt_hos_terms): arrays (nd1, nd2) and (M, nd1, nd2)."""
+        inf = self.info()
+        nd1, nd2 = inf["nd1"], inf["nd2"]
+        eta = np.zeros((nd1, nd2), order="F")
+        phizm = np.zeros(self.M * nd1 * nd2)
+        self._check(self.lib.hosnwt_hos_terms(self._h, _dptr(eta), _dptr(phizm)), "hos_terms")
+        return eta, np.stack([phizm[m * nd1 * nd2:(m + 1) * nd1 * nd2].reshape((nd1, nd2), order="F")
+                              for m in range(self.M)])
+
     def transform(self, grid, direction, csx, csy, a):
         """SPACE_2_FOURIER (direction=+1) / FOURIER_2_SPACE (-1) on the
         'n', 'big' or 'add' grid."""
@@ -370,8 +383,13 @@ def tc_gemm(A, B, bias=None, act=0, Dadd=None, out=None, out_bf16=False, err=Non
         out = torch.empty((M, N), dtype=torch.bfloat16 if out_bf16 else torch.float32, device=A.device)
     if err is None:
         err = torch.zeros(1, dtype=torch.int32, device=A.device)
+    # the row stride of a one-row matrix is arbitrary in PyTorch (a transposed
+    # column reports 1); the kernel never steps over it, so pass the row length
+    lda = A.stride(0) if M > 1 else K
+    ldb = B.stride(0) if N > 1 else K
+    ldd = out.stride(0) if M > 1 else N
     rc = load_library().hosnwt_tc_gemm_bf16(
-        A.data_ptr(), A.stride(0), B.data_ptr(), B.stride(0), out.data_ptr(), out.stride(0),
+        A.data_ptr(), lda, B.data_ptr(), ldb, out.data_ptr(), ldd,
         1 if out.dtype == torch.bfloat16 else 0, M, N, K, bias.data_ptr() if bias is not None else None,
         int(act), Dadd.data_ptr() if Dadd is not None else None, err.data_ptr(), stream)
     if rc != HOSNWT_OK:

@@ -157,6 +157,15 @@ int hosnwt_probes(hosnwt_ctx* ctx, double* out);
 int hosnwt_solveHOS2(hosnwt_ctx* ctx, const double* const* y, double* const* k,
                      double delta_t, double time, double alpha_prev, double pos_top_prev);
 
+/* Snapshot hook for training a surrogate of the high HOS orders: the
+ * fields of the last right-hand side evaluated on this context (stage 5 of
+ * the last hosnwt_step, or the last hosnwt_solveHOS2), on the dealiased
+ * grid nd1 x nd2, column-major: eta_big = eta (etapm(:,:,1)) and phizm =
+ * the M vertical-velocity terms phizm(:,:,1..M) of HOSphis_modes
+ * (resol_HOS.f90:665-915), order after order (M * nd1 * nd2 doubles), each
+ * after its partial dealiasing.  Synchronises the context's stream. */
+int hosnwt_hos_terms(hosnwt_ctx* ctx, double* eta_big, double* phizm);
+
 /* Test hook: one spectral transform on host arrays.
  * grid: 0 free surface (n1 x n2), 1 dealiased (nd1 x nd2), 2 wavemaker
  * (n3_add x n2).  dir: +1 SPACE_2_FOURIER, -1 FOURIER_2_SPACE.

@@ -1424,6 +1424,9 @@ class Tank:
                 phimext = self.dealias(iHOS + 1, phimext)
                 self._tick(1)
                 aHOS[iHOS + 1] = F.S2F_big(phimext)
+        # kept for the per-order snapshot check of the GPU hook hosnwt_hos_terms
+        self.last_phizm = [None] + [p.copy() for p in phizm[1:]]
+        self.last_eta_big = etapm[0].copy()
         res = {}
         if M >= 2:
             phizMm1 = np.zeros((self.nd1, self.nd2))
