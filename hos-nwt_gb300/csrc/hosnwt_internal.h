@@ -7,6 +7,7 @@
 
 #include <complex>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -25,6 +26,31 @@ __device__ __forceinline__ void pdl_wait() {
   asm volatile("griddepcontrol.wait;\n\tgriddepcontrol.launch_dependents;" ::: "memory");
 #endif
 }
+
+// Runs a set-up action once per device (thread-safe).  Kernel attributes
+// such as the dynamic shared-memory limit belong to a device, so a process
+// that drives two GPUs sets them on each; host threads making their first
+// launch at the same time are serialised by the mutex.
+struct PerDeviceOnce {
+  std::mutex m;
+  unsigned long long done[4] = {0, 0, 0, 0};  // one bit per device ordinal < 256
+  template <typename F>
+  void run(F&& f) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+    std::lock_guard<std::mutex> g(m);
+    if (dev < 0 || dev >= 256) {
+      f();
+      return;
+    }
+    unsigned long long& w = done[dev >> 6];
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(w & bit)) {
+      f();
+      w |= bit;
+    }
+  }
+};
 
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,

@@ -31,6 +31,8 @@ constexpr int kCntLen = 4096;                                 // arrival counter
 constexpr long long kScratchLen = kTableLen + kPartLen + kCntLen / 2;
 
 static __device__ __align__(256) double g_noalloc_scratch[kScratchLen];
+// the regions are disjoint at the largest length: the table holds m = 0..D
+static_assert(kTableLen >= kNoallocMaxN, "cos table shorter than the longest transform");
 
 std::mutex g_setup_mutex;
 double* g_scratch_addr[256] = {};  // device address of the array, per device
@@ -49,11 +51,18 @@ int scratch_address(double** out) {
   return HOSNWT_OK;
 }
 
-// quarter-wave table cos(pi m / (2D)), m = 0..D, built on the device
+// quarter-wave table cos(pi m / (2D)), m = 0..D, built on the device; the
+// exact values at m = D (0) and m = 2D/3 (1/2) are set as the context's
+// host-built table sets them.  Other entries may differ from that table in
+// the last bit, so results may differ from hosnwt_transform's in the last
+// bits (far inside the transform tolerance).
 __global__ void k_noalloc_table(double* q, int D) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m > D) return;
-  q[m] = (m == D) ? 0.0 : cospi((double)m / (2.0 * (double)D));
+  double v = cospi((double)m / (2.0 * (double)D));
+  if (m == D) v = 0.0;
+  if (D % 3 == 0 && 3 * m == 2 * D) v = 0.5;
+  q[m] = v;
 }
 
 }  // namespace
@@ -70,15 +79,20 @@ extern "C" int hosnwt_transform_noalloc(int dir, int cs, int n, int nlines, cons
   int rc = scratch_address(&base);
   if (rc != HOSNWT_OK) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the status returned below covers this call's own launches: clear a
+  // launch error an earlier call left on this host thread
+  (void)cudaGetLastError();
   double* q = base;
   double* part = base + kTableLen;
   unsigned int* cnt = reinterpret_cast<unsigned int*>(base + kTableLen + kPartLen);
   int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return HOSNWT_ERR_CUDA;
   // the counters must start at zero; the table is rebuilt for this length
-  cudaMemsetAsync(cnt, 0, sizeof(unsigned int) * kCntLen, st);
+  if (cudaMemsetAsync(cnt, 0, sizeof(unsigned int) * kCntLen, st) != cudaSuccess) return HOSNWT_ERR_CUDA;
   k_noalloc_table<<<(n + 255) / 256, 256, 0, st>>>(q, n - 1);
+  if (cudaGetLastError() != cudaSuccess) return HOSNWT_ERR_CUDA;
   Tables tb{};
   tb.n1 = n;
   tb.n2 = 1;

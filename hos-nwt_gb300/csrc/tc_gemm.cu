@@ -135,7 +135,10 @@ struct GemmArgs {
   const float* bias;   // N entries or null
   int act;             // 0 none, 1 GELU
   const float* Dadd;   // optional FP32 M x N (ldd) added before the activation
-  unsigned* err;       // error flag (1: a wait timed out)
+  unsigned* err;       // error flag (1: a wait timed out; 2: the wait for the
+                       // MMAs to finish timed out too, so the CTA exited
+                       // without freeing its tensor memory: treat the
+                       // context as unusable)
 };
 
 template <int BN>
@@ -150,6 +153,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ uint64_t full_bar[kStages], empty_bar[kStages], done_bar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
+  __shared__ int keep_tmem;  // 1: MMAs may still write the accumulator
   __shared__ int n_issued, n_consumed;  // stages loaded by TMA / read by the MMAs
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
@@ -162,6 +166,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     mbar_init(&done_bar, 1);
     abort_flag = 0;
+    keep_tmem = 0;
     n_issued = n_consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -224,7 +229,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       // the MMAs finish before their tensor memory is freed
       for (int kb = n_consumed; kb < n_issued; ++kb)
         (void)mbar_wait(&full_bar[kb % kStages], (unsigned)((kb / kStages) & 1));
-      if (!ready) (void)mbar_wait(&done_bar, 0u);
+      if (!ready && !mbar_wait(&done_bar, 0u)) {
+        // the MMAs did not report completion: freeing their tensor memory
+        // now could let another CTA's accumulator be overwritten
+        keep_tmem = 1;
+        atomicExch(g.err, 2u);
+      }
     }
   } else {
     // Every MMA has completed, so the stage ring is free: each warp passes
@@ -260,7 +270,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0)
+  if (warp == 0 && !keep_tmem)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN < 32 ? 32 : BN)
                  : "memory");
 }
@@ -298,11 +308,8 @@ bool make_map(CUtensorMap* m, const void* ptr, int rows, int cols, long long ld,
 template <int BN>
 cudaError_t launch_gemm(const CUtensorMap& ma, const CUtensorMap& mb, const GemmArgs& g, cudaStream_t st) {
   const size_t smem = 1024 + (size_t)kStages * (kBM + BN) * kBK * 2;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_tc_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  static PerDeviceOnce attr;
+  attr.run([&] { cudaFuncSetAttribute(k_tc_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); });
   const dim3 grid((g.M + kBM - 1) / kBM, (g.N + BN - 1) / BN);
   k_tc_gemm<BN><<<grid, kThreads, smem, st>>>(ma, mb, g);
   return cudaGetLastError();

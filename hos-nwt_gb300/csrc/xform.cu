@@ -1449,15 +1449,14 @@ bool ytl_can_pair(int D, int A, int B, int nout, int N) {
 void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
   b.early = early ? 1 : 0;
   for (int i = 0; i < b.njobs; ++i) g_xform_fmas += (double)b.job[i].nlines * two_level_fmas(b.job[i]);
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_set;
+  attr_set.run([&] {
     for (int nj : {1, 2, 4, 8, kMaxJobs})
       with_capacity(nj, [&](auto c) {
         allow_smem(two_level_pass1<decltype(c)::value>);
         allow_smem(two_level_pass2<decltype(c)::value>);
       });
-    attr_set = true;
-  }
+  });
   // pass 1: one k' per cluster while that gives fewer than two clusters per
   // SM, else up to 8 k' per cluster so that each CTA reuses its staged row;
   // the j1 sums are split over a cluster when there are few rows
@@ -1495,12 +1494,11 @@ void launch_two_level(AxisBatch& b, int nsm, bool early, cudaStream_t st) {
   int minl = 1 << 30;
   for (int i = 0; i < b.njobs; ++i) minl = std::min(minl, b.job[i].nlines);
   if (minl >= 16) {
-    static bool attr_l = false;
-    if (!attr_l) {
+    static PerDeviceOnce attr_l;
+    attr_l.run([&] {
       for (int nj : {1, 2, 4, 8, kMaxJobs})
         with_capacity(nj, [&](auto c) { allow_smem(two_level_pass2_lines<decltype(c)::value>); });
-      attr_l = true;
-    }
+    });
     long long blocks = 0;
     for (int i = 0; i < b.njobs; ++i) blocks += (long long)b.job[i].nlines * ((p2_lanes(b.job[i]) + 31) / 32);
     const int lpc = (int)std::min<long long>(16, std::max<long long>(4, blocks / (4LL * std::max(nsm, 1))));
@@ -1575,12 +1573,11 @@ bool launch_two_level_fused(AxisBatch& b, int nsm, bool early, cudaStream_t st) 
   size_t smem = 0;
   for (int i = 0; i < b.njobs; ++i) smem = std::max(smem, fused_smem(b.job[i], nsplit));
   if (smem > 200 * 1024) return false;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_set;
+  attr_set.run([&] {
     for (int nj : {1, 2, 4, 8, kMaxJobs})
       with_capacity(nj, [&](auto c) { allow_smem(two_level_fused<decltype(c)::value>); });
-    attr_set = true;
-  }
+  });
   b.early = early ? 1 : 0;
   int total = 0;
   for (int i = 0; i < b.njobs; ++i) {
@@ -1666,12 +1663,11 @@ void launch_batch_x(AxisBatch& b, const Tables& tb, cudaStream_t st) {
   size_t smem = 0;
   for (int i = 0; i < b.njobs; ++i)
     smem = std::max(smem, sizeof(double) * ((size_t)b.job[i].D + 1 + 2 * (size_t)kMaxPairChunk));
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_set;
+  attr_set.run([&] {
     for (int nj : {1, 2, 4, 8, kMaxJobs})
       with_capacity(nj, [&](auto c) { allow_smem(axis_pass_lanes_k<decltype(c)::value>); });
-    attr_set = true;
-  }
+  });
   if (total > 0)
     with_capacity(b.njobs, [&](auto c) {
       constexpr int NJ = decltype(c)::value;
@@ -1703,15 +1699,14 @@ void pick_factors_y(int D, int nin, int nout, int* Aout, int* Bout) {
 void launch_ytl(AxisBatch& b, bool early, cudaStream_t st) {
   b.early = early ? 1 : 0;
   for (int i = 0; i < b.njobs; ++i) g_xform_fmas += (double)b.job[i].nlines * y_two_level_fmas(b.job[i]);
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_set;
+  attr_set.run([&] {
     for (int nj : {1, 2, 4, 8, kMaxJobs})
       with_capacity(nj, [&](auto c) {
         allow_smem(ytl_pass1<decltype(c)::value>);
         allow_smem(ytl_pass2<decltype(c)::value>);
       });
-    attr_set = true;
-  }
+  });
   int total = 0;
   size_t smem1 = 0, smem2 = 0;
   for (int i = 0; i < b.njobs; ++i) {

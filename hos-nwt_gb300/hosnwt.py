@@ -153,6 +153,9 @@ def read_input(path):
     return out
 
 
+NOALLOC_MAX_N = 16385  # HOSNWT_NOALLOC_MAX_N of include/hosnwt.h
+
+
 def transform_noalloc(direction, cs, n, nlines, in_ptr, out_ptr, stream=0):
     """hosnwt_transform_noalloc on device pointers (integers): the transform
     for callers that cannot allocate device memory; see include/hosnwt.h."""

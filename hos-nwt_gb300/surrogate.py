@@ -70,7 +70,11 @@ def gemm_bf16(A, B):
 def check_kernel_flags():
     """Raise if a wait inside the tensor-core kernel timed out."""
     for t in _ERR.values():
-        if int(t.item()) != 0:
+        v = int(t.item())
+        if v == 2:
+            raise hosnwt.HosError("tc_gemm: the MMAs never reported completion; their tensor memory was "
+                                  "left allocated, so the CUDA context must not be used further")
+        if v != 0:
             raise hosnwt.HosError("tc_gemm: a bounded wait timed out")
 
 

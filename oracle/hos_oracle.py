@@ -234,21 +234,33 @@ def TF_adim_new(typ, k, hinge):
 # ----------------------------------------------------------------------------
 # r2r transforms with FFTW conventions (fourier_FFTW.f90:89-653)
 # ----------------------------------------------------------------------------
+# Threads of the scipy transforms (1: single-threaded, like the Fortran
+# reference).  The benchmark's CPU arm raises it to the host's core count.
+_WORKERS = 1
+
+
+def set_workers(n):
+    """Threads used by every scipy.fft call of the oracle."""
+    global _WORKERS
+    _WORKERS = max(1, int(n))
+
+
 def _r2r(a, axis, kind):
     """Unnormalised FFTW r2r along `axis`.  kind: REDFT00, RODFT00, REDFT01,
     REDFT10, RODFT01, RODFT10.  scipy's norm=None types match FFTW exactly."""
+    w = _WORKERS
     if kind == "REDFT00":
-        return sfft.dct(a, type=1, axis=axis)
+        return sfft.dct(a, type=1, axis=axis, workers=w)
     if kind == "RODFT00":
-        return sfft.dst(a, type=1, axis=axis)
+        return sfft.dst(a, type=1, axis=axis, workers=w)
     if kind == "REDFT10":
-        return sfft.dct(a, type=2, axis=axis)
+        return sfft.dct(a, type=2, axis=axis, workers=w)
     if kind == "REDFT01":
-        return sfft.dct(a, type=3, axis=axis)
+        return sfft.dct(a, type=3, axis=axis, workers=w)
     if kind == "RODFT10":
-        return sfft.dst(a, type=2, axis=axis)
+        return sfft.dst(a, type=2, axis=axis, workers=w)
     if kind == "RODFT01":
-        return sfft.dst(a, type=3, axis=axis)
+        return sfft.dst(a, type=3, axis=axis, workers=w)
     raise ValueError(kind)
 
 
@@ -1248,12 +1260,29 @@ class Tank:
         kx_add = self.kx_add
         cy_mat = np.cos(self.ky[:, None] * self.cy[None, :])   # (j2, i2)
         sy_mat = np.sin(self.ky[:, None] * self.cy[None, :])
-        # B[q](i1, i2, i3) = sum_j2 a(i3,j2) tab(i1,j2,i3) trig(j2,i2)
-        B_phi = np.einsum("jk,ijk,jl->ilk", a_add.T, self.csh_add_x, cy_mat)
-        B_t = np.einsum("jk,ijk,jl->ilk", da_add.T, self.csh_add_x, cy_mat)
-        B_x = np.einsum("jk,ijk,jl->ilk", a_add.T, self.k_add_sh_add_x, cy_mat)
-        B_y = np.einsum("jk,ijk,jl->ilk", a_add.T, self.kycsh_add_x, sy_mat)
-        B_z = np.einsum("jk,ijk,jl->ilk", a_add.T, self.kx_add_csh_add_x, cy_mat)
+        # B[q](i1, i2, i3) = sum_j2 a(i3,j2) tab(i1,j2,i3) trig(j2,i2): the
+        # elementwise product first, then the j2 sum as one matrix product
+        n1, n2, n3a = self.csh_add_x.shape[0], cy_mat.shape[0], a_add.shape[0]
+
+        def ysum(a, tab, trig):
+            p = a.T[None, :, :] * tab                      # (i1, j2, i3)
+            if n2 > 2:
+                # ky(j2) y(i2) = pi j2 i2 / (n2 - 1): the sums are the
+                # REDFT00 (cos) / RODFT00 on the interior (sin) along j2
+                if trig is cy_mat:
+                    sgn = np.where(np.arange(n2) % 2 == 0, 1.0, -1.0)[None, :, None]
+                    return 0.5 * (_r2r(p, 1, "REDFT00") + p[:, :1, :] + sgn * p[:, -1:, :])
+                out = np.zeros_like(p)
+                out[:, 1:-1, :] = 0.5 * _r2r(p[:, 1:-1, :], 1, "RODFT00")
+                return out
+            q = p.transpose(0, 2, 1).reshape(n1 * n3a, n2)
+            return (q @ trig).reshape(n1, n3a, trig.shape[1]).transpose(0, 2, 1)
+
+        B_phi = ysum(a_add, self.csh_add_x, cy_mat)
+        B_t = ysum(da_add, self.csh_add_x, cy_mat)
+        B_x = ysum(a_add, self.k_add_sh_add_x, cy_mat)
+        B_y = ysum(a_add, self.kycsh_add_x, sy_mat)
+        B_z = ysum(a_add, self.kx_add_csh_add_x, cy_mat)
         arg = kx_add[None, None, :] * (eta[:, :, None] + 1.0)
         c = np.cos(arg)
         s = np.sin(arg)

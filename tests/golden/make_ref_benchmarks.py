@@ -1,6 +1,6 @@
 """Fixtures from the reference's own result files.
 
-python tests/golden/make_ref_benchmarks.py [REFERENCE_ROOT]
+python tests/golden/make_ref_benchmarks.py REFERENCE_ROOT
 
 Reads the probe records that the reference HOS-NWT wrote in
 Benchmark/Sloshing, Benchmark/Regular_3D, Benchmark/Irreg_2D and
@@ -35,7 +35,10 @@ def read_xy(path):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_ref_benchmarks.py REFERENCE_ROOT "
+                         "(the HOS-NWT source tree holding Benchmark/)")
+    root = sys.argv[1]
     bench = os.path.join(root, "Benchmark")
     # Sloshing: 4th natural mode, 0.2 m, linear (M = 1), 129 modes, 20 Hz output
     # (configuration from the Ref_data input echo)

@@ -45,3 +45,10 @@ def test_missing_input_is_an_error(lib):
     import hosnwt
     with pytest.raises(RuntimeError):
         hosnwt.read_input("/nonexistent/input_HOS-NWT.dat")
+
+
+def test_noalloc_limit_matches_header():
+    import hosnwt
+    txt = open(os.path.join(ROOT, "include", "hosnwt.h")).read()
+    m = re.search(r"#define\s+HOSNWT_NOALLOC_MAX_N\s+(\d+)", txt)
+    assert m and int(m.group(1)) == hosnwt.NOALLOC_MAX_N

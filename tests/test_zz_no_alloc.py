@@ -43,6 +43,32 @@ def test_noalloc_matches_transform(lib):
                 assert _rel(got[l], ref) < 1e-13 * np.sqrt(n), (rep, n, grid, direction, cs, l)
 
 
+def test_noalloc_many_lines_and_longest(lib):
+    """More lines than one launch takes (the line-group loop runs three
+    times, reusing the shared counters and partial sums), and the longest
+    length the fixed array admits, against the oracle's transform."""
+    torch = pytest.importorskip("torch")
+    import hosnwt
+    from oracle.hos_oracle import Fourier
+
+    stream = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(9)
+    for n, direction, cs, nlines in ((771, 1, "cos", 40), (771, -1, "sin", 40),
+                                     (hosnwt.NOALLOC_MAX_N, 1, "cos", 1), (hosnwt.NOALLOC_MAX_N, -1, "sin", 2)):
+        F = Fourier(n, 1, n, 1, 4)
+        host = rng.standard_normal((nlines, n))
+        d_in = torch.from_numpy(host).cuda()
+        for rep in range(2):
+            d_out = torch.full_like(d_in, np.nan)
+            hosnwt.transform_noalloc(direction, cs, n, nlines, d_in.data_ptr(), d_out.data_ptr(), stream)
+            torch.cuda.synchronize()
+            got = d_out.cpu().numpy()
+            for l in range(nlines):
+                a = host[l][:, None]
+                ref = (F.S2F(a, cs, "cos") if direction == 1 else F.F2S(a, cs, "cos"))[:, 0]
+                assert _rel(got[l], ref) < 1e-13 * np.sqrt(n), (rep, n, direction, cs, l)
+
+
 def test_noalloc_rejects_sizes(lib):
     import hosnwt
     for n in (4, 16386):
