@@ -1,8 +1,11 @@
-"""Benchmark of the HOS-NWT hot path: RK4(5) steps per second of the 2-D
-irregular tank (n1 = 1025, n3 = 65, M = 5, p1 = 5; 512-component JONSWAP,
-Hs = 0.10 m, Tp = 1.4 s; synthetic seeded phases).
+"""Benchmark of the HOS-NWT hot path: RK4(5) steps per second of one wave
+tank, by default the 3-D directional tank (513 x 257 modes, n3 = 33, M = 5,
+p1 = p2 = 4; 50 m x 30 m x 5 m, snake flap, JONSWAP Hs = 0.08 m, Tp = 1.2 s,
+cos^2s spreading s = 10; synthetic seeded phases and directions), the
+largest benchmark configuration the plain FP64 path runs on one GPU.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cuda|reference]
+                  [--workload directional_3d|irregular_2d|regular_2d|...]
 
 One step = one adaptive RK4(5) step of runge4_adapt2 (five nonlinear
 right-hand sides, error estimate) at the CFL-limited step size, followed by
@@ -15,11 +18,13 @@ results inside each timed call).  Under torchrun every rank runs its own
 replica tank (the path does not shard); value = total steps/s.
 
 --impl reference times the CPU restatement of the reference (the oracle:
-numpy/scipy FP64, single thread like the Fortran reference) on the same tank.
+numpy/scipy FP64, its transforms threaded over every host core; the Fortran
+reference cannot be built on these hosts) on the same tank.
 
-Other workloads (--workload): regular_2d (the 2-D regular-wave tank, n1 =
-257, M = 3), directional_3d (513 x 257, M = 5), ensemble (64 independent
-2-D tanks), tc_gemm (the surrogate's tensor-core contraction).
+Other workloads (--workload): irregular_2d (2-D JONSWAP tank, n1 = 1025,
+M = 5), regular_2d (2-D regular-wave tank, n1 = 257, M = 3), ensemble (64
+independent 2-D tanks), tc_gemm (the surrogate's tensor-core contraction),
+surrogate (the offline FNO).
 """
 from __future__ import annotations
 
@@ -48,25 +53,49 @@ UNIT = "steps/s"
 
 
 WORKLOAD_TEXT = {
+    "directional_3d": "directional_3d: 3-D directional JONSWAP tank 50 m x 30 m x 5 m, snake flap hinged 2.0 m "
+                      "above the bottom, Hs=0.08 m Tp=1.2 s gamma=3.3, cos^2s spreading s=10, n1=513 n2=257 "
+                      "n3=33 M=5 p1=p2=4, RK4(5) tol 1e-7",
     "irregular_2d": "irregular_2d: 2-D JONSWAP tank 50 m x 5 m, flap, 512 components, "
                     "n1=1025 n3=65 M=5 p1=5, RK4(5) tol 1e-7",
     "regular_2d": "regular_2d: 2-D regular wave T=1.0 s H=0.05 m, tank 50 m x 5 m, flap hinged 2.0 m above "
                   "the bottom, 3 s ramp, n1=257 n3=33 M=3 p1=3, RK4(5) tol 1e-7",
 }
+SINGLE_TANK = ("directional_3d", "irregular_2d", "regular_2d")
 
 
-def _workload_config(w, info=None):
+def _single_tank(name, directory):
+    if name == "directional_3d":
+        return workloads.directional_3d(directory)
+    if name == "irregular_2d":
+        return workloads.irregular_2d(directory)
+    return workloads.regular_2d()
+
+
+def _workload_config(w):
+    """The workload's `config`: the same dict in both arms."""
     cfg = {"workload": WORKLOAD_TEXT[w["name"]],
-           "n1": w["n1"], "n3": w["n3"], "mHOS": w["mHOS"], "p1": w["p1"],
+           "n1": w["n1"], "n2": w["n2"], "n3": w["n3"], "mHOS": w["mHOS"], "p1": w["p1"], "p2": w["p2"],
            "l2": "flushed between steps (256 MiB write outside the timed events)",
            "parallelism": "replicas"}
     if w["name"] == "irregular_2d":
         cfg.update({"wave_components": 512, "seed": 513})
-    if info is not None:
-        cfg["nd1"] = info["nd1"]
-        cfg["dt_nondim"] = info["delt"]
-        cfg["dt_s"] = info["delt"] * info["Tscale"]
+    if w["name"] == "directional_3d":
+        cfg.update({"seed": 2025})
     return cfg
+
+
+def _tank_info(info):
+    """Sizes and step of the tank the library built (beside `config`)."""
+    return {"nd1": info["nd1"], "nd2": info["nd2"], "n3_add": info["n3_add"], "dt_nondim": info["delt"],
+            "dt_s": info["delt"] * info["Tscale"]}
+
+
+def _host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
 
 
 class ClockSampler:
@@ -195,23 +224,6 @@ def _measured_peaks():
     return 6800.0, "of fallback"
 
 
-def _two_level_fmas(D, nin, nout):
-    """FMAs of the two-level pass pair the library picks for a REDFT00
-    length with D = A * B (the choice of pick_factors in xform.cu), or of
-    the direct symmetric sum when no factor pair is cheaper."""
-    direct = 0.5 * nin * nout
-    best = 0.6 * direct
-    for A in range(2, D // 2 + 1):
-        if D % A:
-            continue
-        B = D // A
-        if B < 2 or B > 256:
-            continue
-        paired = B % 2 == 0 and nout == D + 1
-        best = min(best, 2.0 * (A // 2 + 1) * nin + 2.0 * B * ((D // 2 + 1) if paired else nout))
-    return best if best < 0.6 * direct else direct
-
-
 def _fp64_step(fmas, ms, peak_gflops):
     """FP64 rate of a whole step: the FMAs of its transform passes (counted
     by the library as it builds the step graph) over the step's device
@@ -227,12 +239,17 @@ def _fused_pass():
     return os.environ.get("HOSNWT_FUSED_PASS", "0")[:1] == "1"
 
 
-def _profile_traffic():
-    """Per-launch DRAM traffic of the roofline batch's kernels from the
-    committed ncu summary of the pass the library runs, if present."""
-    name = "two_level_fused_irregular_2d.md" if _fused_pass() else "two_level_passes_irregular_2d.md"
-    p = os.path.join(ROOT, "profiles", name)
-    if not os.path.exists(p):
+# ncu summaries (profiles/) of the roofline transform of each workload
+PROFILE_OF = {"directional_3d": "roofline_transform_directional_3d.md",
+              "irregular_2d": "roofline_transform_irregular_2d.md"}
+
+
+def _profile_traffic(name):
+    """Per-launch DRAM traffic of the roofline transform from the committed
+    ncu summary of this workload, if present."""
+    fn = PROFILE_OF.get(name)
+    p = os.path.join(ROOT, "profiles", fn) if fn else None
+    if not p or not os.path.exists(p):
         return None
     for line in open(p):
         if line.startswith("traffic_bytes_per_launch:"):
@@ -243,47 +260,54 @@ def _profile_traffic():
     return None
 
 
-def cpu_baseline(w, budget_s=15.0, max_steps=400):
-    """The oracle (numpy/scipy FP64, one thread) on a bounded sample of the
-    same tank: as many RK4(5) steps as fit in about `budget_s` seconds."""
-    from oracle.hos_oracle import Tank as OTank
-    o = OTank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
-              wave_files_dir=w["wave_dir"])
+def _oracle(w, threads):
+    import oracle.hos_oracle as ho
+    ho.set_workers(threads)
+    return ho.Tank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
+                   wave_files_dir=w["wave_dir"])
+
+
+STATE_OUT = ("eta", "phis", "a_add_1", "a_add_2", "a_add_ramp", "a_add_3", "eta1st", "eta2nd", "a1st", "a2nd")
+
+
+def cpu_baseline(w, budget_s=20.0, max_steps=400):
+    """The oracle (numpy/scipy FP64, transforms threaded over the host's
+    cores) on a bounded sample of the same tank: as many RK4(5) steps as fit
+    in about `budget_s` seconds (at least one)."""
+    cores = _host_cores()
+    o = _oracle(w, cores)
     h = o.delt
     st = o.state_tuple()
     res, _, _, _ = o.runge4_adapt2(0.0, *st, h)  # warm-up
     n, t0 = 0, time.perf_counter()
     t = 0.0
-    while n < max_steps and time.perf_counter() - t0 < budget_s:
+    while n < max_steps and (n == 0 or time.perf_counter() - t0 < budget_s):
         res, err, deta, _ = o.runge4_adapt2(t, *st, h)
         t += h
         n += 1
     el = time.perf_counter() - t0
-    return {"value": n / el, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{n} RK4(5) steps of the {w['name']} tank (n1={w['n1']}, M={w['mHOS']}) with the numpy/scipy "
-                      f"oracle, {el:.1f} s on one host core"}
+    return {"value": n / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} RK4(5) steps of the {w['name']} tank (n1={w['n1']}, n2={w['n2']}, M={w['mHOS']}) "
+                      f"with the numpy/scipy oracle, transforms on {cores} threads, {el:.1f} s"}
 
 
 def run_reference(args, w):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from oracle.hos_oracle import Tank as OTank
-    o = OTank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
-              wave_files_dir=w["wave_dir"])
+    cores = _host_cores()
+    o = _oracle(w, cores)
     h = o.delt
     st = list(o.state_tuple())
     t = 0.0
     for _ in range(args.warmup):
         res, err, deta, _ = o.runge4_adapt2(t, *st, h)
-        st = [res[k] for k in ("eta", "phis", "a_add_1", "a_add_2", "a_add_ramp", "a_add_3",
-                               "eta1st", "eta2nd", "a1st", "a2nd")]
+        st = [res[k] for k in STATE_OUT]
         t += h
     t0 = time.perf_counter()
     for _ in range(args.steps):
         res, err, deta, _ = o.runge4_adapt2(t, *st, h)
-        st = [res[k] for k in ("eta", "phis", "a_add_1", "a_add_2", "a_add_ramp", "a_add_3",
-                               "eta1st", "eta2nd", "a1st", "a2nd")]
+        st = [res[k] for k in STATE_OUT]
         t += h
     el = time.perf_counter() - t0
     v = args.steps / el
@@ -292,10 +316,10 @@ def run_reference(args, w):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": _workload_config(w),
             "sim_s_per_wall_s": v * h * o.Tscale,
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": f"{args.steps} RK4(5) steps of the same tank on one host core "
-                                       "(CPU restatement of the Fortran reference; it is not buildable "
-                                       "here: no gfortran/FFTW)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} RK4(5) steps of the same tank after {args.warmup} warm-up "
+                                       f"steps, transforms on {cores} threads (CPU restatement of the "
+                                       "Fortran reference; it is not buildable here: no gfortran/FFTW)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -320,11 +344,12 @@ def run_cuda(args, w):
     h = info["delt"]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
-    # roofline of the dominant kernels: the big-grid transform passes (a
-    # batch of four FOURIER_2_SPACE_BIG of extended n1 modes, the shape of
-    # the HOS order loop), replayed back to back in a CUDA graph.
-    n1, nd1 = info["n1"], info["nd1"]
-    ms_tl = tank.time_transform("big", -1, "cos", "cos", (n1, 1), (nd1, 1), batch=4, nrep=50)
+    # roofline of the dominant work: a FOURIER_2_SPACE_BIG of the n1 x n2
+    # extended modes (both passes; batch of four in a 2-D tank), the shape of
+    # the HOS order loop, replayed back to back in a CUDA graph
+    n1, n2, nd1, nd2 = info["n1"], info["n2"], info["nd1"], info["nd2"]
+    batch = 1 if n2 > 1 else 4
+    ms_tl = tank.time_transform("big", -1, "cos", "cos", (n1, n2), (nd1, nd2), batch=batch, nrep=20)
 
     def l2_flush():
         flush.zero_()
@@ -356,7 +381,7 @@ def run_cuda(args, w):
     info = tank.info()
 
     # e2e: the drop-in call with pinned host arrays, copies inside the timed call
-    n1, n2, na = info["n1"], info["n2"], info["n3_add"]
+    na = info["n3_add"]
     shapes = [(n1, n2)] * 2 + [(na, n2)] * 4 + [(n1, n2)] * 4
     pinned = []
     for s in shapes:
@@ -382,19 +407,17 @@ def run_cuda(args, w):
     io_bytes = 8 * sum(s[0] * s[1] for s in shapes)
 
     ms = ms_tl
-    alg_bytes = 16.0 * nd1 * 4          # 8-byte read + 8-byte write per output element
+    alg_bytes = 16.0 * nd1 * nd2 * batch  # 8-byte read + 8-byte write per output element
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     peak, peak_src = _measured_peaks()
     fp64_peak = hosnwt.fp64_peak_gflops()
-    fp64_flops = 2.0 * _two_level_fmas(nd1 - 1, n1, nd1) * 4
-    fp64_achieved = fp64_flops / (ms * 1e-3) / 1e9
-    traffic = _profile_traffic() if w["name"] == "irregular_2d" else None
+    traffic = _profile_traffic(w["name"])
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": _workload_config(w, info),
+                "config": _workload_config(w), "tank": _tank_info(info),
                 "sim_s_per_wall_s": value / world * h * info["Tscale"],
                 "wall_ms_per_step": 1e3 * wall / args.steps,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes,
@@ -405,15 +428,13 @@ def run_cuda(args, w):
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic,
                              "peak_source": peak_src,
-                             "kernel": ("two_level_fused" if _fused_pass() else "two_level_pass1 + two_level_pass2")
-                                       + " (4 x FOURIER_2_SPACE_BIG of n1 modes)",
+                             "kernel": f"the transform passes of {batch} x FOURIER_2_SPACE_BIG of {n1} x {n2} "
+                                       f"modes to the {nd1} x {nd2} grid",
                              "ms_per_launch": ms,
-                             "timing": "the batch's transform launches, 50 replays in one CUDA graph (L2 warm)",
-                             "fp64": {"achieved_gflops": fp64_achieved, "peak_gflops": fp64_peak,
-                                      "frac": fp64_achieved / fp64_peak,
-                                      "note": "FMAs of the two-level algorithm actually run; the "
-                                              "passes are latency-bound; FP64 peak measured live "
-                                              "with a DFMA loop"}},
+                             "timing": "the transform's launches, 20 replays in one CUDA graph, CUDA events on "
+                                       "the library's stream",
+                             "note": "FP64-pipe bound, not HBM bound: GB300 runs FP64 at about 1.2 TFLOP/s; "
+                                     "fp64_step gives the step's transform FMAs against the FP64 peak"},
                 }
         if world == 1:
             line["cpu_baseline"] = cpu_baseline(w)
@@ -517,35 +538,6 @@ def run_ensemble(args):
         t.close()
     if dist is not None:
         dist.destroy_process_group()
-
-
-def run_3d(args):
-    """The 3-D directional tank (513 x 257, M = 5, p = 4): RK4(5) steps/s."""
-    import torch
-    import hosnwt
-    with tempfile.TemporaryDirectory() as tmp:
-        w = workloads.directional_3d(tmp)
-        tank = hosnwt.Tank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
-                           probes=w["probes"], wave_dir=w["wave_dir"])
-    inf = tank.info()
-    h = inf["delt"]
-    for _ in range(args.warmup):
-        tank.step(h)
-        tank.accept(h)
-    torch.cuda.synchronize()
-    ms0 = tank.info()["device_ms"]
-    for _ in range(args.steps):
-        tank.step(h)
-        tank.accept(h)
-    dev_ms = tank.info()["device_ms"] - ms0
-    line = {"metric": "RK4(5) steps/s, 3-D directional tank", "value": args.steps / (dev_ms * 1e-3),
-            "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "directional_3d: 50x30 m, n1=513 n2=257 n3=33 M=5 p1=p2=4",
-                       "nd1": inf["nd1"], "nd2": inf["nd2"], "dt_s": h * inf["Tscale"]},
-            "sim_s_per_wall_s": args.steps * h * inf["Tscale"] / (dev_ms * 1e-3),
-            "fp64_step": _fp64_step(inf["fmas_per_step"], dev_ms / args.steps, hosnwt.fp64_peak_gflops())}
-    print(json.dumps(line), flush=True)
 
 
 GEMM_SHAPES = [
@@ -755,38 +747,41 @@ def run_profile_step(args, w):
 
 
 def run_profile_roofline(args, w):
-    """The roofline batch of run_cuda (four FOURIER_2_SPACE_BIG of n1 modes:
-    the two-launch pass pair, or one two_level_fused launch under
-    HOSNWT_FUSED_PASS=1) inside a cudaProfilerStart / Stop range, for
-    `ncu --profile-from-start off -k regex:two_level`."""
+    """The roofline transform of run_cuda (FOURIER_2_SPACE_BIG of the n1 x n2
+    extended modes; a batch of four in a 2-D tank) once inside a
+    cudaProfilerStart / Stop range, for `ncu --profile-from-start off`.
+    time_transform runs the transform three times uncaptured before its
+    graph replay: the capture holds those three and the replay."""
     import torch
     import hosnwt
     tank = hosnwt.Tank(w["inp"], w["n1"], w["n2"], w["n3"], w["mHOS"], w["p1"], w["p2"],
                        probes=w["probes"], wave_dir=w["wave_dir"])
     info = tank.info()
-    n1, nd1 = info["n1"], info["nd1"]
+    n1, n2, nd1, nd2 = info["n1"], info["n2"], info["nd1"], info["nd2"]
+    batch = 1 if n2 > 1 else 4
     torch.cuda.synchronize()
     torch.cuda.profiler.start()
-    tank.time_transform("big", -1, "cos", "cos", (n1, 1), (nd1, 1), batch=4, nrep=1)
+    tank.time_transform("big", -1, "cos", "cos", (n1, n2), (nd1, nd2), batch=batch, nrep=1)
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()
-    print(json.dumps({"profile_roofline": w["name"], "n1": n1, "nd1": nd1}), flush=True)
+    print(json.dumps({"profile_roofline": w["name"], "n1": n1, "n2": n2, "nd1": nd1, "nd2": nd2,
+                      "batch": batch}), flush=True)
     tank.close()
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cuda", choices=("cuda", "reference"))
-    ap.add_argument("--workload", default="irregular_2d", choices=("irregular_2d", "regular_2d", "ensemble", "directional_3d", "tc_gemm",
-                                                   "surrogate"))
+    ap.add_argument("--workload", default="directional_3d",
+                    choices=SINGLE_TANK + ("ensemble", "tc_gemm", "surrogate"))
     ap.add_argument("--sim-seconds", type=float, default=1.0, help="ensemble: simulated seconds per tank")
     ap.add_argument("--profile-step", action="store_true",
                     help="run one step inside a cudaProfilerStart/Stop range (for ncu) and exit")
     ap.add_argument("--profile-roofline", action="store_true",
-                    help="run the roofline transform batch once inside a cudaProfilerStart/Stop range and exit")
+                    help="run the roofline transform once inside a cudaProfilerStart/Stop range and exit")
     args = ap.parse_args()
     if args.workload == "tc_gemm":
         run_profile_gemm(args) if args.profile_step else run_tc_gemm(args)
@@ -794,26 +789,16 @@ def main():
     if args.workload == "surrogate":
         run_surrogate(args)
         return
-    if args.profile_roofline:
-        with tempfile.TemporaryDirectory() as tmp:
-            run_profile_roofline(args, workloads.irregular_2d(tmp))
-        return
-    if args.profile_step:
-        with tempfile.TemporaryDirectory() as tmp:
-            if args.workload == "directional_3d":
-                run_profile_step(args, workloads.directional_3d(tmp))
-            else:
-                run_profile_step(args, workloads.irregular_2d(tmp))
-        return
     if args.workload == "ensemble":
         run_ensemble(args)
         return
-    if args.workload == "directional_3d":
-        run_3d(args)
-        return
     with tempfile.TemporaryDirectory() as tmp:
-        w = workloads.regular_2d() if args.workload == "regular_2d" else workloads.irregular_2d(tmp)
-        if args.impl == "reference":
+        w = _single_tank(args.workload, tmp)
+        if args.profile_roofline:
+            run_profile_roofline(args, w)
+        elif args.profile_step:
+            run_profile_step(args, w)
+        elif args.impl == "reference":
             run_reference(args, w)
         else:
             run_cuda(args, w)

@@ -20,7 +20,7 @@ INC = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhosnwt.so")
 
-SOURCES = ["xform.cu", "rhs.cu", "noalloc.cu", "tc_gemm.cu", "host.cpp"]
+SOURCES = ["xform.cu", "fft.cu", "rhs.cu", "noalloc.cu", "tc_gemm.cu", "host.cpp"]
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC]

@@ -222,6 +222,49 @@ struct Tables;
 void launch_y_f2s(const Tables& tb, const double* in, int nlines, long long y_stride, double* out,
                   long long out_y_stride, int cs, cudaStream_t st);
 
+// ---------------------------------------------------------------------------
+// FFT-based passes (fft.cu).  A REDFT00 / RODFT00 pass of length N = D + 1
+// over many lines runs as one real DFT of length D per line (two lines
+// packed into one complex DFT), computed by Stockham stages in shared
+// memory; a prime D goes through Rader's cyclic convolution of length D - 1.
+// ---------------------------------------------------------------------------
+constexpr int kFftMaxSt = 16;      // stages of one complex FFT
+constexpr int kFftMaxRadix = 127;  // largest odd prime factor of a stage
+
+struct FftStages {
+  int L;                     // complex length
+  int nst;                   // number of Stockham stages
+  int rad[kFftMaxSt];        // radix of each stage, in order
+  const double2* tw;         // exp(-2 pi i q / L), q = 0..L-1
+};
+
+// Device description of one transform length D (built once per context).
+struct FftDesc {
+  int D;
+  int rader;                 // 1: D prime, its DFT through a cyclic convolution of length D - 1
+  FftStages fft;             // complex FFT of length D, or D - 1 when rader
+  const int* gperm;          // rader: input index g^m mod D, m = 0..D-2
+  const int* gscat;          // rader: output index g^-n mod D, n = 0..D-2
+  const double2* bconj;      // rader: conj(FFT(exp(-2 pi i g^-q / D))) / (D - 1)
+  const double2* trig;       // (cos, sin)(pi j / D), j = 0..D
+};
+
+struct FftPlanInfo {
+  int D = 0;
+  const FftDesc* dev = nullptr;
+  double cost_line = 0.0;    // FP64 instructions per line (two lines share one complex FFT)
+};
+
+// Build the device tables of length D; device allocations are appended to
+// `allocs` (freed by the owner).  Returns false when D is not supported
+// (a prime factor above kFftMaxRadix that is not D itself, or a prime D
+// whose D - 1 has one).
+bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out);
+
+struct AxisJob;
+// FP64 instructions per line of the FFT pass of job J with plan f.
+double fft_line_cost(const FftPlanInfo& f);
+
 struct Tables {
   int n1, n2, nd1, nd2, n3_add;
   int nsm;                   // SMs of the device (sizes the split of the sums)
@@ -242,7 +285,19 @@ struct Tables {
   const double* q_nd1;
   const double* q_nd2;
   const double* q_add;
+  // FFT plans of the axis lengths (x and y, free-surface and dealiased grids)
+  FftPlanInfo fft[4];
+  int nfft = 0;
 };
+
+// The plan of tb for J's length when the FFT pass should run J (a REDFT00 /
+// RODFT00 job over enough lines to fill the GPU, whose FFT costs fewer FP64
+// instructions per line than `cost_other`), else null.  The environment
+// variable HOSNWT_FFT=0 turns the FFT passes off and HOSNWT_FFT=1 takes
+// them whenever a plan exists (read once when the library loads).
+const FftPlanInfo* fft_choice(const AxisJob& J, const Tables& tb, double cost_other);
+// Launch the FFT passes of b's jobs, job i with plan[i].
+void launch_fft_jobs(const AxisBatch& b, const FftPlanInfo* const* plan, const Tables& tb, cudaStream_t st);
 
 // FP64 FMAs of the transform passes launched from this host thread since
 // the counter was last reset (the algorithm's own count: terms times

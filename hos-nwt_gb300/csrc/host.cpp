@@ -849,8 +849,21 @@ int setup(Ctx& c, const char* wave_dir, const double* probes_xy, int nprobes) {
     c.tb3.cs = dalloc<double>(c, (size_t)c.tb.cs_cap);
   }
   c.tb.q_n1 = d.q_n1; c.tb.q_n2 = d.q_n2; c.tb.q_nd1 = d.q_nd1; c.tb.q_nd2 = d.q_nd2; c.tb.q_add = d.q_add;
+  // FFT plans of the x and y lengths (passes over many lines: 3-D tanks)
+  c.tb.nfft = 0;
+  if (n2 > 1) {
+    for (int D : {n1 - 1, n2 - 1, nd1 - 1, nd2 - 1}) {
+      bool seen = false;
+      for (int i = 0; i < c.tb.nfft; ++i) seen = seen || c.tb.fft[i].D == D;
+      if (seen) continue;
+      FftPlanInfo f;
+      if (build_fft_plan(D, c.allocs, &f)) c.tb.fft[c.tb.nfft++] = f;
+    }
+  }
   for (Tables* t : {&c.tb2, &c.tb3}) {
     t->q_n1 = d.q_n1; t->q_n2 = d.q_n2; t->q_nd1 = d.q_nd1; t->q_nd2 = d.q_nd2; t->q_add = d.q_add;
+    t->nfft = c.tb.nfft;
+    for (int i = 0; i < c.tb.nfft; ++i) t->fft[i] = c.tb.fft[i];
   }
   for (void* p : c.allocs)
     if (!p) return fail(c, HOSNWT_ERR_CUDA, "device allocation failed");

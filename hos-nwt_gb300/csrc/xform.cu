@@ -1738,15 +1738,35 @@ void launch_ytl(AxisBatch& b, bool early, cudaStream_t st) {
 // y passes: two-level where the length factors well (scratch permitting),
 // direct sums otherwise
 void launch_batch_y(AxisBatch& in, const Tables& tb, cudaStream_t st) {
-  AxisBatch b{}, b2{};
-  b.njobs = b2.njobs = 0;
-  b.acc = b2.acc = in.acc;
+  AxisBatch b{}, b2{}, bf{};
+  b.njobs = b2.njobs = bf.njobs = 0;
+  b.acc = b2.acc = bf.acc = in.acc;
+  const FftPlanInfo* fplan[kMaxJobs];
   long long cs_used = 0;
   for (int i = 0; i < in.njobs; ++i) {
     AxisJob J = in.job[i];
     J.A = J.B = 0;
     J.cs = nullptr;
     const bool c1s1 = (J.aj == 2 && J.bj == 0 && J.ak == 1 && J.bk == 0);
+    if (c1s1) {
+      const int nin = std::min(J.nin, J.N);
+      int A = 0, B = 0;
+      pick_factors_y(J.D, nin, J.nout, &A, &B);
+      double other = 0.5 * (double)nin * J.nout;
+      if (A > 0) {
+        J.A = A;
+        J.B = B;
+        J.mode = ytl_can_pair(J.D, A, B, J.nout, J.N) ? 1 : 0;
+        other = y_two_level_fmas(J);
+        J.A = J.B = 0;
+        J.mode = 0;
+      }
+      if (const FftPlanInfo* f = fft_choice(J, tb, other)) {
+        fplan[bf.njobs] = f;
+        bf.job[bf.njobs++] = J;
+        continue;
+      }
+    }
     if (c1s1 && tb.cs) {
       int A = 0, B = 0;
       pick_factors_y(J.D, std::min(J.nin, J.N), J.nout, &A, &B);
@@ -1763,6 +1783,7 @@ void launch_batch_y(AxisBatch& in, const Tables& tb, cudaStream_t st) {
     }
     b.job[b.njobs++] = J;
   }
+  if (bf.njobs) launch_fft_jobs(bf, fplan, tb, st);
   if (b2.njobs) launch_ytl(b2, tb.q_const, st);
   if (b.njobs == 0) return;
   int total = 0;
@@ -1898,16 +1919,29 @@ void launch_ordered(const XfReq* reqs, const int* idx, int n, const Tables& tb, 
     Y.gscale = R.scale;
     Y.epi = R.acc ? 1 : 0;
   }
-  // two-level passes for the x jobs whose length factors well
-  AxisBatch b2{}, bd{};
-  b2.njobs = bd.njobs = 0;
-  b2.acc = bd.acc = bx.acc;
+  // FFT passes for the x jobs over many lines where they cost less, then
+  // two-level passes for the jobs whose length factors well
+  AxisBatch b2{}, bd{}, bf{};
+  b2.njobs = bd.njobs = bf.njobs = 0;
+  b2.acc = bd.acc = bf.acc = bx.acc;
+  const FftPlanInfo* fplan[kMaxJobs];
   long long cs_used = 0;
   for (int i = 0; i < bx.njobs; ++i) {
     AxisJob J = bx.job[i];
     J.A = J.B = 0;
     J.cs = nullptr;
     const bool c1s1 = (J.aj == 2 && J.bj == 0 && J.ak == 1 && J.bk == 0);
+    if (c1s1) {
+      const int nin = std::min(J.nin, J.N);
+      int A = 0, B = 0;
+      pick_factors(J.D, nin, J.nout, &A, &B);
+      const double other = A > 0 ? x_two_level_cost(A, B, J.D, nin, J.nout) : 0.5 * (double)nin * J.nout;
+      if (const FftPlanInfo* f = fft_choice(J, tb, other)) {
+        fplan[bf.njobs] = f;
+        bf.job[bf.njobs++] = J;
+        continue;
+      }
+    }
     if (c1s1 && tb.cs) {
       int A = 0, B = 0;
       pick_factors(J.D, std::min(J.nin, J.N), J.nout, &A, &B);
@@ -1924,6 +1958,7 @@ void launch_ordered(const XfReq* reqs, const int* idx, int n, const Tables& tb, 
     }
     bd.job[bd.njobs++] = J;
   }
+  if (bf.njobs) launch_fft_jobs(bf, fplan, tb, st);
   if (b2.njobs && !launch_two_level_fused(b2, tb.nsm, tb.q_const, st))
     launch_two_level(b2, tb.nsm, tb.q_const, st);
   if (bd.njobs) launch_batch_x(bd, tb, st);

@@ -24,7 +24,7 @@ def test_reference_arm_line():
         assert key in d, key
     assert d["impl"] == "reference"
     assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 2
-    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] == 1
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
     assert d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["workload"].startswith("regular_2d") and d["config"]["n1"] == 257
@@ -35,3 +35,19 @@ def test_reference_arm_other_ranks_exit_quietly():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
                         "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
     assert r.returncode == 0 and not r.stdout.strip()
+
+
+def test_both_arms_share_the_config():
+    """The GPU arm's `config` is the same dict the reference arm prints
+    (tank sizes the library derives go beside it, under `tank`)."""
+    import tempfile
+    sys.path.insert(0, ROOT)
+    import bench
+    with tempfile.TemporaryDirectory() as tmp:
+        for name in bench.SINGLE_TANK:
+            w = bench._single_tank(name, tmp)
+            c = bench._workload_config(w)
+            assert c["workload"].startswith(name) and c["n1"] == w["n1"] and c["n2"] == w["n2"]
+    import inspect
+    src = inspect.getsource(bench.run_cuda) + inspect.getsource(bench.run_reference)
+    assert src.count('"config": _workload_config(w)') == 2

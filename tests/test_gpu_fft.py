@@ -1,0 +1,77 @@
+"""The FFT transform passes (fft.cu) against the oracle, through the C ABI.
+
+Four 3-D tanks whose axis lengths D = N - 1 cover the FFT plans: powers of
+two, Rader's algorithm for prime D (641 = 2^7 5 + 1, 257 = 2^8 + 1), and the
+generic odd radix (61, 19, 11, 97, 79, 13).  Every kind (cos / sin along x
+and y, S2F and F2S) on the free-surface and dealiased grids is compared with
+the oracle's transforms at 1e-13 * sqrt(N) of max |ref|.  Each run is a
+separate process with HOSNWT_FFT = 1 (FFT passes wherever a plan exists),
+0 (the sum passes only) or unset (the library's choice), since the library
+reads the variable once when it loads.
+"""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+# (n1, n2, p1, p2): x / y lengths D of the free-surface and dealiased grids
+SIZES = [
+    (513, 257, 4, 4),   # 512, 256 | 1281 = 3 7 61, 641 prime
+    (257, 129, 3, 3),   # 256, 128 | 513 = 3^3 19, 257 prime
+    (257, 65, 5, 5),    # 256, 64  | 770 = 2 5 7 11, 194 = 2 97
+    (514, 33, 3, 3),    # 513, 32  | 1027 = 13 79, 65 = 5 13
+]
+
+SCRIPT = r"""
+import json, sys
+import numpy as np
+sys.path[:0] = [ROOT, ROOT + "/hos-nwt_gb300"]
+import hosnwt
+from oracle.hos_oracle import Fourier, default_input
+rng = np.random.default_rng(11)
+worst = 0.0
+for n1, n2, p1, p2 in SIZES:
+    M = max(p1, p2, 3)
+    inp = default_input(T_stop=5.0, amp_mono=0.02, nu_mono=0.7, theta_mono=10.0, ylen=20.0, toler=1e-7)
+    g = hosnwt.Tank(inp, n1, n2, 9, M, p1, p2)
+    nd1, nd2 = ((p1 + 1) * n1) // 2, ((p2 + 1) * n2) // 2
+    F = Fourier(n1, n2, nd1, nd2, 16)
+    for grid, shp in (("n", (n1, n2)), ("big", (nd1, nd2))):
+        for csx in ("cos", "sin"):
+            for csy in ("cos", "sin"):
+                for direction in (1, -1):
+                    a = rng.standard_normal(shp)
+                    if grid == "n":
+                        ref = F.S2F(a, csx, csy) if direction == 1 else F.F2S(a, csx, csy)
+                    else:
+                        ref = F.S2F_big(a, csx, csy) if direction == 1 else F.F2S_big(a, csx, csy)
+                    got = g.transform(grid, direction, csx, csy, a)
+                    rel = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
+                    tol = 1e-13 * np.sqrt(max(shp))
+                    if not rel < tol:
+                        print(json.dumps({"fail": [n1, n2, p1, p2, grid, csx, csy, direction, rel, tol]}))
+                        sys.exit(1)
+                    worst = max(worst, rel / tol)
+    g.close()
+print(json.dumps({"worst_fraction_of_tol": worst}))
+"""
+
+
+@pytest.mark.parametrize("mode", ["1", "0", "auto"])
+def test_fft_transforms_match_oracle(lib, mode):
+    env = dict(os.environ)
+    env.pop("HOSNWT_FFT", None)
+    if mode != "auto":
+        env["HOSNWT_FFT"] = mode
+    src = f"ROOT = {ROOT!r}\nSIZES = {SIZES!r}\n" + SCRIPT
+    r = subprocess.run([sys.executable, "-c", src], cwd=ROOT, env=env, capture_output=True, text=True,
+                       timeout=900)
+    assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-3000:])
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["worst_fraction_of_tol"] < 1.0
