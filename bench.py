@@ -56,17 +56,22 @@ WORKLOAD_TEXT = {
     "directional_3d": "directional_3d: 3-D directional JONSWAP tank 50 m x 30 m x 5 m, snake flap hinged 2.0 m "
                       "above the bottom, Hs=0.08 m Tp=1.2 s gamma=3.3, cos^2s spreading s=10, n1=513 n2=257 "
                       "n3=33 M=5 p1=p2=4, RK4(5) tol 1e-7",
+    "steep_3d": "steep_3d: 3-D directional JONSWAP tank 50 m x 30 m x 5 m, snake flap hinged 2.0 m above "
+                "the bottom, Hs=0.15 m Tp=1.3 s gamma=5, cos^2s spreading s=15, n1=1025 n2=513 n3=33 M=7 "
+                "p1=p2=7, RK4(5) tol 1e-7",
     "irregular_2d": "irregular_2d: 2-D JONSWAP tank 50 m x 5 m, flap, 512 components, "
                     "n1=1025 n3=65 M=5 p1=5, RK4(5) tol 1e-7",
     "regular_2d": "regular_2d: 2-D regular wave T=1.0 s H=0.05 m, tank 50 m x 5 m, flap hinged 2.0 m above "
                   "the bottom, 3 s ramp, n1=257 n3=33 M=3 p1=3, RK4(5) tol 1e-7",
 }
-SINGLE_TANK = ("directional_3d", "irregular_2d", "regular_2d")
+SINGLE_TANK = ("directional_3d", "steep_3d", "irregular_2d", "regular_2d")
 
 
 def _single_tank(name, directory):
     if name == "directional_3d":
         return workloads.directional_3d(directory)
+    if name == "steep_3d":
+        return workloads.steep_3d(directory)
     if name == "irregular_2d":
         return workloads.irregular_2d(directory)
     return workloads.regular_2d()
@@ -82,6 +87,8 @@ def _workload_config(w):
         cfg.update({"wave_components": 512, "seed": 513})
     if w["name"] == "directional_3d":
         cfg.update({"seed": 2025})
+    if w["name"] == "steep_3d":
+        cfg.update({"seed": 200})
     return cfg
 
 
@@ -241,6 +248,7 @@ def _fused_pass():
 
 # ncu summaries (profiles/) of the roofline transform of each workload
 PROFILE_OF = {"directional_3d": "roofline_transform_directional_3d.md",
+              "steep_3d": "roofline_transform_steep_3d.md",
               "irregular_2d": "roofline_transform_irregular_2d.md"}
 
 

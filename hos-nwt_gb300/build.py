@@ -24,6 +24,8 @@ SOURCES = ["xform.cu", "fft.cu", "rhs.cu", "noalloc.cu", "tc_gemm.cu", "host.cpp
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INC, "-I", CSRC]
+# extra nvcc flags (e.g. -DHOSNWT_FFT_MIN_BLOCKS=4) for tuning builds
+FLAGS += os.environ.get("HOSNWT_NVCC_FLAGS", "").split()
 
 
 def _deps():

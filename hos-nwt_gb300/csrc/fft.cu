@@ -18,6 +18,9 @@
 //             S(2m) = -Im T_m,  S(2m+1) = Re T_0 / 2 + sum_{l=1..m} Re T_l
 // where T = DFT_D(t).  The odd outputs are prefix sums, done per line by a
 // warp with a shuffle scan in a fixed order (the results are deterministic).
+// The kernel carries t scaled by 2 / w (w the interior input weight) and the
+// unpacked spectra unhalved, so that the input weights, the halvings and the
+// output scales become one multiply per output.
 //
 // The complex DFT runs in shared memory as Stockham autosort stages (natural
 // order in and out): radix 2, 3, 4, 5, 8 butterflies in registers, and a
@@ -44,8 +47,12 @@ namespace hos {
 namespace {
 
 constexpr int kFT = 256;           // threads per CTA (8 warps)
+#ifndef HOSNWT_FFT_MIN_BLOCKS
+#define HOSNWT_FFT_MIN_BLOCKS 3    // resident CTAs per SM the register budget is cut for
+#endif
 constexpr int kFW = kFT / 32;
 constexpr int kFMaxLines = 16;     // lines per CTA (8 line pairs)
+constexpr size_t kFftSmemMax = 220 * 1024;  // dynamic shared memory of one CTA
 
 struct FftJob {
   const double* in;
@@ -55,7 +62,8 @@ struct FftJob {
   long long win_sk, win_sl;
   int nlines, nin, nout;
   int jlo, jhi, klo, khi;
-  double w0, wm, wl, s0, sm, sl, gscale;
+  double e0, eD;             // end input weights relative to the interior weight
+  double f0, fm, fl;         // output scales at k = 0, interior k, k = D (times w / 4)
   int sin_kind;
   int epi;
   int pairs;                 // line pairs per CTA
@@ -69,6 +77,12 @@ struct FftBatchT {
   int njobs;
   AccEpi acc;
 };
+
+// Shared-memory index of complex element i of an FFT buffer: one 16-byte
+// slot of padding per 8 elements, so that the stride-R writes of the first
+// Stockham stages fall in different banks within each quarter warp.
+__device__ __forceinline__ int pz(int i) { return i + (i >> 3); }
+__host__ __device__ constexpr long long padded(long long n) { return n + (n >> 3) + 1; }
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
@@ -126,6 +140,36 @@ __device__ __forceinline__ void dft<5>(double2* v) {
 }
 
 template <>
+__device__ __forceinline__ void dft<7>(double2* v) {
+  // cos / sin (2 pi q / 7), q = 1, 2, 3
+  const double c1 = 0.62348980185873353053, c2 = -0.22252093395631440429, c3 = -0.90096886790241912624;
+  const double s1 = 0.78183148246802980871, s2 = 0.97492791218182360702, s3 = 0.43388373911755812048;
+  const double2 x0 = v[0];
+  const double2 t1 = cadd(v[1], v[6]), t2 = cadd(v[2], v[5]), t3 = cadd(v[3], v[4]);
+  const double2 d1 = csub(v[1], v[6]), d2 = csub(v[2], v[5]), d3 = csub(v[3], v[4]);
+  double2 a1, a2, a3, b1, b2, b3;
+  a1.x = fma(c3, t3.x, fma(c2, t2.x, fma(c1, t1.x, x0.x)));
+  a1.y = fma(c3, t3.y, fma(c2, t2.y, fma(c1, t1.y, x0.y)));
+  a2.x = fma(c1, t3.x, fma(c3, t2.x, fma(c2, t1.x, x0.x)));
+  a2.y = fma(c1, t3.y, fma(c3, t2.y, fma(c2, t1.y, x0.y)));
+  a3.x = fma(c2, t3.x, fma(c1, t2.x, fma(c3, t1.x, x0.x)));
+  a3.y = fma(c2, t3.y, fma(c1, t2.y, fma(c3, t1.y, x0.y)));
+  b1.x = fma(s3, d3.x, fma(s2, d2.x, s1 * d1.x));
+  b1.y = fma(s3, d3.y, fma(s2, d2.y, s1 * d1.y));
+  b2.x = fma(-s1, d3.x, fma(-s3, d2.x, s2 * d1.x));
+  b2.y = fma(-s1, d3.y, fma(-s3, d2.y, s2 * d1.y));
+  b3.x = fma(s2, d3.x, fma(-s1, d2.x, s3 * d1.x));
+  b3.y = fma(s2, d3.y, fma(-s1, d2.y, s3 * d1.y));
+  v[0] = cadd(x0, cadd(t1, cadd(t2, t3)));
+  v[1] = cadd(a1, cmi(b1));
+  v[6] = csub(a1, cmi(b1));
+  v[2] = cadd(a2, cmi(b2));
+  v[5] = csub(a2, cmi(b2));
+  v[3] = cadd(a3, cmi(b3));
+  v[4] = csub(a3, cmi(b3));
+}
+
+template <>
 __device__ __forceinline__ void dft<8>(double2* v) {
   const double r = 0.70710678118654752440;  // sqrt(1/2)
   double2 e[4] = {v[0], v[2], v[4], v[6]};
@@ -143,37 +187,30 @@ __device__ __forceinline__ void dft<8>(double2* v) {
   }
 }
 
-// One Stockham stage of radix R (R in {2, 3, 4, 5, 8}) on P sequences of
+// One Stockham stage of radix R (R in {2, 3, 4, 5, 7, 8}) on P sequences of
 // length L, src -> dst; Ns is the product of the radices of earlier stages.
 // Butterfly j takes src[j + t L/R], twiddled by exp(-2 pi i t k / (Ns R))
 // with k = j mod Ns, and writes dst[(j - k) R + k + t Ns].
 template <int R>
 __device__ void st_small(const double2* __restrict__ src, double2* __restrict__ dst, int L, int Ns, int P,
-                         const double2* __restrict__ tw) {
+                         const double2* __restrict__ stw) {
   const int nb = L / R;
-  const int ts = L / (Ns * R);
   const int W = P * nb;
   for (int w = threadIdx.x; w < W; w += kFT) {
     const int p = w / nb, j = w - p * nb;
-    const double2* s = src + (long long)p * L;
-    double2* d = dst + (long long)p * L;
+    const int off = p * L;
     const int k = j % Ns;
     double2 v[R];
 #pragma unroll
-    for (int t = 0; t < R; ++t) v[t] = s[j + t * nb];
+    for (int t = 0; t < R; ++t) v[t] = src[pz(off + j + t * nb)];
     if (k != 0) {
-      const int step = k * ts;  // t k ts < L for t < R
-      int q = step;
 #pragma unroll
-      for (int t = 1; t < R; ++t) {
-        v[t] = cmul(v[t], __ldg(tw + q));
-        q += step;
-      }
+      for (int t = 1; t < R; ++t) v[t] = cmul(v[t], __ldg(stw + (t - 1) * Ns + k));
     }
     dft<R>(v);
-    const int base = (j - k) * R + k;
+    const int base = off + (j - k) * R + k;
 #pragma unroll
-    for (int t = 0; t < R; ++t) d[base + t * Ns] = v[t];
+    for (int t = 0; t < R; ++t) dst[pz(base + t * Ns)] = v[t];
   }
 }
 
@@ -184,24 +221,24 @@ __device__ void st_small(const double2* __restrict__ src, double2* __restrict__ 
 //   X_o = A - i B, X_{R-o} = A + i B,
 //   A = v_0 + sum_t s_t cos(2 pi t o / R),  B = sum_t d_t sin(2 pi t o / R).
 __device__ void st_generic(double2* __restrict__ src, double2* __restrict__ dst, int L, int Ns, int R, int P,
-                           const double2* __restrict__ tw) {
+                           const double2* __restrict__ tw, const double2* __restrict__ stw) {
   const int nb = L / R, h = (R + 1) / 2;
-  const int ts = L / (Ns * R), rs = L / R;
+  const int rs = L / R;
   const int W1 = P * nb * (h - 1);
   for (int w = threadIdx.x; w < W1; w += kFT) {
     const int j = w % nb;
     const int r = w / nb;
     const int t = 1 + r % (h - 1);
     const int p = r / (h - 1);
-    double2* s = src + (long long)p * L;
-    double2 va = s[j + t * nb], vb = s[j + (R - t) * nb];
+    const int off = p * L;
+    double2 va = src[pz(off + j + t * nb)], vb = src[pz(off + j + (R - t) * nb)];
     const int k = j % Ns;
     if (k != 0) {
-      va = cmul(va, __ldg(tw + t * k * ts));
-      vb = cmul(vb, __ldg(tw + (R - t) * k * ts));
+      va = cmul(va, __ldg(stw + (t - 1) * Ns + k));
+      vb = cmul(vb, __ldg(stw + (R - t - 1) * Ns + k));
     }
-    s[j + t * nb] = cadd(va, vb);
-    s[j + (R - t) * nb] = csub(va, vb);
+    src[pz(off + j + t * nb)] = cadd(va, vb);
+    src[pz(off + j + (R - t) * nb)] = csub(va, vb);
   }
   __syncthreads();
   const int W2 = P * nb * h;
@@ -210,22 +247,21 @@ __device__ void st_generic(double2* __restrict__ src, double2* __restrict__ dst,
     const int r = w / nb;
     const int o = r % h;
     const int p = r / h;
-    const double2* s = src + (long long)p * L;
-    double2* d = dst + (long long)p * L;
+    const int off = p * L;
     const int k = j % Ns;
-    const int base = (j - k) * R + k;
-    const double2 v0 = s[j];
+    const int base = off + (j - k) * R + k;
+    const double2 v0 = src[pz(off + j)];
     if (o == 0) {
       double2 a = v0;
-      for (int t = 1; t < h; ++t) a = cadd(a, s[j + t * nb]);
-      d[base] = a;
+      for (int t = 1; t < h; ++t) a = cadd(a, src[pz(off + j + t * nb)]);
+      dst[pz(base)] = a;
       continue;
     }
     double2 A = v0, B = make_double2(0.0, 0.0);
     int q = o;
     for (int t = 1; t < h; ++t) {
       const double2 c = __ldg(tw + q * rs);  // (cos, -sin)(2 pi q / R)
-      const double2 st = s[j + t * nb], dt = s[j + (R - t) * nb];
+      const double2 st = src[pz(off + j + t * nb)], dt = src[pz(off + j + (R - t) * nb)];
       A.x = fma(st.x, c.x, A.x);
       A.y = fma(st.y, c.x, A.y);
       B.x = fma(dt.x, -c.y, B.x);
@@ -233,8 +269,57 @@ __device__ void st_generic(double2* __restrict__ src, double2* __restrict__ dst,
       q += o;
       if (q >= R) q -= R;
     }
-    d[base + o * Ns] = make_double2(A.x + B.y, A.y - B.x);
-    d[base + (R - o) * Ns] = make_double2(A.x - B.y, A.y + B.x);
+    dst[pz(base + o * Ns)] = make_double2(A.x + B.y, A.y - B.x);
+    dst[pz(base + (R - o) * Ns)] = make_double2(A.x - B.y, A.y + B.x);
+  }
+}
+
+// One in-place stage of radix R on P sequences of length L (stride `ld`
+// between sequences): butterfly (b, j) holds elements b S + j + t m, t < R.
+// Decimation in frequency: DFT, then twiddle the outputs; in time: twiddle
+// the inputs, then DFT.  Each butterfly reads and writes only its own
+// elements, so a stage needs no barrier inside it.
+template <int R, bool DIF>
+__device__ void ip_stage(double2* __restrict__ x, int L, int ld, int S, int P, const double2* __restrict__ tw) {
+  const int m = S / R;
+  const int nb = L / R;
+  for (int w = threadIdx.x; w < P * nb; w += kFT) {
+    const int p = w / nb, bj = w - p * nb;
+    const int blk = bj / m, j = bj - blk * m;
+    const int base = p * ld + blk * S + j;
+    double2 v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = x[pz(base + t * m)];
+    if (!DIF && j != 0) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) v[t] = cmul(v[t], __ldg(tw + (t - 1) * m + j));
+    }
+    dft<R>(v);
+    if (DIF && j != 0) {
+#pragma unroll
+      for (int t = 1; t < R; ++t) v[t] = cmul(v[t], __ldg(tw + (t - 1) * m + j));
+    }
+#pragma unroll
+    for (int t = 0; t < R; ++t) x[pz(base + t * m)] = v[t];
+  }
+}
+
+template <bool DIF>
+__device__ void ip_fft(const FftInplace& F, double2* x, int ld, int P) {
+  for (int i = 0; i < F.nst; ++i) {
+    const int s = DIF ? i : F.nst - 1 - i;
+    int S = F.L;
+    for (int q = 0; q < s; ++q) S /= F.rad[q];
+    const double2* tw = F.tw + F.off[s];
+    switch (F.rad[s]) {
+      case 2: ip_stage<2, DIF>(x, F.L, ld, S, P, tw); break;
+      case 3: ip_stage<3, DIF>(x, F.L, ld, S, P, tw); break;
+      case 4: ip_stage<4, DIF>(x, F.L, ld, S, P, tw); break;
+      case 5: ip_stage<5, DIF>(x, F.L, ld, S, P, tw); break;
+      case 7: ip_stage<7, DIF>(x, F.L, ld, S, P, tw); break;
+      default: ip_stage<8, DIF>(x, F.L, ld, S, P, tw); break;
+    }
+    __syncthreads();
   }
 }
 
@@ -244,13 +329,15 @@ __device__ double2* run_fft(const FftStages& F, double2* a, double2* b, int P) {
   int Ns = 1;
   for (int s = 0; s < F.nst; ++s) {
     const int R = F.rad[s];
+    const double2* stw = F.stw + F.twoff[s];
     switch (R) {
-      case 2: st_small<2>(a, b, F.L, Ns, P, F.tw); break;
-      case 3: st_small<3>(a, b, F.L, Ns, P, F.tw); break;
-      case 4: st_small<4>(a, b, F.L, Ns, P, F.tw); break;
-      case 5: st_small<5>(a, b, F.L, Ns, P, F.tw); break;
-      case 8: st_small<8>(a, b, F.L, Ns, P, F.tw); break;
-      default: st_generic(a, b, F.L, Ns, R, P, F.tw); break;
+      case 2: st_small<2>(a, b, F.L, Ns, P, stw); break;
+      case 3: st_small<3>(a, b, F.L, Ns, P, stw); break;
+      case 4: st_small<4>(a, b, F.L, Ns, P, stw); break;
+      case 5: st_small<5>(a, b, F.L, Ns, P, stw); break;
+      case 7: st_small<7>(a, b, F.L, Ns, P, stw); break;
+      case 8: st_small<8>(a, b, F.L, Ns, P, stw); break;
+      default: st_generic(a, b, F.L, Ns, R, P, F.tw, stw); break;
     }
     __syncthreads();
     Ns *= R;
@@ -262,9 +349,10 @@ __device__ double2* run_fft(const FftStages& F, double2* a, double2* b, int P) {
 }
 
 // One CTA = `pairs` line pairs of one job.  Shared memory: two complex
-// buffers of pairs x D and the outputs of 2 pairs lines (D + 1 each).
+// buffers of pairs x (D + 1) padded elements; the outputs of the 2 pairs
+// lines (D + 1 each) are staged in whichever buffer the FFT leaves free.
 template <int NJ>
-__global__ void __launch_bounds__(kFT) k_fft_pass(const FftBatchT<NJ> b) {
+__global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const FftBatchT<NJ> b) {
   extern __shared__ __align__(16) double2 fsm[];
   __shared__ double red[kFW][kFMaxLines];
   __shared__ double2 z0s[kFMaxLines / 2], a0s[kFMaxLines / 2];
@@ -274,9 +362,10 @@ __global__ void __launch_bounds__(kFT) k_fft_pass(const FftBatchT<NJ> b) {
   const FftDesc& F = *J.desc;
   const int D = F.D, P = J.pairs, NL = 2 * P;
   const int line0 = ((int)blockIdx.x - b.start[jb]) * NL;
+  const bool blue = (F.mode == FFT_BLUESTEIN);
+  const int zld = blue ? F.ip.L : D;  // stride between the pairs' sequences
   double2* A = fsm;
-  double2* B = A + (long long)P * D;
-  double* O = reinterpret_cast<double*>(B + (long long)P * D);  // NL x (D + 1)
+  double2* B = A + padded((long long)P * (D + 1));
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   pdl_wait();
 
@@ -288,31 +377,32 @@ __global__ void __launch_bounds__(kFT) k_fft_pass(const FftBatchT<NJ> b) {
   const double* __restrict__ x = J.in + (long long)(valid ? line : 0) * J.in_sl;
   const double* __restrict__ wr = J.win ? J.win + (long long)(valid ? line : 0) * J.win_sl : nullptr;
   const int jlo = J.jlo, jend = min(J.jhi, J.nin);
+  // input j over the interior weight (the end weights enter at j = 0)
   auto U = [&](int j) -> double {
     if (!valid || j < jlo || j >= jend) return 0.0;
     double v = __ldg(x + (long long)j * J.in_sk);
     if (wr) v *= __ldg(wr + (long long)j * J.win_sk);
-    return v * ((j == 0) ? J.w0 : (j == D ? J.wl : J.wm));
+    return v;
   };
   const bool is_sin = J.sin_kind != 0;
   double c1 = 0.0;
   for (int w = tid; w < NL * D; w += kFT) {
     const int j = w / NL;
-    const double ua = U(j), ub = U(D - j);
-    const double2 cs = __ldg(F.trig + j);
+    double ua = U(j), ub = U(D - j);
+    const double2 cs = __ldg(F.trig + j);  // (cos, 2 sin)(theta_j)
     double t;
-    if (!is_sin) {
-      if (j == 0) {
-        t = ua + ub;
-        c1 += ua - ub;
-      } else {
-        t = fma(-cs.y, ua - ub, 0.5 * (ua + ub));
-        c1 = fma(ua, cs.x, c1);
-      }
+    if (j == 0) {
+      ua *= J.e0;
+      ub *= J.eD;
+      t = is_sin ? 0.0 : 2.0 * (ua + ub);
+      c1 += ua - ub;
+    } else if (!is_sin) {
+      t = fma(-cs.y, ua - ub, ua + ub);
+      c1 = fma(ua, cs.x, c1);
     } else {
-      t = (j == 0) ? 0.0 : fma(cs.y, ua + ub, 0.5 * (ua - ub));
+      t = fma(cs.y, ua + ub, ua - ub);
     }
-    reinterpret_cast<double*>(A + (long long)(l >> 1) * D + j)[l & 1] = t;
+    reinterpret_cast<double*>(A + pz((l >> 1) * zld + j))[l & 1] = t;
   }
   if (!is_sin) {
     // lanes with the same line: lane = l (mod NL)
@@ -323,59 +413,94 @@ __global__ void __launch_bounds__(kFT) k_fft_pass(const FftBatchT<NJ> b) {
 
   // ---- the complex DFT of length D of every pair
   double2* Z;
-  if (!F.rader) {
+  double* O;  // NL x (D + 1) outputs, in the buffer the DFT leaves free
+  if (F.mode == FFT_STOCKHAM) {
     Z = run_fft(F.fft, A, B, P);
-  } else {
-    const int Ls = D - 1;
-    double2* C = reinterpret_cast<double2*>(O);  // P x Ls fits in the output area
-    for (int w = tid; w < P * Ls; w += kFT) {
-      const int p = w / Ls, m = w - p * Ls;
-      B[(long long)p * Ls + m] = A[(long long)p * D + __ldg(F.gperm + m)];
-    }
-    if (tid < P) z0s[tid] = A[(long long)tid * D];
-    __syncthreads();
-    double2* S1 = run_fft(F.fft, B, C, P);
-    double2* S2 = (S1 == B) ? C : B;
-    if (tid < P) a0s[tid] = S1[(long long)tid * Ls];
-    for (int w = tid; w < P * Ls; w += kFT) {
-      const int m = w % Ls;
-      const double2 a = S1[w], c = __ldg(F.bconj + m);
-      // conj(a) * c
-      S2[w] = make_double2(fma(a.x, c.x, a.y * c.y), fma(a.x, c.y, -a.y * c.x));
+    O = reinterpret_cast<double*>(Z == A ? B : A);
+  } else if (blue) {
+    // X_k = conj-chirp_k sum_j (z_j conj-chirp_j) chirp_{k-j}: a cyclic
+    // convolution of length M >= 2 D + 2, in place in A
+    const int M = zld;
+    for (int w = tid; w < P * M; w += kFT) {
+      const int j = w % M;
+      const int idx = pz(w);
+      A[idx] = (j < D) ? cmul(A[idx], __ldg(F.chirp + j)) : make_double2(0.0, 0.0);
     }
     __syncthreads();
-    double2* S3 = (S2 == B) ? C : B;
-    double2* Y = run_fft(F.fft, S2, S3, P);
-    for (int w = tid; w < P * Ls; w += kFT) {
-      const int p = w / Ls, n = w - p * Ls;
-      const double2 y = Y[w], z0 = z0s[p];
-      A[(long long)p * D + __ldg(F.gscat + n)] = make_double2(z0.x + y.x, z0.y - y.y);
+    ip_fft<true>(F.ip, A, M, P);
+    for (int w = tid; w < P * M; w += kFT) {
+      const double2 a = A[pz(w)], c = __ldg(F.hrev + w % M);
+      A[pz(w)] = make_double2(fma(a.x, c.x, a.y * c.y), fma(a.x, c.y, -a.y * c.x));  // conj(a) c
     }
-    if (tid < P) A[(long long)tid * D] = cadd(z0s[tid], a0s[tid]);
+    __syncthreads();
+    ip_fft<false>(F.ip, A, M, P);
+    for (int w = tid; w < P * D; w += kFT) {
+      const int p = w / D, k = w - p * D;
+      const int idx = pz(p * M + k);
+      const double2 y = A[idx];
+      A[idx] = cmul(__ldg(F.chirp + k), make_double2(y.x, -y.y));
+    }
     __syncthreads();
     Z = A;
+    O = nullptr;  // rows in each pair's free tail, see orow
+  } else {
+    const int Ls = D - 1;
+    for (int w = tid; w < P * Ls; w += kFT) {
+      const int p = w / Ls, m = w - p * Ls;
+      B[pz(p * Ls + m)] = A[pz(p * D + __ldg(F.gperm + m))];
+    }
+    if (tid < P) z0s[tid] = A[pz(tid * D)];
+    __syncthreads();
+    // z now lives in B (permuted) and z0s: A is free for the ping-pong
+    double2* S1 = run_fft(F.fft, B, A, P);
+    double2* S2 = (S1 == B) ? A : B;
+    if (tid < P) a0s[tid] = S1[pz(tid * Ls)];
+    for (int w = tid; w < P * Ls; w += kFT) {
+      const int m = w % Ls;
+      const double2 a = S1[pz(w)], c = __ldg(F.bconj + m);
+      // conj(a) * c
+      S2[pz(w)] = make_double2(fma(a.x, c.x, a.y * c.y), fma(a.x, c.y, -a.y * c.x));
+    }
+    __syncthreads();
+    double2* Y = run_fft(F.fft, S2, S1, P);
+    Z = (Y == A) ? B : A;
+    for (int w = tid; w < P * Ls; w += kFT) {
+      const int p = w / Ls, n = w - p * Ls;
+      const double2 y = Y[pz(w)], z0 = z0s[p];
+      Z[pz(p * D + __ldg(F.gscat + n))] = make_double2(z0.x + y.x, z0.y - y.y);
+    }
+    if (tid < P) Z[pz(tid * D)] = cadd(z0s[tid], a0s[tid]);
+    __syncthreads();
+    O = reinterpret_cast<double*>(Y);
   }
 
+  // output row of line ll: D + 1 doubles
+  auto orow = [&](int ll) -> double* {
+    if (!blue) return O + (long long)ll * (D + 1);
+    return reinterpret_cast<double*>(A + pz((ll >> 1) * zld + D) + 1) + (ll & 1) * (D + 1);
+  };
+
   // ---- unpack the two real spectra of each pair; even outputs and the
-  // inputs of the odd-output prefix sums go to O
+  // inputs of the odd-output prefix sums go to the output rows
   const int ne = D / 2, no = (D - 1) / 2;
   for (int w = tid; w < P * (ne + 1); w += kFT) {
     const int p = w / (ne + 1), m = w - p * (ne + 1);
-    const double2 z1 = Z[(long long)p * D + m];
-    const double2 z2 = Z[(long long)p * D + (m == 0 ? 0 : D - m)];
-    // T_a = (z1 + conj z2) / 2, T_b = (z1 - conj z2) / (2 i)
-    const double tr[2] = {0.5 * (z1.x + z2.x), 0.5 * (z1.y + z2.y)};
-    const double ti[2] = {0.5 * (z1.y - z2.y), 0.5 * (z2.x - z1.x)};
+    const double2 z1 = Z[pz(p * zld + m)];
+    const double2 z2 = Z[pz(p * zld + (m == 0 ? 0 : D - m))];
+    // 2 T_a = z1 + conj z2, 2 T_b = (z1 - conj z2) / i: real parts tr,
+    // imaginary parts with the sign flipped nti
+    const double tr[2] = {z1.x + z2.x, z1.y + z2.y};
+    const double nti[2] = {z2.y - z1.y, z1.x - z2.x};
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      double* o = O + (long long)(2 * p + h) * (D + 1);
+      double* o = orow(2 * p + h);
       if (!is_sin) {
         o[2 * m] = tr[h];
-        if (m >= 1 && m <= no) o[2 * m + 1] = -ti[h];
+        if (m >= 1 && m <= no) o[2 * m + 1] = nti[h];
       } else {
-        o[2 * m] = -ti[h];
+        o[2 * m] = nti[h];
         if (m == 0) {
-          if (no >= 0 && D >= 1) o[1] = 0.5 * tr[h];
+          o[1] = 0.5 * tr[h];
         } else if (m <= no) {
           o[2 * m + 1] = tr[h];
         }
@@ -385,7 +510,7 @@ __global__ void __launch_bounds__(kFT) k_fft_pass(const FftBatchT<NJ> b) {
   if (!is_sin && tid < NL) {
     double s = 0.0;
     for (int w = 0; w < kFW; ++w) s += red[w][tid];
-    O[(long long)tid * (D + 1) + 1] = s;
+    orow(tid)[1] = 4.0 * s;
   }
   __syncthreads();
 
@@ -394,7 +519,7 @@ __global__ void __launch_bounds__(kFT) k_fft_pass(const FftBatchT<NJ> b) {
     const int n = no + 1;
     const int c = (n + 31) / 32;
     for (int ll = warp; ll < NL; ll += kFW) {
-      double* o = O + (long long)ll * (D + 1) + 1;
+      double* o = orow(ll) + 1;
       const int i0 = min(lane * c, n), i1 = min(i0 + c, n);
       double s = 0.0;
       for (int i = i0; i < i1; ++i) s += o[2 * i];
@@ -417,12 +542,12 @@ __global__ void __launch_bounds__(kFT) k_fft_pass(const FftBatchT<NJ> b) {
   // ---- scale and store (line fastest, like the loads)
   if (valid) {
     double* __restrict__ out = J.out + (long long)line * J.out_sl;
-    const double* o = O + (long long)l * (D + 1);
+    const double* o = orow(l);
     for (int w = tid; w < NL * J.nout; w += kFT) {
       const int k = w / NL;
       const bool active = (k >= J.klo) && (k < J.khi);
-      const double sc = (k == 0) ? J.s0 : ((k == D) ? J.sl : J.sm);
-      const double y = active ? o[k] * sc * J.gscale : 0.0;
+      const double sc = (k == 0) ? J.f0 : ((k == D) ? J.fl : J.fm);
+      const double y = active ? o[k] * sc : 0.0;
       out[(long long)k * J.out_sk] = y;
       if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, y);
     }
@@ -468,6 +593,7 @@ double stage_cost(int R, bool first) {
     case 3: bf = 4.7; break;
     case 4: bf = 4.0; break;
     case 5: bf = 7.0; break;
+    case 7: bf = 9.5; break;
     case 8: bf = 7.0; break;
     default: bf = R + 3.0; break;
   }
@@ -482,7 +608,7 @@ double stages_cost(const std::vector<int>& rad, int L) {
 
 // Radices of a complex FFT of length L: odd prime factors above 5 first
 // (the first stage needs no twiddles), then 8s, a 4 or a 2, then 5s and 3s.
-bool factor_stages(int L, std::vector<int>& rad) {
+bool factor_stages(int L, std::vector<int>& rad, int maxp = kFftMaxRadix) {
   rad.clear();
   if (L < 2) return false;
   int n = L, twos = 0;
@@ -498,7 +624,7 @@ bool factor_stages(int L, std::vector<int>& rad) {
     }
   if (n > 1) odd.push_back(n);
   for (int p : odd)
-    if (p > kFftMaxRadix) return false;
+    if (p > maxp) return false;
   std::sort(odd.begin(), odd.end(), [](int a, int b2) { return a > b2; });
   for (int p : odd)
     if (p > 5) rad.push_back(p);
@@ -583,21 +709,136 @@ T* upload_vec(const std::vector<T>& v, std::vector<void*>& allocs) {
   return static_cast<T*>(p);
 }
 
-// Reference DFT of a short sequence in long double (Rader's kernel spectrum).
-std::vector<std::complex<long double>> dft_ld(const std::vector<std::complex<long double>>& a) {
-  const int n = (int)a.size();
-  std::vector<std::complex<long double>> r(n);
-  for (int k = 0; k < n; ++k) {
-    std::complex<long double> s = 0;
-    for (int j = 0; j < n; ++j) {
-      const long long q = (long long)j * k % n;
-      const long double ang = -2.0L * kPiL * (long double)q / (long double)n;
-      s += a[j] * std::complex<long double>(cosl(ang), sinl(ang));
-    }
-    r[k] = s;
-  }
-  return r;
+using cld = std::complex<long double>;
+
+cld unit_root(long long q, long long n) {  // exp(-2 pi i q / n)
+  q %= n;
+  if (q < 0) q += n;
+  if (q == 0) return cld(1, 0);
+  if (4 * q == n) return cld(0, -1);
+  if (2 * q == n) return cld(-1, 0);
+  if (4 * q == 3 * n) return cld(0, 1);
+  const long double a = 2.0L * kPiL * (long double)q / (long double)n;
+  return cld(cosl(a), -sinl(a));
 }
+
+// Host DFT in long double (forward, exp(-2 pi i j k / n)): recursive
+// mixed-radix Cooley-Tukey on the smallest prime factor, for the tables
+// of Rader's and Bluestein's kernels.
+std::vector<cld> fft_ld(const std::vector<cld>& a) {
+  const int n = (int)a.size();
+  if (n <= 1) return a;
+  int r = n;
+  for (int q = 2; (long long)q * q <= n; ++q)
+    if (n % q == 0) {
+      r = q;
+      break;
+    }
+  std::vector<cld> w(n);
+  for (int q = 0; q < n; ++q) w[q] = unit_root(q, n);
+  std::vector<cld> out(n);
+  if (r == n) {
+    for (int k = 0; k < n; ++k) {
+      cld acc = 0;
+      for (int j = 0; j < n; ++j) acc += a[j] * w[(long long)j * k % n];
+      out[k] = acc;
+    }
+    return out;
+  }
+  const int m = n / r;
+  std::vector<std::vector<cld>> sub(r);
+  for (int t = 0; t < r; ++t) {
+    std::vector<cld> x(m);
+    for (int k = 0; k < m; ++k) x[k] = a[(long long)k * r + t];
+    sub[t] = fft_ld(x);
+  }
+  for (int q = 0; q < r; ++q)
+    for (int k = 0; k < m; ++k) {
+      const int f = k + q * m;
+      cld acc = 0;
+      for (int t = 0; t < r; ++t) acc += sub[t][k] * w[(long long)t * f % n];
+      out[f] = acc;
+    }
+  return out;
+}
+
+// Radices of a 7-smooth length for the in-place FFT: 8s, a 4 or a 2, then
+// 7s, 5s and 3s; false if L has a prime factor above 7.
+bool factor_smooth(int L, std::vector<int>& rad) { return factor_stages(L, rad, 7); }
+
+double inplace_cost(const std::vector<int>& rad, int L) {
+  double c = 0.0;
+  for (size_t s = 0; s < rad.size(); ++s) c += stage_cost(rad[s], s + 1 == rad.size());
+  return c * L;
+}
+
+// digit-reversed position of frequency k after the in-place DIF stages
+std::vector<int> dif_positions(int L, const std::vector<int>& rad) {
+  std::vector<int> pos(L);
+  for (int k = 0; k < L; ++k) {
+    int kk = k, p = 0, span = L;
+    for (int R : rad) {
+      const int q = kk % R;
+      kk /= R;
+      span /= R;
+      p += q * span;
+    }
+    pos[k] = p;
+  }
+  return pos;
+}
+
+}  // namespace
+
+namespace {
+
+// Stockham stages of length L with their twiddles
+bool upload_stages(const std::vector<int>& rad, int L, std::vector<void*>& allocs, FftStages* f) {
+  f->L = L;
+  f->nst = (int)rad.size();
+  for (int s = 0; s < f->nst; ++s) f->rad[s] = rad[s];
+  f->tw = upload_vec(twiddles(L), allocs);
+  // stage twiddles exp(-2 pi i t k / (Ns R)) at (t - 1) Ns + k
+  std::vector<double2> stw;
+  long long Ns = 1;
+  for (int st = 0; st < f->nst; ++st) {
+    const int R = rad[st];
+    f->twoff[st] = (int)stw.size();
+    const long long den = Ns * R;
+    for (int t = 1; t < R; ++t)
+      for (long long k = 0; k < Ns; ++k) {
+        const cld w = unit_root((long long)t * k, den);
+        stw.push_back(make_double2((double)w.real(), (double)w.imag()));
+      }
+    Ns *= R;
+  }
+  f->stw = upload_vec(stw, allocs);
+  return f->tw && f->stw;
+}
+
+// In-place stages of length L with their twiddles
+bool upload_inplace(const std::vector<int>& rad, int L, std::vector<void*>& allocs, FftInplace* f) {
+  f->L = L;
+  f->nst = (int)rad.size();
+  std::vector<double2> tw;
+  int S = L;
+  for (int s = 0; s < f->nst; ++s) {
+    const int R = rad[s], m = S / R;
+    f->rad[s] = R;
+    f->off[s] = (int)tw.size();
+    for (int q = 1; q < R; ++q)
+      for (int j = 0; j < m; ++j) {
+        const cld w = unit_root((long long)q * j, S);
+        tw.push_back(make_double2((double)w.real(), (double)w.imag()));
+      }
+    S = m;
+  }
+  f->tw = upload_vec(tw, allocs);
+  return f->tw != nullptr;
+}
+
+// shared memory of the Bluestein mode must hold the padded convolution
+constexpr long long kBlueMaxM = 12400;
 
 }  // namespace
 
@@ -605,41 +846,31 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
   if (D < 8 || !out) return false;
   FftDesc h{};
   h.D = D;
-  std::vector<int> rad;
-  int L = D;
-  double fcost = 0.0;
-  if (factor_stages(D, rad)) {
-    h.rader = 0;
-    fcost = stages_cost(rad, D);
-  } else if (is_prime(D) && factor_stages(D - 1, rad)) {
-    h.rader = 1;
-    L = D - 1;
-    fcost = 2.0 * stages_cost(rad, L) + 8.0 * L;
-  } else {
-    return false;
-  }
-  h.fft.L = L;
-  h.fft.nst = (int)rad.size();
-  for (int s = 0; s < h.fft.nst; ++s) h.fft.rad[s] = rad[s];
-  h.fft.tw = upload_vec(twiddles(L), allocs);
-  if (!h.fft.tw) return false;
-  // (cos, sin)(pi j / D), j = 0..D
-  std::vector<double2> trig(D + 1);
-  for (int j = 0; j <= D; ++j) {
-    long double c, s;
-    if (j == 0) { c = 1; s = 0; }
-    else if (j == D) { c = -1; s = 0; }
-    else if (2 * j == D) { c = 0; s = 1; }
-    else {
-      const long double a = kPiL * (long double)j / (long double)D;
-      c = cosl(a);
-      s = sinl(a);
+  // candidate algorithms and their FP64 instructions per complex DFT
+  std::vector<int> rad_s, rad_r, rad_b;
+  double cost_s = 1e300, cost_r = 1e300, cost_b = 1e300;
+  if (factor_stages(D, rad_s)) cost_s = stages_cost(rad_s, D);
+  if (is_prime(D) && factor_stages(D - 1, rad_r)) cost_r = 2.0 * stages_cost(rad_r, D - 1) + 8.0 * (D - 1);
+  int M = 0;
+  for (long long c = 2LL * D + 2; c <= std::min<long long>(3LL * D, kBlueMaxM); ++c) {
+    std::vector<int> r;
+    if (!factor_smooth((int)c, r)) continue;
+    const double cb = 2.0 * inplace_cost(r, (int)c) + 4.0 * c + 8.0 * D;
+    if (cb < cost_b) {
+      cost_b = cb;
+      M = (int)c;
+      rad_b = r;
     }
-    trig[j] = make_double2((double)c, (double)s);
   }
-  h.trig = upload_vec(trig, allocs);
-  if (!h.trig) return false;
-  if (h.rader) {
+  double fcost;
+  if (cost_s <= cost_r && cost_s <= cost_b) {
+    h.mode = FFT_STOCKHAM;
+    fcost = cost_s;
+    if (!upload_stages(rad_s, D, allocs, &h.fft)) return false;
+  } else if (cost_r <= cost_b) {
+    h.mode = FFT_RADER;
+    fcost = cost_r;
+    if (!upload_stages(rad_r, D - 1, allocs, &h.fft)) return false;
     const int p = D, g = primitive_root(p);
     if (g == 0) return false;
     std::vector<int> gp(p - 1), gs(p - 1);
@@ -648,29 +879,63 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
       gp[m] = (int)powmod(g, m, p);
       gs[m] = (int)powmod(ginv, m, p);
     }
-    std::vector<std::complex<long double>> bq(p - 1);
-    for (int q = 0; q < p - 1; ++q) {
-      const long double ang = -2.0L * kPiL * (long double)gs[q] / (long double)p;
-      bq[q] = std::complex<long double>(cosl(ang), sinl(ang));
-    }
-    const std::vector<std::complex<long double>> B = dft_ld(bq);
+    std::vector<cld> bq(p - 1);
+    for (int q = 0; q < p - 1; ++q) bq[q] = unit_root(gs[q], p);
+    const std::vector<cld> B = fft_ld(bq);
     std::vector<double2> bc(p - 1);
     for (int k = 0; k < p - 1; ++k) {
-      const std::complex<long double> v = std::conj(B[k]) / (long double)(p - 1);
+      const cld v = std::conj(B[k]) / (long double)(p - 1);
       bc[k] = make_double2((double)v.real(), (double)v.imag());
     }
     h.gperm = upload_vec(gp, allocs);
     h.gscat = upload_vec(gs, allocs);
     h.bconj = upload_vec(bc, allocs);
     if (!h.gperm || !h.gscat || !h.bconj) return false;
+  } else if (M > 0) {
+    h.mode = FFT_BLUESTEIN;
+    fcost = cost_b;
+    if (!upload_inplace(rad_b, M, allocs, &h.ip)) return false;
+    // chirp exp(-i pi j^2 / D) (exact phase index j^2 mod 2D), the kernel
+    // h_n = conj chirp_|n| on |n| < D of the cyclic length M, and its
+    // conjugated spectrum over M in the DIF output order
+    std::vector<double2> chirp(D);
+    std::vector<cld> hk(M, cld(0, 0));
+    for (int j = 0; j < D; ++j) {
+      const cld w = unit_root((long long)j * j % (2LL * D), 2LL * D);
+      chirp[j] = make_double2((double)w.real(), (double)w.imag());
+      hk[j] = std::conj(w);
+      if (j > 0) hk[M - j] = std::conj(w);
+    }
+    const std::vector<cld> H = fft_ld(hk);
+    const std::vector<int> pos = dif_positions(M, rad_b);
+    std::vector<double2> hrev(M);
+    for (int k = 0; k < M; ++k) {
+      const cld v = std::conj(H[k]) / (long double)M;
+      hrev[pos[k]] = make_double2((double)v.real(), (double)v.imag());
+    }
+    h.chirp = upload_vec(chirp, allocs);
+    h.hrev = upload_vec(hrev, allocs);
+    if (!h.chirp || !h.hrev) return false;
+  } else {
+    return false;
   }
+  // (cos, 2 sin)(pi j / D), j = 0..D
+  std::vector<double2> trig(D + 1);
+  for (int j = 0; j <= D; ++j) {
+    const cld w = unit_root(j, 2LL * D);  // exp(-i pi j / D)
+    trig[j] = make_double2((double)w.real(), (double)(-2.0L * w.imag()));
+  }
+  h.trig = upload_vec(trig, allocs);
+  if (!h.trig) return false;
   std::vector<FftDesc> one(1, h);
   const FftDesc* dev = upload_vec(one, allocs);
   if (!dev) return false;
   out->D = D;
+  out->mode = h.mode;
+  out->M = (h.mode == FFT_BLUESTEIN) ? M : 0;
   out->dev = dev;
-  // two lines share one complex FFT; pre/post processing about 12 per point
-  out->cost_line = 0.5 * fcost + 12.0 * (D + 1);
+  // two lines share one complex FFT; pre/post processing about 7 per point
+  out->cost_line = 0.5 * fcost + 7.0 * (D + 1);
   return true;
 }
 
@@ -680,7 +945,7 @@ const FftPlanInfo* fft_choice(const AxisJob& J, const Tables& tb, double cost_ot
   const int mode = fft_mode();
   if (mode == 0) return nullptr;
   const bool c1s1 = (J.aj == 2 && J.bj == 0 && J.ak == 1 && J.bk == 0);
-  if (!c1s1 || J.nlines < 32) return nullptr;
+  if (!c1s1 || J.nlines < 32 || J.wm == 0.0) return nullptr;
   for (int i = 0; i < tb.nfft; ++i) {
     const FftPlanInfo& f = tb.fft[i];
     if (f.D != J.D || !f.dev) continue;
@@ -691,20 +956,21 @@ const FftPlanInfo* fft_choice(const AxisJob& J, const Tables& tb, double cost_ot
 
 namespace {
 
-size_t fft_smem(int D, int P) {
-  return (size_t)P * D * 2 * sizeof(double2) + (size_t)2 * P * (D + 1) * sizeof(double);
+size_t fft_smem(const FftPlanInfo& f, int P) {
+  if (f.mode == FFT_BLUESTEIN) return (size_t)padded((long long)P * f.M) * sizeof(double2);
+  return (size_t)2 * padded((long long)P * (f.D + 1)) * sizeof(double2);
 }
 
 // line pairs per CTA: enough butterflies per stage for the 8 warps, enough
 // CTAs for the SMs, shared memory within budget; lines-contiguous (y)
 // passes take at least two pairs so that a warp's loads fill 32-byte sectors
-int pick_pairs(const AxisJob& J, int nsm) {
+int pick_pairs(const AxisJob& J, const FftPlanInfo& f, int nsm) {
   const bool ymode = (J.in_sk != 1);
   int P = ymode ? 8 : 4;
   const int Pmin = ymode ? 2 : 1;
   while (P > Pmin) {
     const long long ctas = (J.nlines + 2LL * P - 1) / (2LL * P);
-    if (fft_smem(J.D, P) > 200 * 1024) {
+    if (fft_smem(f, P) > kFftSmemMax) {
       P /= 2;
       continue;
     }
@@ -714,7 +980,7 @@ int pick_pairs(const AxisJob& J, int nsm) {
     }
     break;
   }
-  while (P > 1 && fft_smem(J.D, P) > 200 * 1024) P /= 2;
+  while (P > 1 && fft_smem(f, P) > kFftSmemMax) P /= 2;
   return P;
 }
 
@@ -745,18 +1011,17 @@ void launch_fft_jobs(const AxisBatch& in, const FftPlanInfo* const* plan, const 
     f.jhi = J.jhi;
     f.klo = J.klo;
     f.khi = J.khi;
-    f.w0 = J.w0;
-    f.wm = J.wm;
-    f.wl = J.wl;
-    f.s0 = J.s0;
-    f.sm = J.sm;
-    f.sl = J.sl;
-    f.gscale = J.gscale;
+    // the kernel's outputs are 4 / wm times the transform
+    f.e0 = J.w0 / J.wm;
+    f.eD = J.wl / J.wm;
+    f.f0 = 0.25 * J.wm * J.s0 * J.gscale;
+    f.fm = 0.25 * J.wm * J.sm * J.gscale;
+    f.fl = 0.25 * J.wm * J.sl * J.gscale;
     f.sin_kind = (J.off != 0) ? 1 : 0;
     f.epi = J.epi;
     f.desc = plan[i]->dev;
-    f.pairs = pick_pairs(J, tb.nsm);
-    smem = std::max(smem, fft_smem(J.D, f.pairs));
+    f.pairs = pick_pairs(J, *plan[i], tb.nsm);
+    smem = std::max(smem, fft_smem(*plan[i], f.pairs));
     b.start[i] = total;
     total += (J.nlines + 2 * f.pairs - 1) / (2 * f.pairs);
     g_xform_fmas += (double)J.nlines * plan[i]->cost_line;
@@ -768,7 +1033,7 @@ void launch_fft_jobs(const AxisBatch& in, const FftPlanInfo* const* plan, const 
     for (int nj : {1, 2, 4, 8, kMaxJobs})
       with_fft_capacity(nj, [&](auto c) {
         cudaFuncSetAttribute(k_fft_pass<decltype(c)::value>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             210 * 1024);
+                             (int)kFftSmemMax);
       });
   });
   with_fft_capacity(b.njobs, [&](auto c) {

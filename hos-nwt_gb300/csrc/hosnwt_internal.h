@@ -235,30 +235,55 @@ struct FftStages {
   int L;                     // complex length
   int nst;                   // number of Stockham stages
   int rad[kFftMaxSt];        // radix of each stage, in order
+  int twoff[kFftMaxSt];      // offset of each stage's twiddles in stw
   const double2* tw;         // exp(-2 pi i q / L), q = 0..L-1
+  const double2* stw;        // stage twiddles: stage s (radix R, Ns the product of the
+                             //   earlier radices) holds exp(-2 pi i t k / (Ns R)) at
+                             //   twoff[s] + (t - 1) Ns + k, t = 1..R-1, k < Ns
 };
+
+// In-place mixed-radix FFT of length L (radices 2, 3, 4, 5, 7, 8): the
+// decimation-in-frequency form takes natural order to digit-reversed order,
+// the decimation-in-time form digit-reversed order back to natural order.
+// Stage s has span S (L over the product of the earlier radices) and
+// m = S / R; its twiddles exp(-2 pi i q j / S) sit at off[s] + (q - 1) m + j.
+struct FftInplace {
+  int L;
+  int nst;
+  int rad[kFftMaxSt];
+  int off[kFftMaxSt];
+  const double2* tw;
+};
+
+enum FftMode { FFT_STOCKHAM = 0, FFT_RADER = 1, FFT_BLUESTEIN = 2 };
 
 // Device description of one transform length D (built once per context).
 struct FftDesc {
   int D;
-  int rader;                 // 1: D prime, its DFT through a cyclic convolution of length D - 1
-  FftStages fft;             // complex FFT of length D, or D - 1 when rader
+  int mode;                  // FftMode
+  FftStages fft;             // Stockham FFT of length D (mode 0) or D - 1 (mode 1)
   const int* gperm;          // rader: input index g^m mod D, m = 0..D-2
   const int* gscat;          // rader: output index g^-n mod D, n = 0..D-2
   const double2* bconj;      // rader: conj(FFT(exp(-2 pi i g^-q / D))) / (D - 1)
-  const double2* trig;       // (cos, sin)(pi j / D), j = 0..D
+  FftInplace ip;             // bluestein: in-place FFT of the convolution length M
+  const double2* chirp;      // bluestein: exp(-i pi j^2 / D), j < D
+  const double2* hrev;       // bluestein: conj(FFT_M(chirp kernel)) / M, digit-reversed
+  const double2* trig;       // (cos, 2 sin)(pi j / D), j = 0..D
 };
 
 struct FftPlanInfo {
   int D = 0;
+  int mode = 0;
+  int M = 0;                 // bluestein convolution length
   const FftDesc* dev = nullptr;
   double cost_line = 0.0;    // FP64 instructions per line (two lines share one complex FFT)
 };
 
 // Build the device tables of length D; device allocations are appended to
-// `allocs` (freed by the owner).  Returns false when D is not supported
-// (a prime factor above kFftMaxRadix that is not D itself, or a prime D
-// whose D - 1 has one).
+// `allocs` (freed by the owner).  The cheapest of a Stockham FFT of length D
+// (prime factors up to kFftMaxRadix), Rader's algorithm (D prime) and
+// Bluestein's chirp convolution is taken.  Returns false on an allocation
+// failure or a length whose convolution does not fit in shared memory.
 bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out);
 
 struct AxisJob;

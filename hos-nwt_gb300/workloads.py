@@ -14,6 +14,8 @@ the tank, wavemaker, spectrum and numerical sizes stated below.
   directional_3d  50 x 30 m tank, snake flap, JONSWAP Hs = 0.08 m, Tp = 1.2 s,
                 cos^2s spreading (s = 10) drawn per frequency bin;
                 n1 = 513, n2 = 257, n3 = 33, M = 5, p1 = p2 = 4
+  steep_3d      the same tank with JONSWAP Hs = 0.15 m, Tp = 1.3 s, gamma = 5,
+                s = 15; n1 = 1025, n2 = 513, n3 = 33, M = 7, p1 = p2 = 7
 Every case uses an absorbing beach over the last 10 m (xabsf = 0.8).
 """
 from __future__ import annotations
@@ -108,6 +110,35 @@ def directional_3d(directory, seed=2025, n1=513, n2=257, n3=33, mHOS=5, p1=4, p2
     probes = [(5.0, 15.0), (10.0, 15.0), (20.0, 15.0), (20.0, 7.5), (30.0, 15.0)]
     return dict(inp=inp, n1=n1, n2=n2, n3=n3, mHOS=mHOS, p1=p1, p2=p2, probes=probes, wave_dir=directory,
                 Hs=0.08, name="directional_3d")
+
+
+def steep_3d(directory, seed=200, n1=1025, n2=513, n3=33, mHOS=7, p1=7, p2=7, T_stop=100.0):
+    """The steep 3-D tank of the surrogate study, run on the plain FP64 path:
+    50 x 30 m, h = 5 m, snake flap, JONSWAP Hs = 0.15 m, Tp = 1.3 s,
+    gamma = 5, cos^2s spreading with s = 15 drawn per frequency bin (0.4 to
+    2.5 Hz, bins of 1/128 Hz), phases U[0, 2 pi) from PCG64(seed);
+    n1 = 1025, n2 = 513, n3 = 33, M = 7, p1 = p2 = 7 (dealiased grid
+    4100 x 2052)."""
+    clock, rnum = 32.0, 12
+    harmo = np.arange(int(0.4 * 2 ** rnum / clock), int(2.5 * 2 ** rnum / clock) + 1)
+    f = harmo * clock / 2 ** rnum
+    df = clock / 2 ** rnum
+    S = jonswap_density(f, 0.15, 1.3, 5.0)
+    S *= (0.15 / (4.0 * math.sqrt(np.sum(S * df)))) ** 2
+    amp = np.sqrt(2.0 * S * df)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    th = np.linspace(-np.pi, np.pi, 4001)
+    cdf = np.cumsum(np.cos(th / 2.0) ** 30)
+    cdf /= cdf[-1]
+    angle = np.degrees(np.interp(rng.uniform(size=harmo.size), cdf, th))
+    phase = rng.uniform(0.0, 2 * np.pi, harmo.size)
+    name = "S015_13"
+    write_wave_files(directory, name, harmo, clock, rnum, amp, angle, phase, 5.0, 30.0, 2.0, 0.4, 2.5)
+    inp = base_input(icase=3, file_name=name, T_stop=T_stop, toler=1e-7, f_out=10.0, Hs=0.15, Tp=1.3,
+                     gamma=5.0)
+    probes = [(5.0, 15.0), (10.0, 15.0), (20.0, 15.0), (20.0, 7.5), (30.0, 15.0)]
+    return dict(inp=inp, n1=n1, n2=n2, n3=n3, mHOS=mHOS, p1=p1, p2=p2, probes=probes, wave_dir=directory,
+                Hs=0.15, name="steep_3d")
 
 
 def ensemble(n_tanks=64, seed=7, T_stop=60.0, n3=33):

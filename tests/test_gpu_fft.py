@@ -1,8 +1,10 @@
 """The FFT transform passes (fft.cu) against the oracle, through the C ABI.
 
-Four 3-D tanks whose axis lengths D = N - 1 cover the FFT plans: powers of
-two, Rader's algorithm for prime D (641 = 2^7 5 + 1, 257 = 2^8 + 1), and the
-generic odd radix (61, 19, 11, 97, 79, 13).  Every kind (cos / sin along x
+Six 3-D tanks whose axis lengths D = N - 1 cover the FFT plans: powers of
+two, Rader's algorithm for prime D (641 = 2^7 5 + 1, 257 = 2^8 + 1), the
+generic odd radix (61, 19, 11, 97, 79, 13, 43) and Bluestein's chirp
+convolution for lengths with a large prime factor (2051 = 7 293, and the
+prime 4099, whose 4098 = 2 3 683 rules Rader out).  Every kind (cos / sin along x
 and y, S2F and F2S) on the free-surface and dealiased grids is compared with
 the oracle's transforms at 1e-13 * sqrt(N) of max |ref|.  Each run is a
 separate process with HOSNWT_FFT = 1 (FFT passes wherever a plan exists),
@@ -26,6 +28,8 @@ SIZES = [
     (257, 129, 3, 3),   # 256, 128 | 513 = 3^3 19, 257 prime
     (257, 65, 5, 5),    # 256, 64  | 770 = 2 5 7 11, 194 = 2 97
     (514, 33, 3, 3),    # 513, 32  | 1027 = 13 79, 65 = 5 13
+    (65, 513, 3, 7),    # 64, 512  | 129 = 3 43, 2051 = 7 293 (Bluestein)
+    (1025, 33, 7, 3),   # 1024, 32 | 4099 prime (Bluestein), 65
 ]
 
 SCRIPT = r"""
