@@ -7,11 +7,13 @@ tests/golden/make_baseline_fixtures.py from the oracle).
                       first 10 s of the time loop)
   c3  directional_3d  513 x 257, n3 = 33, M = 5, p1 = p2 = 4 (one right-hand
                       side, one RK4(5) step)
+  c5  steep_3d        1025 x 513, n3 = 33, M = 7, p1 = p2 = 7 (one right-hand
+                      side, one RK4(5) step)
 
 The right-hand side and the step start from a seeded synthetic state: random
 modal amplitudes under a Gaussian envelope over the lower modes, drawn from
 PCG64.random (uniform doubles: the bit stream numpy keeps stable across
-versions).  Arrays too large to commit (the 3-D case) are stored as a
+versions).  Arrays too large to commit (the 3-D cases) are stored as a
 seeded sample of entries, their max |.| and sum of squares, and projections
 on seeded random vectors, all size-independent checks.
 """
@@ -41,7 +43,15 @@ def spec(name, directory):
         return workloads.irregular_2d(directory)
     if name == "c3":
         return workloads.directional_3d(directory)
+    if name == "c5":
+        return workloads.steep_3d(directory)
     raise KeyError(name)
+
+
+SAMPLED = ("c3", "c5")  # cases stored as size-independent records
+# width of the modal envelope (fraction of n): the M = 7 tank needs a milder
+# spectrum, since the order-M terms grow like (k eta)^M
+ENVELOPE = {"c5": 0.05}
 
 
 def oracle_tank(w):
@@ -63,13 +73,13 @@ def _envelope(n, frac):
     return np.exp(-(np.arange(n) / max(frac * n, 1.0)) ** 2)
 
 
-def modal_state(n1, n2, n3a, omega, seed=2024, amp=1e-3):
+def modal_state(n1, n2, n3a, omega, seed=2024, amp=1e-3, frac=0.2):
     """The 10 modal arrays of solveHOS2 (G1, G2, a_add_1, a_add_2,
     a_add_ramp, a_add_3, a1st, eta1st, a2nd, eta2nd); first-order
     wavemaker: the second- and third-order arrays are zero."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    env = _envelope(n1, 0.2)[:, None] * _envelope(n2, 0.2)[None, :]
-    enva = _envelope(n3a, 0.3)[:, None] * _envelope(n2, 0.2)[None, :]
+    env = _envelope(n1, frac)[:, None] * _envelope(n2, frac)[None, :]
+    enva = _envelope(n3a, 0.3)[:, None] * _envelope(n2, frac)[None, :]
     G1 = amp * _uniform(rng, (n1, n2)) * env
     G2 = amp * _uniform(rng, (n1, n2)) * env * omega
     G2[0, 0] = 0.0
@@ -82,11 +92,11 @@ def modal_state(n1, n2, n3a, omega, seed=2024, amp=1e-3):
     return [G1, G2, a1, za.copy(), ar, za.copy(), a1st, e1st, z.copy(), z.copy()]
 
 
-def physical_state(o, seed=2025, amp=1e-3):
+def physical_state(o, seed=2025, amp=1e-3, frac=0.2):
     """The 10 arrays of runge4_adapt2 (eta, phis, a_add_1, a_add_2,
     a_add_ramp, a_add_3, eta1st, eta2nd, a1st, a2nd): eta and phis in space
     (F2S of seeded modes), the rest as in modal_state."""
-    m = modal_state(o.n1, o.n2, o.n3_add, o.omega, seed, amp)
+    m = modal_state(o.n1, o.n2, o.n3_add, o.omega, seed, amp, frac)
     eta = o.fourier.F2S(m[0])
     phis = o.fourier.F2S(m[1] / np.where(o.omega > 0, o.omega, 1.0))
     return [eta, phis, m[2], m[3], m[4], m[5], m[7], m[9], m[6], m[8]]

@@ -1,13 +1,14 @@
 """Write the oracle fixtures of the benchmark tank configurations
-(tests/golden/baseline_{c1,c2,c3}.npz; cases in tests/baseline_cases.py):
+(tests/golden/baseline_{c1,c2,c3,c5}.npz; cases in tests/baseline_cases.py):
 
-  python tests/golden/make_baseline_fixtures.py [c1 c2 c3]
+  python tests/golden/make_baseline_fixtures.py [--threads N] [c1 c2 c3 c5]
 
 Per case: one solveHOS2 on a seeded modal state, one runge4_adapt2 on a
 seeded physical state (after one right-hand side at the step's start time,
 which sets the wavemaker state the step's first volume correction reads),
 and, for c1 and c2, the time loop from the initial condition with the probe
-records.  Single-threaded oracle; c3 takes a few minutes.
+records.  The oracle's transforms use N threads (default 1); c5 takes
+several minutes.
 """
 import os
 import sys
@@ -26,9 +27,9 @@ import baseline_cases as bc  # noqa: E402
 LOOP_T = {"c1": None, "c2": 10.0}   # simulated seconds of the time loop (None: the whole run)
 
 
-def rhs_case(w, out, full):
+def rhs_case(name, w, out, full):
     o = bc.oracle_tank(w)
-    y = bc.modal_state(o.n1, o.n2, o.n3_add, o.omega)
+    y = bc.modal_state(o.n1, o.n2, o.n3_add, o.omega, frac=bc.ENVELOPE.get(name, 0.2))
     out["rhs_alpha_prev"] = np.array([o._alpha[0]])
     out["rhs_pos_top"] = np.array([o._pos[0][o.n3 - 1, 0]])
     k = o.solveHOS2({key: a.copy() for key, a in zip(bc.KEYS, y)}, bc.RHS_DT, bc.RHS_T)
@@ -39,11 +40,11 @@ def rhs_case(w, out, full):
             out.update(bc.summarize("rhs_" + key, k[key], 100 + i))
 
 
-def step_case(w, out, full):
+def step_case(name, w, out, full):
     o = bc.oracle_tank(w)
     zero = bc.zero_state(o)
     o.solveHOS2({key: a for key, a in zip(bc.KEYS, zero)}, 0.0, bc.STEP_T0)
-    st = bc.physical_state(o)
+    st = bc.physical_state(o, frac=bc.ENVELOPE.get(name, 0.2))
     h = 0.8 * o.delt
     res, err, deta, _ = o.runge4_adapt2(bc.STEP_T0, *[a.copy() for a in st], h)
     out["step_h"] = np.array([h])
@@ -75,9 +76,9 @@ def make(name):
     out = {}
     with tempfile.TemporaryDirectory() as tmp:
         w = bc.spec(name, tmp)
-        full = name != "c3"
-        rhs_case(w, out, full)
-        step_case(w, out, full)
+        full = name not in bc.SAMPLED
+        rhs_case(name, w, out, full)
+        step_case(name, w, out, full)
         if name in LOOP_T:
             loop_case(w, out, LOOP_T[name])
     np.savez_compressed(os.path.join(HERE, f"baseline_{name}.npz"), **out)
@@ -85,5 +86,10 @@ def make(name):
 
 
 if __name__ == "__main__":
-    for n in (sys.argv[1:] or ["c1", "c2", "c3"]):
+    args = sys.argv[1:]
+    if args[:1] == ["--threads"]:
+        import oracle.hos_oracle as ho
+        ho.set_workers(int(args[1]))
+        args = args[2:]
+    for n in (args or ["c1", "c2", "c3", "c5"]):
         make(n)
