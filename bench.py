@@ -817,6 +817,9 @@ def main():
                     help="run one step inside a cudaProfilerStart/Stop range (for ncu) and exit")
     ap.add_argument("--profile-roofline", action="store_true",
                     help="run the roofline transform once inside a cudaProfilerStart/Stop range and exit")
+    ap.add_argument("--profile-n2", type=int, default=0,
+                    help="with --profile-roofline: a narrower tank of the same x length (n2 modes, same p2), "
+                         "so that a full ncu capture of the x pass holds a few GB on the device")
     args = ap.parse_args()
     if args.workload == "tc_gemm":
         run_profile_gemm(args) if args.profile_step else run_tc_gemm(args)
@@ -829,6 +832,8 @@ def main():
         return
     with tempfile.TemporaryDirectory() as tmp:
         w = _single_tank(args.workload, tmp)
+        if args.profile_n2 > 0:
+            w = dict(w, n2=args.profile_n2)
         if args.profile_roofline:
             run_profile_roofline(args, w)
         elif args.profile_step:
