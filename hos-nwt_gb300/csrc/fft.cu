@@ -34,8 +34,11 @@
 // bound by the FP64 pipe, not by HBM: the design minimises FP64 instructions
 // per output (an FFT instead of the O(N^1.5) or O(N^2) sums) and keeps every
 // SM busy (one CTA per group of line pairs, 8 warps each).
+#include <cuda.h>
+
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -68,15 +71,42 @@ struct FftJob {
   int epi;
   int pairs;                 // line pairs per CTA
   const FftDesc* desc;
+  // TMA staging of a y pass (lines contiguous): the CTA's lines x N points
+  // arrive as tma_nbox boxes of tma_by points, tma_box_bytes apart in
+  // shared memory, through the job's tensor map
+  int tma;
+  int tma_by, tma_nbox, tma_box_bytes;
 };
 
 template <int NJ>
 struct FftBatchT {
+  CUtensorMap tmap[NJ];      // 64-byte aligned: first member of a 64-byte aligned struct
   FftJob job[NJ];
   int start[NJ + 1];
   int njobs;
   AccEpi acc;
 };
+
+constexpr unsigned kTmaSpinLimit = 1u << 22;  // mbarrier polls before a TMA wait gives up
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// Wait for phase 0 of the mbarrier; false after kTmaSpinLimit polls.
+__device__ __forceinline__ bool tma_wait(uint64_t* bar) {
+  const unsigned a = smem_addr(bar);
+  for (unsigned it = 0; it < kTmaSpinLimit; ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
 
 // Shared-memory index of complex element i of an FFT buffer: one 16-byte
 // slot of padding per 8 elements, so that the stride-R writes of the first
@@ -352,10 +382,11 @@ __device__ double2* run_fft(const FftStages& F, double2* a, double2* b, int P) {
 // buffers of pairs x (D + 1) padded elements; the outputs of the 2 pairs
 // lines (D + 1 each) are staged in whichever buffer the FFT leaves free.
 template <int NJ>
-__global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const FftBatchT<NJ> b) {
-  extern __shared__ __align__(16) double2 fsm[];
+__global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const __grid_constant__ FftBatchT<NJ> b) {
+  extern __shared__ __align__(128) double2 fsm[];
   __shared__ double red[kFW][kFMaxLines];
   __shared__ double2 z0s[kFMaxLines / 2], a0s[kFMaxLines / 2];
+  __shared__ __align__(8) uint64_t tma_bar;
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const FftJob& J = b.job[jb];
@@ -378,9 +409,50 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const F
   const double* __restrict__ wr = J.win ? J.win + (long long)(valid ? line : 0) * J.win_sl : nullptr;
   const int jlo = J.jlo, jend = min(J.jhi, J.nin);
   // input j over the interior weight (the end weights enter at j = 0)
+  // y passes with TMA: the CTA's NL lines x N points land in the second
+  // buffer (unused until the first FFT stage), point-major, one box of
+  // tma_by points per tma_box_bytes
+  const bool tma = J.tma != 0;
+  const double* stage = reinterpret_cast<const double*>(
+      (reinterpret_cast<uintptr_t>(B) + 127) & ~static_cast<uintptr_t>(127));
+  if (tma) {
+    if (tid == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&tma_bar)) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(&tma_bar)),
+                   "r"((unsigned)(J.tma_nbox * J.tma_by * NL * 8))
+                   : "memory");
+      for (int bx = 0; bx < J.tma_nbox; ++bx) {
+        const char* dst = reinterpret_cast<const char*>(stage) + (size_t)bx * J.tma_box_bytes;
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+            "[%4];" ::"r"(smem_addr(dst)),
+            "l"(&b.tmap[jb]), "r"(line0), "r"(bx * J.tma_by), "r"(smem_addr(&tma_bar))
+            : "memory");
+      }
+    }
+    // every thread waits; the block decides together, so that the barrier
+    // below is reached by all of its threads or by none
+    if (__syncthreads_and(tma_wait(&tma_bar) ? 1 : 0) == 0) {
+      // a copy that never lands: poison the tile, so that the step's error
+      // estimate becomes NaN and the host reports HOSNWT_ERR_NAN
+      double* st = const_cast<double*>(stage);
+      for (int i = tid; i < J.tma_nbox * J.tma_box_bytes / 8; i += kFT) st[i] = __longlong_as_double(-1LL);
+      __syncthreads();
+    }
+  }
   auto U = [&](int j) -> double {
     if (!valid || j < jlo || j >= jend) return 0.0;
-    double v = __ldg(x + (long long)j * J.in_sk);
+    double v;
+    if (tma) {
+      const int bx = j / J.tma_by;
+      v = stage[(size_t)bx * (J.tma_box_bytes / 8) + (size_t)(j - bx * J.tma_by) * NL + l];
+    } else {
+      v = __ldg(x + (long long)j * J.in_sk);
+    }
     if (wr) v *= __ldg(wr + (long long)j * J.win_sk);
     return v;
   };
@@ -557,7 +629,10 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const F
 template <int NJ>
 FftBatchT<NJ> shrink_fft(const FftBatchT<kMaxJobs>& b) {
   FftBatchT<NJ> s{};
-  for (int i = 0; i < b.njobs; ++i) s.job[i] = b.job[i];
+  for (int i = 0; i < b.njobs; ++i) {
+    s.job[i] = b.job[i];
+    s.tmap[i] = b.tmap[i];
+  }
   for (int i = 0; i <= b.njobs; ++i) s.start[i] = b.start[i];
   s.njobs = b.njobs;
   s.acc = b.acc;
@@ -574,6 +649,15 @@ void with_fft_capacity(int njobs, Fn&& f) {
 }
 
 // ---------------------------------------------------------------- host side
+
+// HOSNWT_FFT_TMA=0 in the environment keeps the y passes on plain loads
+bool fft_tma_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("HOSNWT_FFT_TMA");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 
 int fft_mode() {
   static const int m = [] {
@@ -964,6 +1048,56 @@ size_t fft_smem(const FftPlanInfo& f, int P) {
 // line pairs per CTA: enough butterflies per stage for the 8 warps, enough
 // CTAs for the SMs, shared memory within budget; lines-contiguous (y)
 // passes take at least two pairs so that a warp's loads fill 32-byte sectors
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn fft_encode_fn() {
+  static const EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      return (EncodeTiledFn)p;
+    return (EncodeTiledFn) nullptr;
+  }();
+  return fn;
+}
+
+// TMA staging of a y pass (lines contiguous, points strided by in_sk): a
+// 2-D tensor map of nlines x N doubles and boxes of NL lines x by points.
+// Every rule a tiled copy has is checked here, else the pass keeps its
+// plain loads: a 16-byte aligned base, a 16-byte multiple stride, an inner
+// box extent of NL x 8 bytes (NL even, and every CTA's first line even),
+// box smem offsets on 128-byte boundaries inside the second FFT buffer.
+void setup_tma(FftJob& f, CUtensorMap* map, const FftPlanInfo& plan, int N) {
+  f.tma = 0;
+  const int P = f.pairs, NL = 2 * P;
+  if (f.in_sl != 1 || f.in_sk <= 1 || f.win || plan.mode == FFT_BLUESTEIN || NL % 2) return;
+  if (reinterpret_cast<uintptr_t>(f.in) % 16 != 0 || (f.in_sk * 8) % 16 != 0 || f.in_sk * 8 >= (1LL << 40)) return;
+  if (f.nlines < 1 || N < 2) return;
+  const int nbox = (N + 255) / 256;
+  const int by = (N + nbox - 1) / nbox;
+  const long long box_bytes = ((long long)by * NL * 8 + 127) / 128 * 128;
+  const long long cap = 16LL * padded((long long)P * (plan.D + 1)) - 127;
+  if ((long long)nbox * box_bytes > cap) return;
+  const EncodeTiledFn enc = fft_encode_fn();
+  if (!enc) return;
+  const cuuint64_t dims[2] = {(cuuint64_t)f.nlines, (cuuint64_t)N};
+  const cuuint64_t strides[1] = {(cuuint64_t)(f.in_sk * 8)};
+  const cuuint32_t box[2] = {(cuuint32_t)NL, (cuuint32_t)by};
+  const cuuint32_t estr[2] = {1, 1};
+  if (enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(f.in), dims, strides, box, estr,
+          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return;
+  f.tma = 1;
+  f.tma_by = by;
+  f.tma_nbox = nbox;
+  f.tma_box_bytes = (int)box_bytes;
+}
+
 int pick_pairs(const AxisJob& J, const FftPlanInfo& f, int nsm) {
   const bool ymode = (J.in_sk != 1);
   int P = ymode ? 8 : 4;
@@ -1022,6 +1156,7 @@ void launch_fft_jobs(const AxisBatch& in, const FftPlanInfo* const* plan, const 
     f.desc = plan[i]->dev;
     f.pairs = pick_pairs(J, *plan[i], tb.nsm);
     smem = std::max(smem, fft_smem(*plan[i], f.pairs));
+    if (fft_tma_enabled()) setup_tma(f, &b.tmap[i], *plan[i], J.N);
     b.start[i] = total;
     total += (J.nlines + 2 * f.pairs - 1) / (2 * f.pairs);
     g_xform_fmas += (double)J.nlines * plan[i]->cost_line;
