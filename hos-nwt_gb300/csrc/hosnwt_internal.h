@@ -52,6 +52,10 @@ struct PerDeviceOnce {
   }
 };
 
+// Set while a graph is captured whose kernels must be fully serialised
+// (a body graph that does not accept programmatic dependencies).
+extern thread_local bool g_launch_no_pdl;
+
 template <typename... KArgs, typename... Args>
 inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
                               cudaStream_t st, Args&&... args) {
@@ -64,7 +68,7 @@ inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, siz
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = g_launch_no_pdl ? 0 : 1;
   return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 
@@ -84,8 +88,8 @@ inline cudaError_t launch_pdl_cluster(void (*kern)(KArgs...), dim3 grid, dim3 bl
   attr[1].val.clusterDim.x = cluster;
   attr[1].val.clusterDim.y = 1;
   attr[1].val.clusterDim.z = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 2;
+  cfg.attrs = g_launch_no_pdl ? attr + 1 : attr;
+  cfg.numAttrs = g_launch_no_pdl ? 1 : 2;
   return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 

@@ -949,6 +949,12 @@ void free_device(Ctx& c) {
   c.ev0 = c.ev1 = nullptr;
   if (c.step_graph) cudaGraphExecDestroy(c.step_graph);
   c.step_graph = nullptr;
+  if (c.loop_graph) cudaGraphExecDestroy(c.loop_graph);
+  c.loop_graph = nullptr;
+  if (c.ctl_dev) cudaFree(c.ctl_dev);
+  c.ctl_dev = nullptr;
+  if (c.ctl_host) cudaFreeHost(c.ctl_host);
+  c.ctl_host = nullptr;
   for (void* p : c.allocs)
     if (p) cudaFree(p);
   c.allocs.clear();
@@ -1083,6 +1089,7 @@ extern "C" int hosnwt_get_info(const hosnwt_ctx* h, hosnwt_info* info) {
   info->kernels_per_step = c.kernels_per_step;
   info->device_ms = c.dev_ms;
   info->fmas_per_step = c.fmas_per_step;
+  info->step_control = c.loop_state == 0 ? 0 : (c.loop_state < 0 ? 1 : (c.loop_pdl ? 2 : 3));
   return HOSNWT_OK;
 }
 
@@ -1232,9 +1239,152 @@ static int advance(Ctx& c, double time_next, double* h_rk_io, int* n_acc, int* n
   return cuda_check(c, "advance");
 }
 
+// ---------------------------------------------------------------------------
+// Step control on the device.  An output interval runs as one graph:
+//   copy the control block in -> WHILE { k_ctl_begin, the RK4(5) step,
+//   k_ctl_end (decision, loop condition), k_accept_ctl } -> copy it out
+// so that the host waits once per interval instead of once per step.
+// HOSNWT_DEVICE_LOOP=0 keeps the host loop of advance().
+// ---------------------------------------------------------------------------
+static bool device_loop_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("HOSNWT_DEVICE_LOOP");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+static const int kMaxLoopSteps = 1 << 24;  // attempted steps per interval before the loop stops
+
+// Capture the body into the WHILE node of a fresh graph and instantiate it.
+static bool try_build_loop(Ctx& c, bool pdl) {
+  const Params& P = c.P;
+  cudaGraph_t g = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+  bool ok = false;
+  do {
+    cudaGraphConditionalHandle cond;
+    if (cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) break;
+    cudaGraphNode_t n_in = nullptr, n_loop = nullptr, n_out = nullptr;
+    if (cudaGraphAddMemcpyNode1D(&n_in, g, nullptr, 0, c.ctl_dev, c.ctl_host, sizeof(StepCtl),
+                                 cudaMemcpyHostToDevice) != cudaSuccess)
+      break;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    if (cudaGraphAddNode(&n_loop, g, &n_in, nullptr, 1, &np) != cudaSuccess) break;
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    CtlParams cp{};
+    cp.toler = P.toler;
+    cp.dt_stab = P.dt_stab;
+    cp.delt_out = P.delt_out;
+    cp.Tramp = P.Tramp;
+    cp.iramp = P.iramp;
+    cp.max_iters = kMaxLoopSteps;
+    cp.cond = cond;
+    if (cudaStreamBeginCaptureToGraph(c.st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+        cudaSuccess)
+      break;
+    g_launch_no_pdl = !pdl;
+    const double f0 = g_xform_fmas;
+    enqueue_ctl_step(c, c.ctl_dev, cp, c.st);
+    g_xform_fmas = f0;
+    g_launch_no_pdl = false;
+    cudaGraph_t captured = nullptr;
+    if (cudaStreamEndCapture(c.st, &captured) != cudaSuccess) break;
+    if (cudaGraphAddMemcpyNode1D(&n_out, g, &n_loop, 1, c.ctl_host, c.ctl_dev, sizeof(StepCtl),
+                                 cudaMemcpyDeviceToHost) != cudaSuccess)
+      break;
+    if (cudaGraphInstantiate(&c.loop_graph, g, 0) != cudaSuccess) {
+      c.loop_graph = nullptr;
+      break;
+    }
+    ok = true;
+  } while (false);
+  g_launch_no_pdl = false;
+  cudaGraphDestroy(g);
+  (void)cudaGetLastError();  // a failed attempt leaves no error behind
+  return ok;
+}
+
+// Build the loop graph on first use: with programmatic dependencies inside
+// the body if the runtime accepts them there, else fully serialised; -1
+// (the host loop) if neither builds.
+static void ensure_loop(Ctx& c) {
+  if (c.loop_state != 0) return;
+  c.loop_state = -1;
+  if (!device_loop_enabled() || !c.step_graph) return;
+  if (!c.ctl_dev && cudaMalloc((void**)&c.ctl_dev, sizeof(StepCtl)) != cudaSuccess) {
+    c.ctl_dev = nullptr;
+    (void)cudaGetLastError();
+    return;
+  }
+  if (!c.ctl_host && cudaMallocHost((void**)&c.ctl_host, sizeof(StepCtl)) != cudaSuccess) {
+    c.ctl_host = nullptr;
+    (void)cudaGetLastError();
+    return;
+  }
+  if (try_build_loop(c, true)) {
+    c.loop_state = 1;
+    c.loop_pdl = true;
+  } else if (try_build_loop(c, false)) {
+    c.loop_state = 1;
+    c.loop_pdl = false;
+  }
+}
+
+// Launch one interval of the device loop (the host's h_rk, time_cur and
+// endramp go in through the pinned block); finish_loop collects it.
+static int launch_loop(Ctx& c, double time_next, double h_rk) {
+  StepCtl& b = *c.ctl_host;
+  std::memset(&b, 0, sizeof(StepCtl));
+  b.time_cur = c.time_cur;
+  b.h_rk = h_rk;
+  b.time_next = time_next;
+  b.endramp = c.endramp;
+  timed_begin(c);
+  if (cudaGraphLaunch(c.loop_graph, c.st) != cudaSuccess) return cuda_check(c, "loop graph launch");
+  timed_end(c);
+  return HOSNWT_OK;
+}
+
+static int finish_loop(Ctx& c, double* h_rk_io, int* n_acc, int* n_rej) {
+  if (cudaStreamSynchronize(c.st) != cudaSuccess) return cuda_check(c, "advance");
+  timed_collect(c);
+  const StepCtl& b = *c.ctl_host;
+  c.n_rhs += 5LL * b.iters;
+  c.time_cur = b.time_cur;
+  c.endramp = b.endramp;
+  *h_rk_io = b.h_rk;
+  if (n_acc) *n_acc = b.n_acc;
+  if (n_rej) *n_rej = b.n_rej;
+  if (b.status == 1) {
+    c.err = "non-finite error estimate";
+    return HOSNWT_ERR_NAN;
+  }
+  if (b.status == 2) return fail(c, HOSNWT_ERR_DT_UNDERFLOW, "more than %d attempted steps in one interval",
+                                 kMaxLoopSteps);
+  return cuda_check(c, "advance");
+}
+
+static int advance_any(Ctx& c, double time_next, double* h_rk_io, int* n_acc, int* n_rej) {
+  ensure_loop(c);
+  if (c.loop_state != 1) return advance(c, time_next, h_rk_io, n_acc, n_rej);
+  if (!(c.time_cur < time_next)) {
+    if (n_acc) *n_acc = 0;
+    if (n_rej) *n_rej = 0;
+    return HOSNWT_OK;
+  }
+  const int rc = launch_loop(c, time_next, *h_rk_io);
+  if (rc) return rc;
+  return finish_loop(c, h_rk_io, n_acc, n_rej);
+}
+
 extern "C" int hosnwt_advance(hosnwt_ctx* h, double time_next, double* h_rk, int* n_acc, int* n_rej) {
   if (!h || !h_rk) return HOSNWT_ERR_ARG;
-  return advance(h->c, time_next, h_rk, n_acc, n_rej);
+  return advance_any(h->c, time_next, h_rk, n_acc, n_rej);
 }
 
 extern "C" int hosnwt_probes(hosnwt_ctx* h, double* out) {
@@ -1521,7 +1671,7 @@ extern "C" int hosnwt_run(hosnwt_ctx* h, const char* results_dir) {
     double time_next = c.time_cur + P.delt_out;
     if (time_next > P.T_stop + P.delt_out) time_next = P.T_stop + P.delt_out;
     double h_rk = delt;
-    rc = advance(c, time_next, &h_rk, nullptr, nullptr);
+    rc = advance_any(c, time_next, &h_rk, nullptr, nullptr);
     if (rc) break;
     delt = h_rk;
     rc = check_slope(c, nullptr);
@@ -1633,6 +1783,10 @@ extern "C" int hosnwt_transform(hosnwt_ctx* h, int grid, int dir, int csx, int c
 
 extern "C" int hosnwt_advance_many(hosnwt_ctx* const* ctxs, int n, const double* time_next, double* h_rk) {
   if (!ctxs || n <= 0 || !time_next || !h_rk) return HOSNWT_ERR_ARG;
+  // The device-controlled loop of hosnwt_advance (one graph launch per tank
+  // and interval) was measured slower here: 64 tanks advanced 1 s each took
+  // 18.2 s with every tank's loop graph in flight at once, 15.2 s with the
+  // per-step relaunch below.
   // Independent tanks, each on its own stream with its own step graph and
   // the step control of HOS-NWT.f90:498-571.  Each tank is relaunched as
   // soon as its own step has finished (polled with an event), so tanks of

@@ -35,6 +35,11 @@ inline int nblk(long long n, int t = kEW) { return (int)((n + t - 1) / t); }
 // ---------------------------------------------------------------------------
 // deterministic "last block" reductions (no spin-waits)
 // ---------------------------------------------------------------------------
+// Maximum that keeps a NaN (fmax drops it): a NaN anywhere in a reduced
+// field reaches the error estimate, which the step control rejects as
+// non-finite (HOSNWT_ERR_NAN).
+__device__ __forceinline__ double nan_max(double a, double b) { return (a != a || b != b) ? a + b : fmax(a, b); }
+
 template <int OP>  // 0 sum, 1 max
 __device__ double block_reduce(double v) {
   __shared__ double sh[32];
@@ -42,7 +47,7 @@ __device__ double block_reduce(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const double u = __shfl_down_sync(0xffffffffu, v, o);
-    v = OP == 0 ? v + u : fmax(v, u);
+    v = OP == 0 ? v + u : nan_max(v, u);
   }
   __syncthreads();
   if (lane == 0) sh[w] = v;
@@ -53,7 +58,7 @@ __device__ double block_reduce(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const double u = __shfl_down_sync(0xffffffffu, v, o);
-      v = OP == 0 ? v + u : fmax(v, u);
+      v = OP == 0 ? v + u : nan_max(v, u);
     }
   }
   return v;  // valid in thread 0
@@ -1100,14 +1105,14 @@ __global__ void k_rk_err(const double* __restrict__ part, int nblocks, double* s
   __shared__ double mx[10];
   if (threadIdx.x < 10) {
     double m = 0.0;
-    for (int b = 0; b < nblocks; ++b) m = fmax(m, part[b * 10 + threadIdx.x]);
+    for (int b = 0; b < nblocks; ++b) m = nan_max(m, part[b * 10 + threadIdx.x]);
     mx[threadIdx.x] = m;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     const double tiny = 2.220446049250313080847263336181640625e-16;
     double err = 0.0;
-    for (int s = 0; s < 5; ++s) err = fmax(err, mx[5 + s] / (mx[s] + tiny));
+    for (int s = 0; s < 5; ++s) err = nan_max(err, mx[5 + s] / (mx[s] + tiny));
     sc[SC_ERR] = err;
   }
 }
@@ -1203,8 +1208,8 @@ __global__ void k_diagnostics(const double* __restrict__ eta, const double* __re
     ek += w * ((phis[i] + phi_add[i]) * deta[i]);
   }
   for (long long i = threadIdx.x; i < nB; i += blockDim.x) {
-    mx = fmax(mx, fabs(etax[i]));
-    my = fmax(my, fabs(etay[i]));
+    mx = nan_max(mx, fabs(etax[i]));
+    my = nan_max(my, fabs(etay[i]));
   }
   v = block_reduce<0>(v);
   if (threadIdx.x == 0) out[0] = v;
@@ -1975,6 +1980,107 @@ void enqueue_step(Ctx& c, cudaStream_t st) {
                                      (int)nN, P.igeom, P.d_hinge, P.xlen, d.etam, d.phim, d.NL1,
                                      d.part + 10 * (long long)nb, d.counter);
   E.xf({E.F2S_N(d.etam, d.eta_c), E.F2S_N(d.phim, d.phis_c), E.F2S_N(d.NL1, d.deta_c)});
+}
+
+// ---------------------------------------------------------------------------
+// Step control on the device (HOS-NWT.f90:498-571, as advance() in host.cpp)
+// ---------------------------------------------------------------------------
+// h_loc = h_rk, cut to reach time_next (HOS-NWT.f90:500-504); the step
+// reads t_o and h_loc from the scalar slots
+__global__ void k_ctl_begin(const StepCtl* __restrict__ ctl, double* __restrict__ sc) {
+  pdl_wait();
+  if (threadIdx.x == 0) {
+    const double rem = ctl->time_next - ctl->time_cur;
+    sc[SC_T0] = ctl->time_cur;
+    sc[SC_H] = (rem < ctl->h_rk) ? rem : ctl->h_rk;
+  }
+}
+
+// Accept / reject, dt_correc with the reference's REAL(4) constants, the
+// clamps and the end of the ramp (HOS-NWT.f90:522-563); sets the loop
+// condition: continue while time_cur < time_next.
+__global__ void k_ctl_end(StepCtl* __restrict__ ctl, const double* __restrict__ sc, CtlParams p) {
+  pdl_wait();
+  if (threadIdx.x != 0) return;
+  const double tiny = 2.220446049250313080847263336181640625e-16;  // epsilon(1.0_rp)
+  const double error = sc[SC_ERR];
+  const double h_loc = sc[SC_H];
+  const double t = ctl->time_cur;
+  double h_rk = ctl->h_rk;
+  ctl->err = error;
+  ctl->iters += 1;
+  ctl->accept = 0;
+  ctl->end_ramp_now = 0;
+  if (!isfinite(error)) {
+    ctl->status = 1;
+    cudaGraphSetConditional(p.cond, 0);
+    return;
+  }
+  double dt_correc;
+  if (error > p.toler && h_rk > 0.001 * 0.95 * p.dt_stab) {
+    dt_correc = (double)0.9f * pow(error / p.toler, -(double)(1.0f / 4.0f));
+    ctl->n_rej += 1;
+    if (fabs(p.Tramp - (t + h_loc)) <= tiny && p.Tramp > t) ctl->endramp = 0;
+  } else {
+    if (p.iramp == 1 && p.Tramp - (t + h_loc) <= tiny && p.Tramp > t && ctl->endramp != 1) {
+      ctl->end_ramp_now = 1;
+      ctl->endramp = 1;
+    }
+    ctl->accept = 1;
+    ctl->time_cur = t + h_loc;
+    dt_correc = fabs(error) < tiny ? 2.0 : 0.9 * pow(error / p.toler, -(1.0 / 4.0));
+    ctl->n_acc += 1;
+  }
+  h_rk = h_rk * dt_correc;
+  h_rk = fmin(fmin(h_rk, 0.95 * p.dt_stab), p.delt_out);
+  h_rk = fmax(fmax(h_rk, 0.0001 * 0.95 * p.dt_stab), 0.0001 * p.delt_out);
+  ctl->h_rk = h_rk;
+  int go = ctl->time_cur < ctl->time_next ? 1 : 0;
+  if (go && ctl->iters >= p.max_iters) {
+    ctl->status = 2;
+    go = 0;
+  }
+  cudaGraphSetConditional(p.cond, go);
+}
+
+// The accept of enqueue_accept, predicated on the decision: y0 <- ynew
+// (less a_add_ramp in a_add_1 at the end of the ramp, HOS-NWT.f90:546-550),
+// eta, phis, deta <- their candidates.
+__global__ void k_accept_ctl(const StepCtl* __restrict__ ctl, double* __restrict__ y0,
+                             const double* __restrict__ ynew, long long S, long long off1, long long offr,
+                             long long nA, double* __restrict__ eta, const double* __restrict__ eta_c,
+                             long long n2N, double* __restrict__ deta, const double* __restrict__ deta_c,
+                             long long nN) {
+  pdl_wait();
+  if (!ctl->accept) return;
+  const bool ramp = ctl->end_ramp_now != 0;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < S + n2N + nN; i += stride) {
+    if (i < S) {
+      double v = ynew[i];
+      if (ramp && i >= off1 && i < off1 + nA) v -= ynew[offr + (i - off1)];
+      y0[i] = v;
+    } else if (i < S + n2N) {
+      eta[i - S] = eta_c[i - S];
+    } else {
+      deta[i - S - n2N] = deta_c[i - S - n2N];
+    }
+  }
+}
+
+void enqueue_ctl_step(Ctx& c, StepCtl* ctl, const CtlParams& p, cudaStream_t st) {
+  const Dev& d = c.d;
+  const StateLayout& L = c.L;
+  const long long nN = (long long)c.P.n1 * c.P.n2;
+  const long long nA = (long long)c.P.n3a * c.P.n2;
+  launch_pdl(k_ctl_begin, dim3(1), dim3(32), 0, st, (const StepCtl*)ctl, d.sc);
+  enqueue_step(c, st);
+  launch_pdl(k_ctl_end, dim3(1), dim3(32), 0, st, ctl, (const double*)d.sc, p);
+  const long long tot = L.size + 3 * nN;
+  const int blocks = (int)std::min<long long>((tot + kEW - 1) / kEW, 4LL * 152);
+  launch_pdl(k_accept_ctl, dim3(blocks), dim3(kEW), 0, st, (const StepCtl*)ctl, d.y0, (const double*)d.ynew,
+             L.size, L.off[S_AADD1], L.off[S_AADDR], nA, d.eta, (const double*)d.eta_c, 2 * nN, d.deta,
+             (const double*)d.deta_c, nN);
 }
 
 void enqueue_accept(Ctx& c, bool end_ramp, cudaStream_t st) {

@@ -105,6 +105,27 @@ struct Dev {
   double *host_io = nullptr;    // pinned staging of hosnwt_runge4_adapt2's arrays
 };
 
+// Step control of HOS-NWT.f90:498-571 on the device: one output interval
+// runs as a CUDA-graph WHILE loop whose body is one RK4(5) step, the
+// accept/reject decision and the accept.  The block is copied in before
+// the loop and out after it.
+struct StepCtl {
+  double time_cur, h_rk, time_next, err;
+  int n_acc, n_rej;
+  int endramp;               // the reference's endramp flag
+  int accept;                // 1: the step just taken is accepted
+  int end_ramp_now;          // 1: this accept removes a_add_ramp from a_add_1
+  int status;                // 0 ok, 1 non-finite error estimate, 2 step limit
+  int iters;                 // attempted steps
+  int pad;
+};
+struct CtlParams {
+  double toler, dt_stab, delt_out, Tramp;
+  int iramp;
+  int max_iters;
+  cudaGraphConditionalHandle cond;
+};
+
 struct Ctx {
   hosnwt_input in{};
   hosnwt_numerics num{};
@@ -132,6 +153,11 @@ struct Ctx {
   static constexpr int kPowEvents = 8;
   cudaEvent_t ev_pw[kPowEvents] = {};  // eta powers final up to a given order
   cudaGraphExec_t step_graph = nullptr;
+  cudaGraphExec_t loop_graph = nullptr;  // device-controlled output interval (built on first use)
+  int loop_state = 0;                     // 0 not tried, 1 built, -1 unavailable (host loop)
+  bool loop_pdl = false;                  // the loop body keeps programmatic launches
+  StepCtl* ctl_dev = nullptr;
+  StepCtl* ctl_host = nullptr;            // pinned
   double time_cur = 0.0;
   int endramp = 0;
   long long n_rhs = 0;
@@ -156,6 +182,10 @@ void enqueue_probes(Ctx& c, cudaStream_t st);
 void enqueue_diagnostics(Ctx& c, double* out, cudaStream_t st);
 void enqueue_slope_filter(Ctx& c, int dir, cudaStream_t st);
 void enqueue_accept(Ctx& c, bool end_ramp, cudaStream_t st);
+// Body of the device-controlled loop: set t_o and h_loc from the control
+// block, one RK4(5) step, the accept/reject decision (sets the loop
+// condition), the accept.
+void enqueue_ctl_step(Ctx& c, StepCtl* ctl, const CtlParams& p, cudaStream_t st);
 void enqueue_set_scalar(Ctx& c, int slot, double v, cudaStream_t st);
 
 }  // namespace hos

@@ -1817,6 +1817,7 @@ void launch_batch_y(AxisBatch& in, const Tables& tb, cudaStream_t st) {
 }  // namespace
 
 thread_local double g_xform_fmas = 0.0;
+thread_local bool g_launch_no_pdl = false;
 const bool g_fused_enabled = [] {
   const char* e = std::getenv("HOSNWT_FUSED_PASS");
   return e && e[0] == '1';

@@ -59,7 +59,7 @@ class HosInfo(ctypes.Structure):
         [(n, ctypes.c_double) for n in ("Tscale", "xlen", "ylen", "dt_stab", "delt", "delt_out",
                                         "T_stop", "toler", "time_cur")] + \
         [("nprobes", ctypes.c_int), ("n_rhs", ctypes.c_longlong), ("kernels_per_step", ctypes.c_int),
-         ("device_ms", ctypes.c_double), ("fmas_per_step", ctypes.c_double)]
+         ("device_ms", ctypes.c_double), ("fmas_per_step", ctypes.c_double), ("step_control", ctypes.c_int)]
 
 
 _lib = None

@@ -78,6 +78,12 @@ typedef struct hosnwt_info {
                               (CUDA events on the context's stream) */
   double fmas_per_step;    /* FP64 FMAs of the transform passes in one step
                               graph (terms x outputs of the algorithm run) */
+  int step_control;        /* where hosnwt_advance decides accept/reject
+                              (HOS-NWT.f90:498-571): 0 not yet chosen (no
+                              advance so far), 1 the host, once per step;
+                              2 the device, a CUDA-graph loop per output
+                              interval with programmatic launches; 3 the
+                              device, kernels fully serialised in the loop */
 } hosnwt_info;
 
 typedef struct hosnwt_ctx hosnwt_ctx;
