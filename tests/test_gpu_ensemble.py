@@ -1,5 +1,6 @@
 """Batched ensemble (hosnwt_advance_many): independent tanks advanced
-together give the same states as the same tanks advanced one by one."""
+together give the same states, to rounding, as the same tanks advanced
+one by one."""
 import numpy as np
 import pytest
 
@@ -29,6 +30,10 @@ def test_advance_many_matches_single(lib):
     for a, b in zip(single, batch):
         ea, pa, _ = a.get_state()
         eb, pb, _ = b.get_state()
-        assert a.info()["time_cur"] == b.info()["time_cur"]
-        assert np.array_equal(ea, eb) and np.array_equal(pa, pb)
+        # single advance runs the step control on the device, advance_many on
+        # the host: the two evaluate pow() of the step correction on different
+        # processors, so the states agree to rounding, not bit for bit
+        assert abs(a.info()["time_cur"] - b.info()["time_cur"]) <= 1e-12
+        assert np.max(np.abs(ea - eb)) <= 1e-10 * np.max(np.abs(eb))
+        assert np.max(np.abs(pa - pb)) <= 1e-10 * np.max(np.abs(pb))
         assert np.max(np.abs(ea)) > 0.0
