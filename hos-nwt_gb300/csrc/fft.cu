@@ -30,10 +30,18 @@
 // a_m = x(g^m), b_q = exp(-2 pi i g^-q / D), a cyclic convolution of length
 // D - 1 done with two FFTs of that length.
 //
-// GB300 runs FP64 at about 2 operations per clock per SM, so these passes are
-// bound by the FP64 pipe, not by HBM: the design minimises FP64 instructions
-// per output (an FFT instead of the O(N^1.5) or O(N^2) sums) and keeps every
-// SM busy (one CTA per group of line pairs, 8 warps each).
+// GB300 runs FP64 (and conversions between FP64 and FP32) at about 2
+// operations per clock per SM, FP32 at 128: in FP64 these passes are bound by
+// the FP64 pipe, not by HBM.  So by default the complex DFT runs in
+// double-float arithmetic (pairs of FP32 numbers, 48-bit significands, see
+// the arithmetic section), on one line per complex sequence: the paired
+// form above gets its odd outputs from prefix sums, whose error grows like
+// sqrt(N) and lands on the high modes that the HOS orders multiply by k^m;
+// the folded form of one line (see the kernel) has no such sums, and its
+// errors match the FP64 paired form.  The inputs, weights and scales move
+// between FP64 and double-float by integer bit manipulation, so that a pass
+// issues about one FP64 instruction per output.  HOSNWT_FFT_DF=0 keeps the
+// FP64 paired form.
 #include <cuda.h>
 
 #include <algorithm>
@@ -41,6 +49,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "hosnwt_internal.h"
@@ -49,11 +58,12 @@ namespace hos {
 
 namespace {
 
-constexpr int kFT = 256;           // threads per CTA (8 warps)
+constexpr int kFT = 256;           // threads per CTA (8 warps); 512 for Bluestein launches
+constexpr int kFTBig = 512;
 #ifndef HOSNWT_FFT_MIN_BLOCKS
 #define HOSNWT_FFT_MIN_BLOCKS 3    // resident CTAs per SM the register budget is cut for
 #endif
-constexpr int kFW = kFT / 32;
+constexpr int kFWMax = kFTBig / 32;
 constexpr int kFMaxLines = 16;     // lines per CTA (8 line pairs)
 constexpr size_t kFftSmemMax = 220 * 1024;  // dynamic shared memory of one CTA
 
@@ -69,7 +79,7 @@ struct FftJob {
   double f0, fm, fl;         // output scales at k = 0, interior k, k = D (times w / 4)
   int sin_kind;
   int epi;
-  int pairs;                 // line pairs per CTA
+  int pairs;                 // complex sequences per CTA: line pairs, or lines in double-float
   const FftDesc* desc;
   // TMA staging of a y pass (lines contiguous): the CTA's lines x N points
   // arrive as tma_nbox boxes of tma_by points, tma_box_bytes apart in
@@ -114,54 +124,237 @@ __device__ __forceinline__ bool tma_wait(uint64_t* bar) {
 __device__ __forceinline__ int pz(int i) { return i + (i >> 3); }
 __host__ __device__ constexpr long long padded(long long n) { return n + (n >> 3) + 1; }
 
+// ---------------------------------------------------------------- arithmetic
+//
+// The FFT core runs on one of two element types of 16 bytes:
+//   double2  FP64 complex;
+//   dfc      double-float complex: each part is an unevaluated sum hi + lo of
+//            two FP32 numbers (|lo| <= ulp(hi) / 2, a 48-bit significand).
+// GB300 issues FP32 at 64 times its FP64 rate, and a double-float add or
+// product takes 7 to 19 FP32 instructions built on the error-free
+// transformations TwoSum (Knuth), FastTwoSum (Dekker) and TwoProd (an FMA
+// gives the exact error of a product), as in the double-double arithmetic of
+// Dekker (1971) and Hida, Li and Bailey (QD, 2001).  The add is the "sloppy"
+// form: its error is bounded by about 2 u^2 (|a| + |b|) with u = 2^-24, which
+// is what the normwise error of an FFT needs.  Every step is an explicit
+// round-to-nearest intrinsic, so that no contraction changes it.
+struct __align__(16) dfc {
+  float rh, ih, rl, il;  // real hi, imag hi, real lo, imag lo
+};
+struct dff {
+  float h, l;
+};
+
+template <typename T>
+struct Ar;
+template <>
+struct Ar<double2> {
+  using R = double;
+  __host__ __device__ static constexpr double k(double c) { return c; }
+};
+template <>
+struct Ar<dfc> {
+  using R = dff;
+  __host__ __device__ static constexpr dff k(double c) {
+    return dff{static_cast<float>(c), static_cast<float>(c - static_cast<double>(static_cast<float>(c)))};
+  }
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ dff fast_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return dff{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dff dadd(dff a, dff b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  return fast_two_sum(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dff dneg(dff a) { return dff{-a.h, -a.l}; }
+// c x
+__device__ __forceinline__ dff dmul(dff c, dff x) {
+  const float p = __fmul_rn(c.h, x.h);
+  float e = __fmaf_rn(c.h, x.h, -p);
+  e = __fmaf_rn(c.h, x.l, e);
+  e = __fmaf_rn(c.l, x.h, e);
+  return fast_two_sum(p, e);
+}
+// acc + c x
+__device__ __forceinline__ dff dfma(dff c, dff x, dff acc) {
+  const float p = __fmul_rn(c.h, x.h);
+  const float e1 = __fmaf_rn(c.h, x.h, -p);
+  float s, e2;
+  two_sum(acc.h, p, s, e2);
+  float lo = __fadd_rn(e1, __fadd_rn(e2, acc.l));
+  lo = __fmaf_rn(c.h, x.l, lo);
+  lo = __fmaf_rn(c.l, x.h, lo);
+  return fast_two_sum(s, lo);
+}
+// x y + u v
+__device__ __forceinline__ dff ddot2(dff x, dff y, dff u, dff v) {
+  const float p1 = __fmul_rn(x.h, y.h), p2 = __fmul_rn(u.h, v.h);
+  const float e1 = __fmaf_rn(x.h, y.h, -p1), e2 = __fmaf_rn(u.h, v.h, -p2);
+  float s, e;
+  two_sum(p1, p2, s, e);
+  float lo = __fadd_rn(e1, e2);
+  lo = __fmaf_rn(x.h, y.l, lo);
+  lo = __fmaf_rn(x.l, y.h, lo);
+  lo = __fmaf_rn(u.h, v.l, lo);
+  lo = __fmaf_rn(u.l, v.h, lo);
+  return fast_two_sum(s, __fadd_rn(lo, e));
+}
+
+// FP64 <-> double-float by bit manipulation: GB300 converts between FP64
+// and FP32 at its FP64 rate, the integer pipe is 30 times faster.  The
+// split truncates x to hi (24 significant bits) and the next 24 bits to lo,
+// then renormalises; |x| below 2^-126 becomes zero (far below the rounding
+// of any nonzero entry of a line), infinities and NaN pass to hi.
+__device__ __forceinline__ dff d2df(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff);
+  const unsigned long long m = b & 0xfffffffffffffULL;
+  if (e == 0x7ff) return dff{__uint_as_float(sign | 0x7f800000u | (m ? 0x400000u : 0u)), 0.f};
+  const int ef = e - 1023 + 127;
+  if (ef <= 0) return dff{__uint_as_float(sign), 0.f};
+  if (ef >= 255) return dff{__uint_as_float(sign | 0x7f800000u), 0.f};
+  const float hi = __uint_as_float(sign | ((unsigned)ef << 23) | (unsigned)(m >> 29));
+  const unsigned ml = (unsigned)(m & 0x1fffffffu);  // the 29 bits below hi
+  if (ml == 0u) return dff{hi, 0.f};
+  const int lz = __clz(ml);                          // >= 3
+  const int el = e - 1023 - 52 + (31 - lz) + 127;    // exponent of the leading bit of ml
+  if (el <= 0) return dff{hi, 0.f};
+  const float lo = __uint_as_float(sign | ((unsigned)el << 23) | ((ml << (lz + 1)) >> 9));
+  return fast_two_sum(hi, lo);
+}
+// exact FP64 value of an FP32 number (FP32 subnormals to zero)
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e == 0u) return __longlong_as_double((long long)sign);
+  const unsigned long long ed = (e == 255u) ? 0x7ffULL : (unsigned long long)(e - 127u + 1023u);
+  return __longlong_as_double((long long)(sign | (ed << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+// hi + lo, exact in FP64 for a normalised pair: one FP64 add
+__device__ __forceinline__ double df2d(dff a) { return f2d_bits(a.h) + f2d_bits(a.l); }
+__device__ __forceinline__ dff dscale(float s, dff a) { return dff{s * a.h, s * a.l}; }  // s a power of two
+
+__device__ __forceinline__ dff dre(dfc a) { return dff{a.rh, a.rl}; }
+__device__ __forceinline__ dff dim(dfc a) { return dff{a.ih, a.il}; }
+__device__ __forceinline__ dfc mkc(dff r, dff i) { return dfc{r.h, i.h, r.l, i.l}; }
+
+// complex operations on both element types (the double2 forms are the FP64
+// expressions of the pass; each dfc form is its double-float counterpart)
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ double2 cmi(double2 a) { return make_double2(a.y, -a.x); }  // -i a
+__device__ __forceinline__ double2 cconj(double2 a) { return make_double2(a.x, -a.y); }
+__device__ __forceinline__ double2 chalf(double2 a) { return make_double2(0.5 * a.x, 0.5 * a.y); }
+__device__ __forceinline__ double2 cfma(double c, double2 x, double2 acc) {  // acc + c x
+  return make_double2(fma(c, x.x, acc.x), fma(c, x.y, acc.y));
+}
+__device__ __forceinline__ double2 csc(double c, double2 x) { return make_double2(c * x.x, c * x.y); }
+__device__ __forceinline__ double2 cmulconj(double2 a, double2 c) {  // conj(a) c
+  return make_double2(fma(a.x, c.x, a.y * c.y), fma(a.x, c.y, -a.y * c.x));
+}
+// exp(-i pi / 4) o and exp(-3 i pi / 4) o, r = sqrt(1/2)
+__device__ __forceinline__ double2 crot1(double r, double2 o) { return make_double2(r * (o.x + o.y), r * (o.y - o.x)); }
+__device__ __forceinline__ double2 crot3(double r, double2 o) {
+  return make_double2(r * (o.y - o.x), -r * (o.x + o.y));
+}
+__device__ __forceinline__ double tre(double2 c) { return c.x; }
+__device__ __forceinline__ double tnim(double2 c) { return -c.y; }
+__device__ __forceinline__ double2 ldt(const double2* p) { return __ldg(p); }
+__device__ __forceinline__ void put_part(double2* e, int part, double v) { reinterpret_cast<double*>(e)[part] = v; }
+template <typename T>
+__device__ __forceinline__ T czero();
+template <>
+__device__ __forceinline__ double2 czero<double2>() { return make_double2(0.0, 0.0); }
+
+__device__ __forceinline__ dfc cmul(dfc a, dfc b) {
+  return mkc(ddot2(dre(a), dre(b), dneg(dim(a)), dim(b)), ddot2(dre(a), dim(b), dim(a), dre(b)));
+}
+__device__ __forceinline__ dfc cadd(dfc a, dfc b) { return mkc(dadd(dre(a), dre(b)), dadd(dim(a), dim(b))); }
+__device__ __forceinline__ dfc csub(dfc a, dfc b) {
+  return mkc(dadd(dre(a), dneg(dre(b))), dadd(dim(a), dneg(dim(b))));
+}
+__device__ __forceinline__ dfc cmi(dfc a) { return dfc{a.ih, -a.rh, a.il, -a.rl}; }
+__device__ __forceinline__ dfc cconj(dfc a) { return dfc{a.rh, -a.ih, a.rl, -a.il}; }
+__device__ __forceinline__ dfc chalf(dfc a) {
+  return dfc{0.5f * a.rh, 0.5f * a.ih, 0.5f * a.rl, 0.5f * a.il};
+}
+__device__ __forceinline__ dfc cfma(dff c, dfc x, dfc acc) { return mkc(dfma(c, dre(x), dre(acc)), dfma(c, dim(x), dim(acc))); }
+__device__ __forceinline__ dfc csc(dff c, dfc x) { return mkc(dmul(c, dre(x)), dmul(c, dim(x))); }
+__device__ __forceinline__ dfc cmulconj(dfc a, dfc c) { return cmul(cconj(a), c); }
+__device__ __forceinline__ dfc crot1(dff r, dfc o) {
+  return mkc(dmul(r, dadd(dre(o), dim(o))), dmul(r, dadd(dim(o), dneg(dre(o)))));
+}
+__device__ __forceinline__ dfc crot3(dff r, dfc o) {
+  return mkc(dmul(r, dadd(dim(o), dneg(dre(o)))), dneg(dmul(r, dadd(dre(o), dim(o)))));
+}
+__device__ __forceinline__ dff tre(dfc c) { return dre(c); }
+__device__ __forceinline__ dff tnim(dfc c) { return dneg(dim(c)); }
+__device__ __forceinline__ dfc ldt(const dfc* p) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  return dfc{v.x, v.y, v.z, v.w};
+}
+template <>
+__device__ __forceinline__ dfc czero<dfc>() { return dfc{0.f, 0.f, 0.f, 0.f}; }
+
+template <typename T>
+__device__ __forceinline__ const T* tab(const double2* p) {
+  return reinterpret_cast<const T*>(p);
+}
 
 // forward DFT of R points in registers, X_k = sum_t v_t exp(-2 pi i t k / R)
-template <int R>
-__device__ __forceinline__ void dft(double2* v);
-
-template <>
-__device__ __forceinline__ void dft<2>(double2* v) {
-  const double2 a = v[0], b = v[1];
+template <typename T>
+__device__ __forceinline__ void dft2(T* v) {
+  const T a = v[0], b = v[1];
   v[0] = cadd(a, b);
   v[1] = csub(a, b);
 }
 
-template <>
-__device__ __forceinline__ void dft<3>(double2* v) {
-  const double s = 0.86602540378443864676;  // sin(2 pi / 3)
-  const double2 t = cadd(v[1], v[2]), d = csub(v[1], v[2]);
-  const double2 m = make_double2(fma(-0.5, t.x, v[0].x), fma(-0.5, t.y, v[0].y));
+template <typename T>
+__device__ __forceinline__ void dft3(T* v) {
+  constexpr auto s = Ar<T>::k(0.86602540378443864676);  // sin(2 pi / 3)
+  constexpr auto ms = Ar<T>::k(-0.86602540378443864676);
+  const T t = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+  const T m = csub(v[0], chalf(t));
   v[0] = cadd(v[0], t);
-  v[1] = make_double2(fma(s, d.y, m.x), fma(-s, d.x, m.y));   // m - i s d
-  v[2] = make_double2(fma(-s, d.y, m.x), fma(s, d.x, m.y));   // m + i s d
+  v[1] = cfma(s, cmi(d), m);   // m - i s d
+  v[2] = cfma(ms, cmi(d), m);  // m + i s d
 }
 
-template <>
-__device__ __forceinline__ void dft<4>(double2* v) {
-  const double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]), c = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+template <typename T>
+__device__ __forceinline__ void dft4(T* v) {
+  const T a = cadd(v[0], v[2]), b = csub(v[0], v[2]), c = cadd(v[1], v[3]), d = csub(v[1], v[3]);
   v[0] = cadd(a, c);
   v[2] = csub(a, c);
   v[1] = cadd(b, cmi(d));
   v[3] = csub(b, cmi(d));
 }
 
-template <>
-__device__ __forceinline__ void dft<5>(double2* v) {
-  const double c1 = 0.30901699437494742410, c2 = -0.80901699437494742410;  // cos(2 pi / 5), cos(4 pi / 5)
-  const double s1 = 0.95105651629515357212, s2 = 0.58778525229247312917;   // sin(2 pi / 5), sin(4 pi / 5)
-  const double2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
-  const double2 d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
-  const double2 x0 = v[0];
-  const double2 a1 = make_double2(fma(c2, t2.x, fma(c1, t1.x, x0.x)), fma(c2, t2.y, fma(c1, t1.y, x0.y)));
-  const double2 a2 = make_double2(fma(c1, t2.x, fma(c2, t1.x, x0.x)), fma(c1, t2.y, fma(c2, t1.y, x0.y)));
-  const double2 b1 = make_double2(fma(s2, d2.x, s1 * d1.x), fma(s2, d2.y, s1 * d1.y));
-  const double2 b2 = make_double2(fma(-s1, d2.x, s2 * d1.x), fma(-s1, d2.y, s2 * d1.y));
+template <typename T>
+__device__ __forceinline__ void dft5(T* v) {
+  // cos(2 pi / 5), cos(4 pi / 5), sin(2 pi / 5), sin(4 pi / 5)
+  constexpr auto c1 = Ar<T>::k(0.30901699437494742410), c2 = Ar<T>::k(-0.80901699437494742410);
+  constexpr auto s1 = Ar<T>::k(0.95105651629515357212), s2 = Ar<T>::k(0.58778525229247312917);
+  constexpr auto ms1 = Ar<T>::k(-0.95105651629515357212);
+  const T t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+  const T d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
+  const T x0 = v[0];
+  const T a1 = cfma(c2, t2, cfma(c1, t1, x0));
+  const T a2 = cfma(c1, t2, cfma(c2, t1, x0));
+  const T b1 = cfma(s2, d2, csc(s1, d1));
+  const T b2 = cfma(ms1, d2, csc(s2, d1));
   v[0] = cadd(x0, cadd(t1, t2));
   v[1] = cadd(a1, cmi(b1));
   v[4] = csub(a1, cmi(b1));
@@ -169,27 +362,23 @@ __device__ __forceinline__ void dft<5>(double2* v) {
   v[3] = csub(a2, cmi(b2));
 }
 
-template <>
-__device__ __forceinline__ void dft<7>(double2* v) {
+template <typename T>
+__device__ __forceinline__ void dft7(T* v) {
   // cos / sin (2 pi q / 7), q = 1, 2, 3
-  const double c1 = 0.62348980185873353053, c2 = -0.22252093395631440429, c3 = -0.90096886790241912624;
-  const double s1 = 0.78183148246802980871, s2 = 0.97492791218182360702, s3 = 0.43388373911755812048;
-  const double2 x0 = v[0];
-  const double2 t1 = cadd(v[1], v[6]), t2 = cadd(v[2], v[5]), t3 = cadd(v[3], v[4]);
-  const double2 d1 = csub(v[1], v[6]), d2 = csub(v[2], v[5]), d3 = csub(v[3], v[4]);
-  double2 a1, a2, a3, b1, b2, b3;
-  a1.x = fma(c3, t3.x, fma(c2, t2.x, fma(c1, t1.x, x0.x)));
-  a1.y = fma(c3, t3.y, fma(c2, t2.y, fma(c1, t1.y, x0.y)));
-  a2.x = fma(c1, t3.x, fma(c3, t2.x, fma(c2, t1.x, x0.x)));
-  a2.y = fma(c1, t3.y, fma(c3, t2.y, fma(c2, t1.y, x0.y)));
-  a3.x = fma(c2, t3.x, fma(c1, t2.x, fma(c3, t1.x, x0.x)));
-  a3.y = fma(c2, t3.y, fma(c1, t2.y, fma(c3, t1.y, x0.y)));
-  b1.x = fma(s3, d3.x, fma(s2, d2.x, s1 * d1.x));
-  b1.y = fma(s3, d3.y, fma(s2, d2.y, s1 * d1.y));
-  b2.x = fma(-s1, d3.x, fma(-s3, d2.x, s2 * d1.x));
-  b2.y = fma(-s1, d3.y, fma(-s3, d2.y, s2 * d1.y));
-  b3.x = fma(s2, d3.x, fma(-s1, d2.x, s3 * d1.x));
-  b3.y = fma(s2, d3.y, fma(-s1, d2.y, s3 * d1.y));
+  constexpr auto c1 = Ar<T>::k(0.62348980185873353053), c2 = Ar<T>::k(-0.22252093395631440429);
+  constexpr auto c3 = Ar<T>::k(-0.90096886790241912624);
+  constexpr auto s1 = Ar<T>::k(0.78183148246802980871), s2 = Ar<T>::k(0.97492791218182360702);
+  constexpr auto s3 = Ar<T>::k(0.43388373911755812048);
+  constexpr auto ms1 = Ar<T>::k(-0.78183148246802980871), ms3 = Ar<T>::k(-0.43388373911755812048);
+  const T x0 = v[0];
+  const T t1 = cadd(v[1], v[6]), t2 = cadd(v[2], v[5]), t3 = cadd(v[3], v[4]);
+  const T d1 = csub(v[1], v[6]), d2 = csub(v[2], v[5]), d3 = csub(v[3], v[4]);
+  const T a1 = cfma(c3, t3, cfma(c2, t2, cfma(c1, t1, x0)));
+  const T a2 = cfma(c1, t3, cfma(c3, t2, cfma(c2, t1, x0)));
+  const T a3 = cfma(c2, t3, cfma(c1, t2, cfma(c3, t1, x0)));
+  const T b1 = cfma(s3, d3, cfma(s2, d2, csc(s1, d1)));
+  const T b2 = cfma(ms1, d3, cfma(ms3, d2, csc(s2, d1)));
+  const T b3 = cfma(s2, d3, cfma(ms1, d2, csc(s3, d1)));
   v[0] = cadd(x0, cadd(t1, cadd(t2, t3)));
   v[1] = cadd(a1, cmi(b1));
   v[6] = csub(a1, cmi(b1));
@@ -199,17 +388,17 @@ __device__ __forceinline__ void dft<7>(double2* v) {
   v[4] = csub(a3, cmi(b3));
 }
 
-template <>
-__device__ __forceinline__ void dft<8>(double2* v) {
-  const double r = 0.70710678118654752440;  // sqrt(1/2)
-  double2 e[4] = {v[0], v[2], v[4], v[6]};
-  double2 o[4] = {v[1], v[3], v[5], v[7]};
-  dft<4>(e);
-  dft<4>(o);
+template <typename T>
+__device__ __forceinline__ void dft8(T* v) {
+  constexpr auto r = Ar<T>::k(0.70710678118654752440);  // sqrt(1/2)
+  T e[4] = {v[0], v[2], v[4], v[6]};
+  T o[4] = {v[1], v[3], v[5], v[7]};
+  dft4(e);
+  dft4(o);
   // o_k *= exp(-i pi k / 4)
-  o[1] = make_double2(r * (o[1].x + o[1].y), r * (o[1].y - o[1].x));
+  o[1] = crot1(r, o[1]);
   o[2] = cmi(o[2]);
-  o[3] = make_double2(r * (o[3].y - o[3].x), -r * (o[3].x + o[3].y));
+  o[3] = crot3(r, o[3]);
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     v[k] = cadd(e[k], o[k]);
@@ -217,25 +406,35 @@ __device__ __forceinline__ void dft<8>(double2* v) {
   }
 }
 
+template <int R, typename T>
+__device__ __forceinline__ void dft(T* v) {
+  if constexpr (R == 2) dft2(v);
+  else if constexpr (R == 3) dft3(v);
+  else if constexpr (R == 4) dft4(v);
+  else if constexpr (R == 5) dft5(v);
+  else if constexpr (R == 7) dft7(v);
+  else dft8(v);
+}
+
 // One Stockham stage of radix R (R in {2, 3, 4, 5, 7, 8}) on P sequences of
 // length L, src -> dst; Ns is the product of the radices of earlier stages.
 // Butterfly j takes src[j + t L/R], twiddled by exp(-2 pi i t k / (Ns R))
 // with k = j mod Ns, and writes dst[(j - k) R + k + t Ns].
-template <int R>
-__device__ void st_small(const double2* __restrict__ src, double2* __restrict__ dst, int L, int Ns, int P,
-                         const double2* __restrict__ stw) {
+template <int R, typename T>
+__device__ void st_small(const T* __restrict__ src, T* __restrict__ dst, int L, int Ns, int P,
+                         const T* __restrict__ stw) {
   const int nb = L / R;
   const int W = P * nb;
-  for (int w = threadIdx.x; w < W; w += kFT) {
+  for (int w = threadIdx.x; w < W; w += blockDim.x) {
     const int p = w / nb, j = w - p * nb;
     const int off = p * L;
     const int k = j % Ns;
-    double2 v[R];
+    T v[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) v[t] = src[pz(off + j + t * nb)];
     if (k != 0) {
 #pragma unroll
-      for (int t = 1; t < R; ++t) v[t] = cmul(v[t], __ldg(stw + (t - 1) * Ns + k));
+      for (int t = 1; t < R; ++t) v[t] = cmul(v[t], ldt(stw + (t - 1) * Ns + k));
     }
     dft<R>(v);
     const int base = off + (j - k) * R + k;
@@ -250,29 +449,30 @@ __device__ void st_small(const double2* __restrict__ src, double2* __restrict__ 
 // each work item forms the outputs o and R - o of one butterfly:
 //   X_o = A - i B, X_{R-o} = A + i B,
 //   A = v_0 + sum_t s_t cos(2 pi t o / R),  B = sum_t d_t sin(2 pi t o / R).
-__device__ void st_generic(double2* __restrict__ src, double2* __restrict__ dst, int L, int Ns, int R, int P,
-                           const double2* __restrict__ tw, const double2* __restrict__ stw) {
+template <typename T>
+__device__ void st_generic(T* __restrict__ src, T* __restrict__ dst, int L, int Ns, int R, int P,
+                           const T* __restrict__ tw, const T* __restrict__ stw) {
   const int nb = L / R, h = (R + 1) / 2;
   const int rs = L / R;
   const int W1 = P * nb * (h - 1);
-  for (int w = threadIdx.x; w < W1; w += kFT) {
+  for (int w = threadIdx.x; w < W1; w += blockDim.x) {
     const int j = w % nb;
     const int r = w / nb;
     const int t = 1 + r % (h - 1);
     const int p = r / (h - 1);
     const int off = p * L;
-    double2 va = src[pz(off + j + t * nb)], vb = src[pz(off + j + (R - t) * nb)];
+    T va = src[pz(off + j + t * nb)], vb = src[pz(off + j + (R - t) * nb)];
     const int k = j % Ns;
     if (k != 0) {
-      va = cmul(va, __ldg(stw + (t - 1) * Ns + k));
-      vb = cmul(vb, __ldg(stw + (R - t - 1) * Ns + k));
+      va = cmul(va, ldt(stw + (t - 1) * Ns + k));
+      vb = cmul(vb, ldt(stw + (R - t - 1) * Ns + k));
     }
     src[pz(off + j + t * nb)] = cadd(va, vb);
     src[pz(off + j + (R - t) * nb)] = csub(va, vb);
   }
   __syncthreads();
   const int W2 = P * nb * h;
-  for (int w = threadIdx.x; w < W2; w += kFT) {
+  for (int w = threadIdx.x; w < W2; w += blockDim.x) {
     const int j = w % nb;
     const int r = w / nb;
     const int o = r % h;
@@ -280,27 +480,25 @@ __device__ void st_generic(double2* __restrict__ src, double2* __restrict__ dst,
     const int off = p * L;
     const int k = j % Ns;
     const int base = off + (j - k) * R + k;
-    const double2 v0 = src[pz(off + j)];
+    const T v0 = src[pz(off + j)];
     if (o == 0) {
-      double2 a = v0;
+      T a = v0;
       for (int t = 1; t < h; ++t) a = cadd(a, src[pz(off + j + t * nb)]);
       dst[pz(base)] = a;
       continue;
     }
-    double2 A = v0, B = make_double2(0.0, 0.0);
+    T A = v0, B = czero<T>();
     int q = o;
     for (int t = 1; t < h; ++t) {
-      const double2 c = __ldg(tw + q * rs);  // (cos, -sin)(2 pi q / R)
-      const double2 st = src[pz(off + j + t * nb)], dt = src[pz(off + j + (R - t) * nb)];
-      A.x = fma(st.x, c.x, A.x);
-      A.y = fma(st.y, c.x, A.y);
-      B.x = fma(dt.x, -c.y, B.x);
-      B.y = fma(dt.y, -c.y, B.y);
+      const T c = ldt(tw + q * rs);  // (cos, -sin)(2 pi q / R)
+      const T st = src[pz(off + j + t * nb)], dt = src[pz(off + j + (R - t) * nb)];
+      A = cfma(tre(c), st, A);
+      B = cfma(tnim(c), dt, B);
       q += o;
       if (q >= R) q -= R;
     }
-    dst[pz(base + o * Ns)] = make_double2(A.x + B.y, A.y - B.x);
-    dst[pz(base + (R - o) * Ns)] = make_double2(A.x - B.y, A.y + B.x);
+    dst[pz(base + o * Ns)] = cadd(A, cmi(B));
+    dst[pz(base + (R - o) * Ns)] = csub(A, cmi(B));
   }
 }
 
@@ -309,38 +507,38 @@ __device__ void st_generic(double2* __restrict__ src, double2* __restrict__ dst,
 // Decimation in frequency: DFT, then twiddle the outputs; in time: twiddle
 // the inputs, then DFT.  Each butterfly reads and writes only its own
 // elements, so a stage needs no barrier inside it.
-template <int R, bool DIF>
-__device__ void ip_stage(double2* __restrict__ x, int L, int ld, int S, int P, const double2* __restrict__ tw) {
+template <int R, bool DIF, typename T>
+__device__ void ip_stage(T* __restrict__ x, int L, int ld, int S, int P, const T* __restrict__ tw) {
   const int m = S / R;
   const int nb = L / R;
-  for (int w = threadIdx.x; w < P * nb; w += kFT) {
+  for (int w = threadIdx.x; w < P * nb; w += blockDim.x) {
     const int p = w / nb, bj = w - p * nb;
     const int blk = bj / m, j = bj - blk * m;
     const int base = p * ld + blk * S + j;
-    double2 v[R];
+    T v[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) v[t] = x[pz(base + t * m)];
     if (!DIF && j != 0) {
 #pragma unroll
-      for (int t = 1; t < R; ++t) v[t] = cmul(v[t], __ldg(tw + (t - 1) * m + j));
+      for (int t = 1; t < R; ++t) v[t] = cmul(v[t], ldt(tw + (t - 1) * m + j));
     }
     dft<R>(v);
     if (DIF && j != 0) {
 #pragma unroll
-      for (int t = 1; t < R; ++t) v[t] = cmul(v[t], __ldg(tw + (t - 1) * m + j));
+      for (int t = 1; t < R; ++t) v[t] = cmul(v[t], ldt(tw + (t - 1) * m + j));
     }
 #pragma unroll
     for (int t = 0; t < R; ++t) x[pz(base + t * m)] = v[t];
   }
 }
 
-template <bool DIF>
-__device__ void ip_fft(const FftInplace& F, double2* x, int ld, int P) {
+template <bool DIF, typename T>
+__device__ void ip_fft(const FftInplace& F, T* x, int ld, int P) {
   for (int i = 0; i < F.nst; ++i) {
     const int s = DIF ? i : F.nst - 1 - i;
     int S = F.L;
     for (int q = 0; q < s; ++q) S /= F.rad[q];
-    const double2* tw = F.tw + F.off[s];
+    const T* tw = tab<T>(F.tw) + F.off[s];
     switch (F.rad[s]) {
       case 2: ip_stage<2, DIF>(x, F.L, ld, S, P, tw); break;
       case 3: ip_stage<3, DIF>(x, F.L, ld, S, P, tw); break;
@@ -355,11 +553,12 @@ __device__ void ip_fft(const FftInplace& F, double2* x, int ld, int P) {
 
 // Complex FFT of P sequences of length F.L held in a (a <-> b ping-pong);
 // returns the buffer that holds the result.
-__device__ double2* run_fft(const FftStages& F, double2* a, double2* b, int P) {
+template <typename T>
+__device__ T* run_fft(const FftStages& F, T* a, T* b, int P) {
   int Ns = 1;
   for (int s = 0; s < F.nst; ++s) {
     const int R = F.rad[s];
-    const double2* stw = F.stw + F.twoff[s];
+    const T* stw = tab<T>(F.stw) + F.twoff[s];
     switch (R) {
       case 2: st_small<2>(a, b, F.L, Ns, P, stw); break;
       case 3: st_small<3>(a, b, F.L, Ns, P, stw); break;
@@ -367,36 +566,44 @@ __device__ double2* run_fft(const FftStages& F, double2* a, double2* b, int P) {
       case 5: st_small<5>(a, b, F.L, Ns, P, stw); break;
       case 7: st_small<7>(a, b, F.L, Ns, P, stw); break;
       case 8: st_small<8>(a, b, F.L, Ns, P, stw); break;
-      default: st_generic(a, b, F.L, Ns, R, P, F.tw, stw); break;
+      default: st_generic(a, b, F.L, Ns, R, P, tab<T>(F.tw), stw); break;
     }
     __syncthreads();
     Ns *= R;
-    double2* t = a;
+    T* t = a;
     a = b;
     b = t;
   }
   return a;
 }
 
-// One CTA = `pairs` line pairs of one job.  Shared memory: two complex
-// buffers of pairs x (D + 1) padded elements; the outputs of the 2 pairs
-// lines (D + 1 each) are staged in whichever buffer the FFT leaves free.
-template <int NJ>
-__global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const __grid_constant__ FftBatchT<NJ> b) {
+// One CTA = `pairs` complex sequences of one job (line pairs, or lines in
+// double-float).  Shared memory: two complex buffers of pairs x (D + 1)
+// padded elements; the outputs of the CTA's lines (D + 1 each) are staged
+// in whichever buffer the FFT leaves free.
+// DF: the complex DFT runs in double-float (the job's desc then holds the
+// double-float tables) on one line per complex sequence, without the prefix
+// sums (see the load loop); the input weights, the pre- and post-processing
+// and the output scales stay FP64.
+template <int NJ, int NT, bool DF>
+__global__ void __launch_bounds__(NT, NT == kFT ? HOSNWT_FFT_MIN_BLOCKS : 1)
+    k_fft_pass(const __grid_constant__ FftBatchT<NJ> b) {
+  using T = typename std::conditional<DF, dfc, double2>::type;
   extern __shared__ __align__(128) double2 fsm[];
-  __shared__ double red[kFW][kFMaxLines];
-  __shared__ double2 z0s[kFMaxLines / 2], a0s[kFMaxLines / 2];
+  __shared__ double red[kFWMax][kFMaxLines];
+  __shared__ T z0s[kFMaxLines / 2], a0s[kFMaxLines / 2];
   __shared__ __align__(8) uint64_t tma_bar;
   int jb = 0;
   while (jb + 1 < b.njobs && (int)blockIdx.x >= b.start[jb + 1]) ++jb;
   const FftJob& J = b.job[jb];
   const FftDesc& F = *J.desc;
-  const int D = F.D, P = J.pairs, NL = 2 * P;
+  // P complex sequences per CTA: line pairs, or lines in double-float
+  const int D = F.D, P = J.pairs, NL = DF ? P : 2 * P;
   const int line0 = ((int)blockIdx.x - b.start[jb]) * NL;
   const bool blue = (F.mode == FFT_BLUESTEIN);
   const int zld = blue ? F.ip.L : D;  // stride between the pairs' sequences
-  double2* A = fsm;
-  double2* B = A + padded((long long)P * (D + 1));
+  T* A = reinterpret_cast<T*>(fsm);
+  T* B = A + padded((long long)P * (D + 1));
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   pdl_wait();
 
@@ -440,7 +647,7 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const _
       // a copy that never lands: poison the tile, so that the step's error
       // estimate becomes NaN and the host reports HOSNWT_ERR_NAN
       double* st = const_cast<double*>(stage);
-      for (int i = tid; i < J.tma_nbox * J.tma_box_bytes / 8; i += kFT) st[i] = __longlong_as_double(-1LL);
+      for (int i = tid; i < J.tma_nbox * J.tma_box_bytes / 8; i += blockDim.x) st[i] = __longlong_as_double(-1LL);
       __syncthreads();
     }
   }
@@ -458,7 +665,52 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const _
   };
   const bool is_sin = J.sin_kind != 0;
   double c1 = 0.0;
-  for (int w = tid; w < NL * D; w += kFT) {
+  if constexpr (DF) {
+    // One line per sequence, from the DFT of length 2D of the even (cos) or
+    // odd (sin) extension of the line, folded to length D: with
+    // s_j = u_j + u_{D-j}, r_j = u_j - u_{D-j} (and s_0 = 2 (u_0 + u_D),
+    // r_0 = 2 (u_0 - u_D)), W = DFT_D(w) gives every output directly:
+    //   cos  w_j = 2 (s_j + r_j sin(theta_j)) + 2 i r_j cos(theta_j),
+    //        4 C(2m) = Re W_m,   4 C(2m+1) = Im W_m
+    //   sin  w_j = 2 (r_j + s_j sin(theta_j)) + 2 i s_j cos(theta_j),  w_0 = 0,
+    //        4 S(2m) = -Im W_m,  4 S(2m+1) = Re W_m
+    // (the even outputs are the DFT of the symmetric part, the odd ones that
+    // of the Hermitian sequence r_j exp(-i theta_j), both real).  Unlike the
+    // prefix sums of the paired form, no output accumulates the errors of
+    // many others, so the error grows like log N, not sqrt N.
+    // the inputs, weights and trigonometric factors in double-float: no
+    // FP64 instruction on the way in
+    auto Ud = [&](int j) -> dff {
+      if (!valid || j < jlo || j >= jend) return dff{0.f, 0.f};
+      double v;
+      if (tma) {
+        const int bx = j / J.tma_by;
+        v = stage[(size_t)bx * (J.tma_box_bytes / 8) + (size_t)(j - bx * J.tma_by) * NL + l];
+      } else {
+        v = __ldg(x + (long long)j * J.in_sk);
+      }
+      dff d = d2df(v);
+      if (wr) d = dmul(d2df(__ldg(wr + (long long)j * J.win_sk)), d);
+      return d;
+    };
+    for (int w = tid; w < NL * D; w += blockDim.x) {
+      const int j = w / NL;
+      dff ua = Ud(j), ub = Ud(D - j);
+      const dfc cs = ldt(tab<dfc>(F.trig) + j);  // (cos, 2 sin)(theta_j)
+      dfc v;
+      if (j == 0) {
+        ua = dmul(d2df(J.e0), ua);
+        ub = dmul(d2df(J.eD), ub);
+        v = is_sin ? czero<dfc>() : mkc(dscale(4.f, dadd(ua, ub)), dscale(4.f, dadd(ua, dneg(ub))));
+      } else {
+        const dff sj = dadd(ua, ub), rj = dadd(ua, dneg(ub));
+        const dff a = is_sin ? sj : rj, c = is_sin ? rj : sj;
+        v = mkc(dfma(dim(cs), a, dscale(2.f, c)), dscale(2.f, dmul(dre(cs), a)));
+      }
+      A[pz(l * zld + j)] = v;
+    }
+  } else {
+  for (int w = tid; w < NL * D; w += blockDim.x) {
     const int j = w / NL;
     double ua = U(j), ub = U(D - j);
     const double2 cs = __ldg(F.trig + j);  // (cos, 2 sin)(theta_j)
@@ -474,9 +726,10 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const _
     } else {
       t = fma(cs.y, ua + ub, ua - ub);
     }
-    reinterpret_cast<double*>(A + pz((l >> 1) * zld + j))[l & 1] = t;
+    put_part(A + pz((l >> 1) * zld + j), l & 1, t);
   }
-  if (!is_sin) {
+  }
+  if (!DF && !is_sin) {
     // lanes with the same line: lane = l (mod NL)
     for (int off = 16; off >= NL; off >>= 1) c1 += __shfl_xor_sync(0xffffffffu, c1, off);
     if (lane < NL) red[warp][lane] = c1;
@@ -484,7 +737,7 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const _
   __syncthreads();
 
   // ---- the complex DFT of length D of every pair
-  double2* Z;
+  T* Z;
   double* O;  // NL x (D + 1) outputs, in the buffer the DFT leaves free
   if (F.mode == FFT_STOCKHAM) {
     Z = run_fft(F.fft, A, B, P);
@@ -493,53 +746,43 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const _
     // X_k = conj-chirp_k sum_j (z_j conj-chirp_j) chirp_{k-j}: a cyclic
     // convolution of length M >= 2 D + 2, in place in A
     const int M = zld;
-    for (int w = tid; w < P * M; w += kFT) {
+    for (int w = tid; w < P * M; w += blockDim.x) {
       const int j = w % M;
       const int idx = pz(w);
-      A[idx] = (j < D) ? cmul(A[idx], __ldg(F.chirp + j)) : make_double2(0.0, 0.0);
+      A[idx] = (j < D) ? cmul(A[idx], ldt(tab<T>(F.chirp) + j)) : czero<T>();
     }
     __syncthreads();
     ip_fft<true>(F.ip, A, M, P);
-    for (int w = tid; w < P * M; w += kFT) {
-      const double2 a = A[pz(w)], c = __ldg(F.hrev + w % M);
-      A[pz(w)] = make_double2(fma(a.x, c.x, a.y * c.y), fma(a.x, c.y, -a.y * c.x));  // conj(a) c
-    }
+    for (int w = tid; w < P * M; w += blockDim.x) A[pz(w)] = cmulconj(A[pz(w)], ldt(tab<T>(F.hrev) + w % M));
     __syncthreads();
     ip_fft<false>(F.ip, A, M, P);
-    for (int w = tid; w < P * D; w += kFT) {
+    for (int w = tid; w < P * D; w += blockDim.x) {
       const int p = w / D, k = w - p * D;
       const int idx = pz(p * M + k);
-      const double2 y = A[idx];
-      A[idx] = cmul(__ldg(F.chirp + k), make_double2(y.x, -y.y));
+      A[idx] = cmul(ldt(tab<T>(F.chirp) + k), cconj(A[idx]));
     }
     __syncthreads();
     Z = A;
     O = nullptr;  // rows in each pair's free tail, see orow
   } else {
     const int Ls = D - 1;
-    for (int w = tid; w < P * Ls; w += kFT) {
+    for (int w = tid; w < P * Ls; w += blockDim.x) {
       const int p = w / Ls, m = w - p * Ls;
       B[pz(p * Ls + m)] = A[pz(p * D + __ldg(F.gperm + m))];
     }
     if (tid < P) z0s[tid] = A[pz(tid * D)];
     __syncthreads();
     // z now lives in B (permuted) and z0s: A is free for the ping-pong
-    double2* S1 = run_fft(F.fft, B, A, P);
-    double2* S2 = (S1 == B) ? A : B;
+    T* S1 = run_fft(F.fft, B, A, P);
+    T* S2 = (S1 == B) ? A : B;
     if (tid < P) a0s[tid] = S1[pz(tid * Ls)];
-    for (int w = tid; w < P * Ls; w += kFT) {
-      const int m = w % Ls;
-      const double2 a = S1[pz(w)], c = __ldg(F.bconj + m);
-      // conj(a) * c
-      S2[pz(w)] = make_double2(fma(a.x, c.x, a.y * c.y), fma(a.x, c.y, -a.y * c.x));
-    }
+    for (int w = tid; w < P * Ls; w += blockDim.x) S2[pz(w)] = cmulconj(S1[pz(w)], ldt(tab<T>(F.bconj) + w % Ls));
     __syncthreads();
-    double2* Y = run_fft(F.fft, S2, S1, P);
+    T* Y = run_fft(F.fft, S2, S1, P);
     Z = (Y == A) ? B : A;
-    for (int w = tid; w < P * Ls; w += kFT) {
+    for (int w = tid; w < P * Ls; w += blockDim.x) {
       const int p = w / Ls, n = w - p * Ls;
-      const double2 y = Y[pz(w)], z0 = z0s[p];
-      Z[pz(p * D + __ldg(F.gscat + n))] = make_double2(z0.x + y.x, z0.y - y.y);
+      Z[pz(p * D + __ldg(F.gscat + n))] = cadd(z0s[p], cconj(Y[pz(w)]));
     }
     if (tid < P) Z[pz(tid * D)] = cadd(z0s[tid], a0s[tid]);
     __syncthreads();
@@ -549,13 +792,27 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const _
   // output row of line ll: D + 1 doubles
   auto orow = [&](int ll) -> double* {
     if (!blue) return O + (long long)ll * (D + 1);
+    if (DF) return reinterpret_cast<double*>(A + pz(ll * zld + D) + 1);
     return reinterpret_cast<double*>(A + pz((ll >> 1) * zld + D) + 1) + (ll & 1) * (D + 1);
   };
 
   // ---- unpack the two real spectra of each pair; even outputs and the
   // inputs of the odd-output prefix sums go to the output rows
   const int ne = D / 2, no = (D - 1) / 2;
-  for (int w = tid; w < P * (ne + 1); w += kFT) {
+  if constexpr (DF) {
+    // outputs scaled in double-float, one FP64 add each to leave it
+    const dff s0 = d2df(J.f0), sm = d2df(J.fm), sl = d2df(J.fl);
+    for (int w = tid; w < P * (ne + 1); w += blockDim.x) {
+      const int p = w / (ne + 1), m = w - p * (ne + 1);
+      const dfc W = Z[pz(p * zld + m)];
+      double* o = orow(p);
+      const int k = 2 * m;
+      o[k] = df2d(dmul(k == 0 ? s0 : (k == D ? sl : sm), is_sin ? dneg(dim(W)) : dre(W)));
+      if (m <= no) o[k + 1] = df2d(dmul(k + 1 == D ? sl : sm, is_sin ? dre(W) : dim(W)));
+    }
+    __syncthreads();
+  } else {
+  for (int w = tid; w < P * (ne + 1); w += blockDim.x) {
     const int p = w / (ne + 1), m = w - p * (ne + 1);
     const double2 z1 = Z[pz(p * zld + m)];
     const double2 z2 = Z[pz(p * zld + (m == 0 ? 0 : D - m))];
@@ -581,7 +838,7 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const _
   }
   if (!is_sin && tid < NL) {
     double s = 0.0;
-    for (int w = 0; w < kFW; ++w) s += red[w][tid];
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][tid];
     orow(tid)[1] = 4.0 * s;
   }
   __syncthreads();
@@ -590,7 +847,7 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const _
   {
     const int n = no + 1;
     const int c = (n + 31) / 32;
-    for (int ll = warp; ll < NL; ll += kFW) {
+    for (int ll = warp; ll < NL; ll += (int)(blockDim.x >> 5)) {
       double* o = orow(ll) + 1;
       const int i0 = min(lane * c, n), i1 = min(i0 + c, n);
       double s = 0.0;
@@ -610,16 +867,17 @@ __global__ void __launch_bounds__(kFT, HOSNWT_FFT_MIN_BLOCKS) k_fft_pass(const _
     }
   }
   __syncthreads();
+  }
 
   // ---- scale and store (line fastest, like the loads)
   if (valid) {
     double* __restrict__ out = J.out + (long long)line * J.out_sl;
     const double* o = orow(l);
-    for (int w = tid; w < NL * J.nout; w += kFT) {
+    for (int w = tid; w < NL * J.nout; w += blockDim.x) {
       const int k = w / NL;
       const bool active = (k >= J.klo) && (k < J.khi);
       const double sc = (k == 0) ? J.f0 : ((k == D) ? J.fl : J.fm);
-      const double y = active ? o[k] * sc : 0.0;
+      const double y = active ? (DF ? o[k] : o[k] * sc) : 0.0;  // double-float rows are scaled
       out[(long long)k * J.out_sk] = y;
       if (J.epi) acc_epilogue(b.acc, (long long)line * J.out_sl + (long long)k * J.out_sk, y);
     }
@@ -649,6 +907,25 @@ void with_fft_capacity(int njobs, Fn&& f) {
 }
 
 // ---------------------------------------------------------------- host side
+
+// HOSNWT_FFT_BIG=0 keeps Bluestein launches at 256 threads per CTA
+bool fft_big_ctas() {
+  static const bool on = [] {
+    const char* e = std::getenv("HOSNWT_FFT_BIG");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+// HOSNWT_FFT_DF=0 in the environment keeps the complex DFT of the passes in
+// FP64 instead of double-float
+bool fft_df_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("HOSNWT_FFT_DF");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
 
 // HOSNWT_FFT_TMA=0 in the environment keeps the y passes on plain loads
 bool fft_tma_enabled() {
@@ -795,6 +1072,17 @@ T* upload_vec(const std::vector<T>& v, std::vector<void*>& allocs) {
 
 using cld = std::complex<long double>;
 
+// double-float copy of an FP64 table: hi = fl32(x), lo = fl32(x - hi), the
+// layout of dfc (real hi, imag hi, real lo, imag lo)
+const double2* upload_df(const std::vector<double2>& v, std::vector<void*>& allocs) {
+  std::vector<float4> f(v.size());
+  for (size_t i = 0; i < v.size(); ++i) {
+    const float rh = (float)v[i].x, ih = (float)v[i].y;
+    f[i] = make_float4(rh, ih, (float)(v[i].x - (double)rh), (float)(v[i].y - (double)ih));
+  }
+  return reinterpret_cast<const double2*>(upload_vec(f, allocs));
+}
+
 cld unit_root(long long q, long long n) {  // exp(-2 pi i q / n)
   q %= n;
   if (q < 0) q += n;
@@ -876,12 +1164,17 @@ std::vector<int> dif_positions(int L, const std::vector<int>& rad) {
 
 namespace {
 
-// Stockham stages of length L with their twiddles
-bool upload_stages(const std::vector<int>& rad, int L, std::vector<void*>& allocs, FftStages* f) {
+// device copy of a table, FP64 or double-float
+const double2* upload_tab(const std::vector<double2>& v, bool df, std::vector<void*>& allocs) {
+  return df ? upload_df(v, allocs) : upload_vec(v, allocs);
+}
+
+// Stockham stages of length L with their twiddles (FP64 or double-float)
+bool upload_stages(const std::vector<int>& rad, int L, bool df, std::vector<void*>& allocs, FftStages* f) {
   f->L = L;
   f->nst = (int)rad.size();
   for (int s = 0; s < f->nst; ++s) f->rad[s] = rad[s];
-  f->tw = upload_vec(twiddles(L), allocs);
+  f->tw = upload_tab(twiddles(L), df, allocs);
   // stage twiddles exp(-2 pi i t k / (Ns R)) at (t - 1) Ns + k
   std::vector<double2> stw;
   long long Ns = 1;
@@ -896,12 +1189,12 @@ bool upload_stages(const std::vector<int>& rad, int L, std::vector<void*>& alloc
       }
     Ns *= R;
   }
-  f->stw = upload_vec(stw, allocs);
+  f->stw = upload_tab(stw, df, allocs);
   return f->tw && f->stw;
 }
 
 // In-place stages of length L with their twiddles
-bool upload_inplace(const std::vector<int>& rad, int L, std::vector<void*>& allocs, FftInplace* f) {
+bool upload_inplace(const std::vector<int>& rad, int L, bool df, std::vector<void*>& allocs, FftInplace* f) {
   f->L = L;
   f->nst = (int)rad.size();
   std::vector<double2> tw;
@@ -917,18 +1210,23 @@ bool upload_inplace(const std::vector<int>& rad, int L, std::vector<void*>& allo
       }
     S = m;
   }
-  f->tw = upload_vec(tw, allocs);
+  f->tw = upload_tab(tw, df, allocs);
   return f->tw != nullptr;
 }
 
 // shared memory of the Bluestein mode must hold the padded convolution
 constexpr long long kBlueMaxM = 12400;
 
+// time of the double-float DFT over its FP64 time (FP32 issues 64 times
+// faster, a double-float operation takes 7 to 19 FP32 instructions; 0.3 is
+// the ratio measured on the steep tank's passes)
+constexpr double kDfCost = 0.3;
+
 }  // namespace
 
 bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
   if (D < 8 || !out) return false;
-  FftDesc h{};
+  FftDesc h{}, hd{};  // FP64 and double-float tables
   h.D = D;
   // candidate algorithms and their FP64 instructions per complex DFT
   std::vector<int> rad_s, rad_r, rad_b;
@@ -947,17 +1245,28 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
     }
   }
   double fcost;
+  int mode;
   if (cost_s <= cost_r && cost_s <= cost_b) {
-    h.mode = FFT_STOCKHAM;
+    mode = FFT_STOCKHAM;
     fcost = cost_s;
-    if (!upload_stages(rad_s, D, allocs, &h.fft)) return false;
   } else if (cost_r <= cost_b) {
-    h.mode = FFT_RADER;
+    mode = FFT_RADER;
     fcost = cost_r;
-    if (!upload_stages(rad_r, D - 1, allocs, &h.fft)) return false;
+  } else if (M > 0) {
+    mode = FFT_BLUESTEIN;
+    fcost = cost_b;
+  } else {
+    return false;
+  }
+  // host tables shared by both arithmetics
+  std::vector<int> gp, gs;
+  std::vector<double2> bc, chirp;
+  std::vector<cld> H;
+  if (mode == FFT_RADER) {
     const int p = D, g = primitive_root(p);
     if (g == 0) return false;
-    std::vector<int> gp(p - 1), gs(p - 1);
+    gp.resize(p - 1);
+    gs.resize(p - 1);
     const long long ginv = powmod(g, p - 2, p);
     for (int m = 0; m < p - 1; ++m) {
       gp[m] = (int)powmod(g, m, p);
@@ -966,23 +1275,16 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
     std::vector<cld> bq(p - 1);
     for (int q = 0; q < p - 1; ++q) bq[q] = unit_root(gs[q], p);
     const std::vector<cld> B = fft_ld(bq);
-    std::vector<double2> bc(p - 1);
+    bc.resize(p - 1);
     for (int k = 0; k < p - 1; ++k) {
       const cld v = std::conj(B[k]) / (long double)(p - 1);
       bc[k] = make_double2((double)v.real(), (double)v.imag());
     }
-    h.gperm = upload_vec(gp, allocs);
-    h.gscat = upload_vec(gs, allocs);
-    h.bconj = upload_vec(bc, allocs);
-    if (!h.gperm || !h.gscat || !h.bconj) return false;
-  } else if (M > 0) {
-    h.mode = FFT_BLUESTEIN;
-    fcost = cost_b;
-    if (!upload_inplace(rad_b, M, allocs, &h.ip)) return false;
+  } else if (mode == FFT_BLUESTEIN) {
     // chirp exp(-i pi j^2 / D) (exact phase index j^2 mod 2D), the kernel
     // h_n = conj chirp_|n| on |n| < D of the cyclic length M, and its
-    // conjugated spectrum over M in the DIF output order
-    std::vector<double2> chirp(D);
+    // spectrum (stored conjugated over M in each plan's DIF output order)
+    chirp.resize(D);
     std::vector<cld> hk(M, cld(0, 0));
     for (int j = 0; j < D; ++j) {
       const cld w = unit_root((long long)j * j % (2LL * D), 2LL * D);
@@ -990,18 +1292,7 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
       hk[j] = std::conj(w);
       if (j > 0) hk[M - j] = std::conj(w);
     }
-    const std::vector<cld> H = fft_ld(hk);
-    const std::vector<int> pos = dif_positions(M, rad_b);
-    std::vector<double2> hrev(M);
-    for (int k = 0; k < M; ++k) {
-      const cld v = std::conj(H[k]) / (long double)M;
-      hrev[pos[k]] = make_double2((double)v.real(), (double)v.imag());
-    }
-    h.chirp = upload_vec(chirp, allocs);
-    h.hrev = upload_vec(hrev, allocs);
-    if (!h.chirp || !h.hrev) return false;
-  } else {
-    return false;
+    H = fft_ld(hk);
   }
   // (cos, 2 sin)(pi j / D), j = 0..D
   std::vector<double2> trig(D + 1);
@@ -1009,17 +1300,54 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
     const cld w = unit_root(j, 2LL * D);  // exp(-i pi j / D)
     trig[j] = make_double2((double)w.real(), (double)(-2.0L * w.imag()));
   }
-  h.trig = upload_vec(trig, allocs);
-  if (!h.trig) return false;
-  std::vector<FftDesc> one(1, h);
-  const FftDesc* dev = upload_vec(one, allocs);
+  const int* gp_dev = mode == FFT_RADER ? upload_vec(gp, allocs) : nullptr;
+  const int* gs_dev = mode == FFT_RADER ? upload_vec(gs, allocs) : nullptr;
+  if (mode == FFT_RADER && (!gp_dev || !gs_dev)) return false;
+  // the device tables of one arithmetic (the stages are the same; measured:
+  // radix-4 stages in double-float, a third of the butterfly's code, made
+  // the steep tank's step 10 % slower)
+  auto tables = [&](bool df, FftDesc& d) -> bool {
+    std::vector<int> r;
+    d.D = D;
+    d.mode = mode;
+    if (mode == FFT_STOCKHAM) {
+      if (!factor_stages(D, r) || !upload_stages(r, D, df, allocs, &d.fft)) return false;
+    } else if (mode == FFT_RADER) {
+      if (!factor_stages(D - 1, r) || !upload_stages(r, D - 1, df, allocs, &d.fft)) return false;
+      d.gperm = gp_dev;
+      d.gscat = gs_dev;
+      d.bconj = upload_tab(bc, df, allocs);
+      if (!d.bconj) return false;
+    } else {
+      if (!factor_smooth(M, r) || !upload_inplace(r, M, df, allocs, &d.ip)) return false;
+      const std::vector<int> pos = dif_positions(M, r);
+      std::vector<double2> hrev(M);
+      for (int k = 0; k < M; ++k) {
+        const cld v = std::conj(H[k]) / (long double)M;
+        hrev[pos[k]] = make_double2((double)v.real(), (double)v.imag());
+      }
+      d.chirp = upload_tab(chirp, df, allocs);
+      d.hrev = upload_tab(hrev, df, allocs);
+      if (!d.chirp || !d.hrev) return false;
+    }
+    d.trig = upload_tab(trig, df, allocs);
+    return d.trig != nullptr;
+  };
+  if (!tables(false, h) || !tables(true, hd)) return false;
+  std::vector<FftDesc> two{h, hd};
+  const FftDesc* dev = upload_vec(two, allocs);
   if (!dev) return false;
   out->D = D;
   out->mode = h.mode;
   out->M = (h.mode == FFT_BLUESTEIN) ? M : 0;
   out->dev = dev;
+  out->dev_df = dev + 1;
   // two lines share one complex FFT; pre/post processing about 7 per point
   out->cost_line = 0.5 * fcost + 7.0 * (D + 1);
+  // in double-float each line takes a whole complex DFT, at kDfCost of its
+  // FP64 time; the pre- and post-processing (FP32 and integer work, one FP64
+  // add per output) about 3 per point
+  out->cost_line_df = kDfCost * fcost + 3.0 * (D + 1);
   return true;
 }
 
@@ -1033,7 +1361,8 @@ const FftPlanInfo* fft_choice(const AxisJob& J, const Tables& tb, double cost_ot
   for (int i = 0; i < tb.nfft; ++i) {
     const FftPlanInfo& f = tb.fft[i];
     if (f.D != J.D || !f.dev) continue;
-    if (mode == 1 || f.cost_line < 0.9 * cost_other) return &f;
+    const double c = fft_df_enabled() ? f.cost_line_df : f.cost_line;
+    if (mode == 1 || c < 0.9 * cost_other) return &f;
   }
   return nullptr;
 }
@@ -1045,9 +1374,6 @@ size_t fft_smem(const FftPlanInfo& f, int P) {
   return (size_t)2 * padded((long long)P * (f.D + 1)) * sizeof(double2);
 }
 
-// line pairs per CTA: enough butterflies per stage for the 8 warps, enough
-// CTAs for the SMs, shared memory within budget; lines-contiguous (y)
-// passes take at least two pairs so that a warp's loads fill 32-byte sectors
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                    const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -1071,9 +1397,9 @@ EncodeTiledFn fft_encode_fn() {
 // plain loads: a 16-byte aligned base, a 16-byte multiple stride, an inner
 // box extent of NL x 8 bytes (NL even, and every CTA's first line even),
 // box smem offsets on 128-byte boundaries inside the second FFT buffer.
-void setup_tma(FftJob& f, CUtensorMap* map, const FftPlanInfo& plan, int N) {
+void setup_tma(FftJob& f, CUtensorMap* map, const FftPlanInfo& plan, int N, bool df) {
   f.tma = 0;
-  const int P = f.pairs, NL = 2 * P;
+  const int P = f.pairs, NL = df ? P : 2 * P;
   if (f.in_sl != 1 || f.in_sk <= 1 || f.win || plan.mode == FFT_BLUESTEIN || NL % 2) return;
   if (reinterpret_cast<uintptr_t>(f.in) % 16 != 0 || (f.in_sk * 8) % 16 != 0 || f.in_sk * 8 >= (1LL << 40)) return;
   if (f.nlines < 1 || N < 2) return;
@@ -1098,12 +1424,16 @@ void setup_tma(FftJob& f, CUtensorMap* map, const FftPlanInfo& plan, int N) {
   f.tma_box_bytes = (int)box_bytes;
 }
 
-int pick_pairs(const AxisJob& J, const FftPlanInfo& f, int nsm) {
+// complex sequences per CTA: enough butterflies per stage for the warps,
+// enough CTAs for the SMs, shared memory within budget; lines-contiguous (y)
+// passes take at least four lines so that a warp's loads fill 32-byte sectors
+int pick_pairs(const AxisJob& J, const FftPlanInfo& f, int nsm, bool df) {
   const bool ymode = (J.in_sk != 1);
+  const int lps = df ? 1 : 2;  // lines per complex sequence
   int P = ymode ? 8 : 4;
-  const int Pmin = ymode ? 2 : 1;
+  const int Pmin = ymode ? 4 / lps : 1;
   while (P > Pmin) {
-    const long long ctas = (J.nlines + 2LL * P - 1) / (2LL * P);
+    const long long ctas = (J.nlines + (long long)lps * P - 1) / ((long long)lps * P);
     if (fft_smem(f, P) > kFftSmemMax) {
       P /= 2;
       continue;
@@ -1153,12 +1483,14 @@ void launch_fft_jobs(const AxisBatch& in, const FftPlanInfo* const* plan, const 
     f.fl = 0.25 * J.wm * J.sl * J.gscale;
     f.sin_kind = (J.off != 0) ? 1 : 0;
     f.epi = J.epi;
-    f.desc = plan[i]->dev;
-    f.pairs = pick_pairs(J, *plan[i], tb.nsm);
+    const bool df = fft_df_enabled();
+    f.desc = df ? plan[i]->dev_df : plan[i]->dev;
+    f.pairs = pick_pairs(J, *plan[i], tb.nsm, df);
     smem = std::max(smem, fft_smem(*plan[i], f.pairs));
-    if (fft_tma_enabled()) setup_tma(f, &b.tmap[i], *plan[i], J.N);
+    if (fft_tma_enabled()) setup_tma(f, &b.tmap[i], *plan[i], J.N, df);
+    const int nl = df ? f.pairs : 2 * f.pairs;  // lines per CTA
     b.start[i] = total;
-    total += (J.nlines + 2 * f.pairs - 1) / (2 * f.pairs);
+    total += (J.nlines + nl - 1) / nl;
     g_xform_fmas += (double)J.nlines * plan[i]->cost_line;
   }
   b.start[b.njobs] = total;
@@ -1167,13 +1499,24 @@ void launch_fft_jobs(const AxisBatch& in, const FftPlanInfo* const* plan, const 
   attr.run([&] {
     for (int nj : {1, 2, 4, 8, kMaxJobs})
       with_fft_capacity(nj, [&](auto c) {
-        cudaFuncSetAttribute(k_fft_pass<decltype(c)::value>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)kFftSmemMax);
+        constexpr int NJ = decltype(c)::value;
+        for (const void* k : {(const void*)k_fft_pass<NJ, kFT, false>, (const void*)k_fft_pass<NJ, kFTBig, false>,
+                              (const void*)k_fft_pass<NJ, kFT, true>, (const void*)k_fft_pass<NJ, kFTBig, true>})
+          cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFftSmemMax);
       });
   });
+  // Bluestein's convolution buffer leaves room for one CTA per SM: give it
+  // 16 warps to hide the arithmetic latency
+  bool big = false;
+  for (int i = 0; i < in.njobs; ++i) big = big || (plan[i]->mode == FFT_BLUESTEIN && fft_big_ctas());
+  const bool df = fft_df_enabled();
   with_fft_capacity(b.njobs, [&](auto c) {
     constexpr int NJ = decltype(c)::value;
-    launch_pdl(k_fft_pass<NJ>, dim3(total), dim3(kFT), smem, st, shrink_fft<NJ>(b));
+    const FftBatchT<NJ> bb = shrink_fft<NJ>(b);
+    if (big && df) launch_pdl(k_fft_pass<NJ, kFTBig, true>, dim3(total), dim3(kFTBig), smem, st, bb);
+    else if (big) launch_pdl(k_fft_pass<NJ, kFTBig, false>, dim3(total), dim3(kFTBig), smem, st, bb);
+    else if (df) launch_pdl(k_fft_pass<NJ, kFT, true>, dim3(total), dim3(kFT), smem, st, bb);
+    else launch_pdl(k_fft_pass<NJ, kFT, false>, dim3(total), dim3(kFT), smem, st, bb);
   });
 }
 

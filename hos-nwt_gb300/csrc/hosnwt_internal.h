@@ -279,8 +279,10 @@ struct FftPlanInfo {
   int D = 0;
   int mode = 0;
   int M = 0;                 // bluestein convolution length
-  const FftDesc* dev = nullptr;
+  const FftDesc* dev = nullptr;     // FP64 tables
+  const FftDesc* dev_df = nullptr;  // double-float tables of the same plan
   double cost_line = 0.0;    // FP64 instructions per line (two lines share one complex FFT)
+  double cost_line_df = 0.0; // the same in FP64-instruction time with a double-float DFT
 };
 
 // Build the device tables of length D; device allocations are appended to
