@@ -3,19 +3,23 @@ tank, by default the steep 3-D directional tank (1025 x 513 modes, n3 = 33,
 M = 7, p1 = p2 = 7, dealiased grid 4100 x 2052; 50 m x 30 m x 5 m, snake
 flap, JONSWAP Hs = 0.15 m, Tp = 1.3 s, gamma = 5, cos^2s spreading s = 15;
 synthetic seeded phases and directions), the largest benchmark
-configuration, run on the plain FP64 path.
+configuration, run on the plain path (FP64 state, right-hand side and RK
+stages; the FFT passes' complex DFT in double-float, HOSNWT_FFT_DF=0 for
+FP64).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cuda|reference]
                   [--workload steep_3d|directional_3d|irregular_2d|regular_2d|...]
 
-One step = one adaptive RK4(5) step of runge4_adapt2 (five nonlinear
-right-hand sides, error estimate) at the CFL-limited step size, followed by
-the accept of HOS-NWT.f90's step control.  `value` is measured with CUDA
-events on the library's stream with the state resident on the device, the L2
-cache flushed between steps (a 256 MiB write outside the timed events);
-`e2e` is the same step through hosnwt_runge4_adapt2 on pinned host arrays
+One step = one attempted RK4(5) step of runge4_adapt2 (five nonlinear
+right-hand sides, error estimate) under the step control of HOS-NWT.f90's
+time loop: each timed call of hosnwt_advance takes the tank one accepted
+step further, its attempts (rejections included) and the step-size update
+running on the device.  `value` = attempts per second, measured with CUDA
+events on the library's stream with the state resident on the device, the
+L2 cache flushed between calls (a 256 MiB write outside the timed events);
+`e2e` is the same metric through hosnwt_runge4_adapt2 on pinned host arrays
 (host-to-device copy of the 10 state arrays and device-to-host copy of the
-results inside each timed call).  Under torchrun every rank runs its own
+results inside each timed call) with the same step control on the host.  Under torchrun every rank runs its own
 replica tank (the path does not shard); value = total steps/s.
 
 --impl reference times the CPU restatement of the reference (the oracle:
@@ -473,6 +477,7 @@ def run_cuda(args, w):
     io_bytes = 8 * sum(s[0] * s[1] for s in shapes)
 
     ms = ms_tl
+    df = os.environ.get("HOSNWT_FFT_DF", "1")[:1] != "0"
     alg_bytes = 16.0 * nd1 * nd2 * batch  # 8-byte read + 8-byte write per output element
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     peak, peak_src = _measured_peaks()
@@ -500,8 +505,14 @@ def run_cuda(args, w):
                              "ms_per_launch": ms,
                              "timing": "the transform's launches, 20 replays in one CUDA graph, CUDA events on "
                                        "the library's stream",
-                             "note": "FP64-pipe bound, not HBM bound: GB300 runs FP64 at about 1.2 TFLOP/s; "
-                                     "fp64_step gives the step's transform FMAs against the FP64 peak"},
+                             "note": ("not HBM bound: the passes' DFT runs in double-float on the FP32 pipe "
+                                      "(bound by instruction issue); fp64_step gives the step's transform work "
+                                      "in FP64 instructions against the FP64 peak" if df else
+                                      "FP64-pipe bound, not HBM bound: GB300 runs FP64 at about 1.2 TFLOP/s; "
+                                      "fp64_step gives the step's transform FMAs against the FP64 peak")},
+                "arithmetic": ("FP64 state, right-hand side and RK stages; the FFT passes' complex DFT in "
+                               "double-float (pairs of FP32, 48-bit significand)" if df else
+                               "FP64 throughout (HOSNWT_FFT_DF=0)"),
                 }
         if world == 1:
             line["cpu_baseline"] = cpu_baseline(w)
