@@ -477,7 +477,9 @@ def run_cuda(args, w):
     io_bytes = 8 * sum(s[0] * s[1] for s in shapes)
 
     ms = ms_tl
-    df = os.environ.get("HOSNWT_FFT_DF", "1")[:1] != "0"
+    # the FFT passes (and with them the double-float DFT) run in 3-D tanks;
+    # 2-D tanks take the FP64 sum passes
+    df = os.environ.get("HOSNWT_FFT_DF", "1")[:1] != "0" and n2 > 1
     alg_bytes = 16.0 * nd1 * nd2 * batch  # 8-byte read + 8-byte write per output element
     achieved = alg_bytes / (ms * 1e-3) / 1e9
     peak, peak_src = _measured_peaks()
@@ -512,7 +514,8 @@ def run_cuda(args, w):
                                       "fp64_step gives the step's transform FMAs against the FP64 peak")},
                 "arithmetic": ("FP64 state, right-hand side and RK stages; the FFT passes' complex DFT in "
                                "double-float (pairs of FP32, 48-bit significand)" if df else
-                               "FP64 throughout (HOSNWT_FFT_DF=0)"),
+                               "FP64 throughout" + (" (HOSNWT_FFT_DF=0)" if n2 > 1 else
+                                                    " (a 2-D tank: FP64 sum passes)")),
                 }
         if world == 1:
             line["cpu_baseline"] = cpu_baseline(w)

@@ -48,7 +48,11 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
 #include <type_traits>
 #include <vector>
 
@@ -1450,12 +1454,34 @@ int pick_pairs(const AxisJob& J, const FftPlanInfo& f, int nsm, bool df) {
 
 }  // namespace
 
-void launch_fft_jobs(const AxisBatch& in, const FftPlanInfo* const* plan, const Tables& tb, cudaStream_t st) {
+namespace {
+
+// One prepared launch of the FFT pass kernel.
+struct FftLaunch {
   FftBatchT<kMaxJobs> b{};
-  b.njobs = in.njobs;
-  b.acc = in.acc;
   size_t smem = 0;
   int total = 0;
+  bool big = false;
+  bool df = false;
+};
+
+// Layout of a batch: threads per CTA (0: the default, 512 for Bluestein
+// jobs and 256 otherwise) and the complex sequences per CTA of every job,
+// scaled by 2^pshift from pick_pairs.
+struct FftLayout {
+  int nt = 0;
+  int pshift = 0;
+};
+
+bool prepare_fft(const AxisBatch& in, const FftPlanInfo* const* plan, const Tables& tb, FftLayout lay, FftLaunch& L) {
+  FftBatchT<kMaxJobs>& b = L.b;
+  b = FftBatchT<kMaxJobs>{};
+  b.njobs = in.njobs;
+  b.acc = in.acc;
+  L.smem = 0;
+  L.total = 0;
+  L.df = fft_df_enabled();
+  const bool df = L.df;
   for (int i = 0; i < in.njobs; ++i) {
     const AxisJob& J = in.job[i];
     FftJob& f = b.job[i];
@@ -1483,18 +1509,32 @@ void launch_fft_jobs(const AxisBatch& in, const FftPlanInfo* const* plan, const 
     f.fl = 0.25 * J.wm * J.sl * J.gscale;
     f.sin_kind = (J.off != 0) ? 1 : 0;
     f.epi = J.epi;
-    const bool df = fft_df_enabled();
     f.desc = df ? plan[i]->dev_df : plan[i]->dev;
-    f.pairs = pick_pairs(J, *plan[i], tb.nsm, df);
-    smem = std::max(smem, fft_smem(*plan[i], f.pairs));
+    int P = pick_pairs(J, *plan[i], tb.nsm, df);
+    P = lay.pshift >= 0 ? P << lay.pshift : P >> -lay.pshift;
+    const int pmax = df ? kFMaxLines : kFMaxLines / 2;
+    if (P < 1 || P > pmax || fft_smem(*plan[i], P) > kFftSmemMax) return false;
+    f.pairs = P;
+    L.smem = std::max(L.smem, fft_smem(*plan[i], f.pairs));
     if (fft_tma_enabled()) setup_tma(f, &b.tmap[i], *plan[i], J.N, df);
     const int nl = df ? f.pairs : 2 * f.pairs;  // lines per CTA
-    b.start[i] = total;
-    total += (J.nlines + nl - 1) / nl;
-    g_xform_fmas += (double)J.nlines * plan[i]->cost_line;
+    b.start[i] = L.total;
+    L.total += (J.nlines + nl - 1) / nl;
   }
-  b.start[b.njobs] = total;
-  if (total <= 0) return;
+  b.start[b.njobs] = L.total;
+  if (lay.nt == 0) {
+    // Bluestein's convolution buffer leaves room for one CTA per SM: give
+    // it 16 warps to hide the arithmetic latency
+    L.big = false;
+    for (int i = 0; i < in.njobs; ++i) L.big = L.big || (plan[i]->mode == FFT_BLUESTEIN && fft_big_ctas());
+  } else {
+    L.big = (lay.nt == kFTBig);
+  }
+  return true;
+}
+
+void launch_prepared(const FftLaunch& L, cudaStream_t st) {
+  if (L.total <= 0) return;
   static PerDeviceOnce attr;
   attr.run([&] {
     for (int nj : {1, 2, 4, 8, kMaxJobs})
@@ -1505,19 +1545,148 @@ void launch_fft_jobs(const AxisBatch& in, const FftPlanInfo* const* plan, const 
           cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFftSmemMax);
       });
   });
-  // Bluestein's convolution buffer leaves room for one CTA per SM: give it
-  // 16 warps to hide the arithmetic latency
-  bool big = false;
-  for (int i = 0; i < in.njobs; ++i) big = big || (plan[i]->mode == FFT_BLUESTEIN && fft_big_ctas());
-  const bool df = fft_df_enabled();
-  with_fft_capacity(b.njobs, [&](auto c) {
+  with_fft_capacity(L.b.njobs, [&](auto c) {
     constexpr int NJ = decltype(c)::value;
-    const FftBatchT<NJ> bb = shrink_fft<NJ>(b);
-    if (big && df) launch_pdl(k_fft_pass<NJ, kFTBig, true>, dim3(total), dim3(kFTBig), smem, st, bb);
-    else if (big) launch_pdl(k_fft_pass<NJ, kFTBig, false>, dim3(total), dim3(kFTBig), smem, st, bb);
-    else if (df) launch_pdl(k_fft_pass<NJ, kFT, true>, dim3(total), dim3(kFT), smem, st, bb);
-    else launch_pdl(k_fft_pass<NJ, kFT, false>, dim3(total), dim3(kFT), smem, st, bb);
+    const FftBatchT<NJ> bb = shrink_fft<NJ>(L.b);
+    if (L.big && L.df) launch_pdl(k_fft_pass<NJ, kFTBig, true>, dim3(L.total), dim3(kFTBig), L.smem, st, bb);
+    else if (L.big) launch_pdl(k_fft_pass<NJ, kFTBig, false>, dim3(L.total), dim3(kFTBig), L.smem, st, bb);
+    else if (L.df) launch_pdl(k_fft_pass<NJ, kFT, true>, dim3(L.total), dim3(kFT), L.smem, st, bb);
+    else launch_pdl(k_fft_pass<NJ, kFT, false>, dim3(L.total), dim3(kFT), L.smem, st, bb);
   });
+}
+
+// ---- the layout tuner
+//
+// A batch's signature holds what sets the cost of its launch (per job: the
+// plan, the lines and their counts, the axis, whether TMA can stage it).
+// While a step graph is captured, launch_fft_jobs records the batches whose
+// signature has no decision; fft_tune_run then times every layout of each
+// on scratch outputs (threads per CTA 256 or 512, sequences per CTA scaled
+// by 1/4 to 2) and keeps the fastest, and the caller captures again.  Only
+// the double-float passes are tuned: their arithmetic per line does not
+// depend on the layout, so a tuned step computes the same bits.
+
+struct FftTuneRecord {
+  std::string sig;
+  AxisBatch in;
+  const FftPlanInfo* plan[kMaxJobs];
+  const Tables* tb;
+};
+
+std::mutex g_tune_mu;
+std::map<std::string, FftLayout> g_tune_done;  // guarded by g_tune_mu
+std::vector<FftTuneRecord> g_tune_pending;     // guarded by g_tune_mu
+thread_local bool g_tune_recording = false;
+
+std::string fft_signature(const AxisBatch& in, const FftPlanInfo* const* plan) {
+  std::string s;
+  char buf[160];
+  for (int i = 0; i < in.njobs; ++i) {
+    const AxisJob& J = in.job[i];
+    std::snprintf(buf, sizeof buf, "%d:%d:%d:%d:%d:%d:%lld:%lld:%d:%d:%d;", plan[i]->D, plan[i]->mode, J.nlines,
+                  J.nin, J.nout, J.N, J.in_sk, J.in_sl, J.win != nullptr ? 1 : 0, J.epi,
+                  (int)(reinterpret_cast<uintptr_t>(J.in) % 16));
+    s += buf;
+  }
+  return s;
+}
+
+}  // namespace
+
+bool fft_tune_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("HOSNWT_FFT_TUNE");
+    return !(e && e[0] == '0');
+  }();
+  return on && fft_df_enabled();
+}
+
+void fft_tune_record(bool on) { g_tune_recording = on; }
+
+int fft_tune_run(cudaStream_t st) {
+  std::vector<FftTuneRecord> todo;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    todo.swap(g_tune_pending);
+  }
+  if (todo.empty()) return 0;
+  // one scratch buffer takes the outputs of every candidate launch
+  long long ext = 1;
+  for (const FftTuneRecord& r : todo)
+    for (int i = 0; i < r.in.njobs; ++i) {
+      const AxisJob& J = r.in.job[i];
+      ext = std::max(ext, (J.nlines - 1) * J.out_sl + (J.nout - 1) * J.out_sk + 1);
+    }
+  double* scratch = nullptr;
+  if (cudaMalloc(&scratch, sizeof(double) * ext) != cudaSuccess) return -1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int tuned = 0;
+  bool ok = true;
+  for (const FftTuneRecord& r : todo) {
+    AxisBatch t = r.in;
+    for (int i = 0; i < t.njobs; ++i) {
+      t.job[i].out = scratch;
+      t.job[i].epi = 0;
+    }
+    FftLayout best;
+    float best_ms = 3.4e38f;
+    for (int nt : {kFT, kFTBig})
+      for (int ps : {-2, -1, 0, 1}) {
+        FftLaunch L;
+        if (!prepare_fft(t, r.plan, *r.tb, FftLayout{nt, ps}, L) || L.total <= 0) continue;
+        launch_prepared(L, st);  // warm-up
+        cudaEventRecord(e0, st);
+        for (int rep = 0; rep < 3; ++rep) launch_prepared(L, st);
+        cudaEventRecord(e1, st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+          ok = false;
+          break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = FftLayout{nt, ps};
+        }
+      }
+    if (!ok) break;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_done[r.sig] = best;
+    ++tuned;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(scratch);
+  return ok && cudaGetLastError() == cudaSuccess ? tuned : -1;
+}
+
+void launch_fft_jobs(const AxisBatch& in, const FftPlanInfo* const* plan, const Tables& tb, cudaStream_t st) {
+  FftLayout lay;
+  if (fft_tune_enabled()) {
+    const std::string sig = fft_signature(in, plan);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_done.find(sig);
+    if (it != g_tune_done.end()) {
+      lay = it->second;
+    } else if (g_tune_recording) {
+      bool seen = false;
+      for (const FftTuneRecord& r : g_tune_pending) seen = seen || r.sig == sig;
+      if (!seen) {
+        FftTuneRecord r;
+        r.sig = sig;
+        r.in = in;
+        for (int i = 0; i < in.njobs; ++i) r.plan[i] = plan[i];
+        r.tb = &tb;
+        g_tune_pending.push_back(r);
+      }
+    }
+  }
+  FftLaunch L;
+  if (!prepare_fft(in, plan, tb, lay, L) && !prepare_fft(in, plan, tb, FftLayout{}, L)) return;
+  for (int i = 0; i < in.njobs; ++i) g_xform_fmas += (double)in.job[i].nlines * plan[i]->cost_line;
+  launch_prepared(L, st);
 }
 
 }  // namespace hos

@@ -329,6 +329,13 @@ struct Tables {
 const FftPlanInfo* fft_choice(const AxisJob& J, const Tables& tb, double cost_other);
 // Launch the FFT passes of b's jobs, job i with plan[i].
 void launch_fft_jobs(const AxisBatch& b, const FftPlanInfo* const* plan, const Tables& tb, cudaStream_t st);
+// Layout tuning of the FFT passes: with recording on (this thread), launches
+// whose batch has no tuned layout are recorded; fft_tune_run times the
+// layouts of the recorded batches on `st` (outside any capture) and keeps
+// the fastest.  Returns the number of batches tuned, -1 on a CUDA error.
+bool fft_tune_enabled();
+void fft_tune_record(bool on);
+int fft_tune_run(cudaStream_t st);
 
 // FP64 FMAs of the transform passes launched from this host thread since
 // the counter was last reset (the algorithm's own count: terms times

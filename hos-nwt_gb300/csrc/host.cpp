@@ -995,15 +995,32 @@ static int cuda_check(Ctx& c, const char* what) {
   return HOSNWT_OK;
 }
 
+// Capture the step graph.  The first capture records the FFT batches that
+// have no tuned layout yet; they are tuned on the stream (fft_tune_run) and
+// the step is captured again with the tuned layouts.
 static int build_step_graph(Ctx& c) {
   cudaGraph_t g = nullptr;
-  if (cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-    return cuda_check(c, "begin capture");
-  cudaMemcpyAsync(c.d.sc + SC_T0, c.d.host_sc + SC_T0, 2 * sizeof(double), cudaMemcpyHostToDevice, c.st);
-  const double f0 = g_xform_fmas;
-  enqueue_step(c, c.st);
-  c.fmas_per_step = g_xform_fmas - f0;
-  if (cudaStreamEndCapture(c.st, &g) != cudaSuccess) return cuda_check(c, "end capture");
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    const bool record = attempt == 0 && fft_tune_enabled();
+    if (cudaStreamBeginCapture(c.st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return cuda_check(c, "begin capture");
+    cudaMemcpyAsync(c.d.sc + SC_T0, c.d.host_sc + SC_T0, 2 * sizeof(double), cudaMemcpyHostToDevice, c.st);
+    const double f0 = g_xform_fmas;
+    fft_tune_record(record);
+    enqueue_step(c, c.st);
+    fft_tune_record(false);
+    c.fmas_per_step = g_xform_fmas - f0;
+    if (cudaStreamEndCapture(c.st, &g) != cudaSuccess) return cuda_check(c, "end capture");
+    if (!record) break;
+    const int tuned = fft_tune_run(c.st);
+    if (tuned < 0) {
+      cudaGraphDestroy(g);
+      return cuda_check(c, "FFT layout tuning");
+    }
+    if (tuned == 0) break;
+    cudaGraphDestroy(g);
+    g = nullptr;
+  }
   size_t nn = 0;
   cudaGraphGetNodes(g, nullptr, &nn);
   std::vector<cudaGraphNode_t> nodes(nn);
@@ -1901,7 +1918,18 @@ extern "C" int hosnwt_time_transform(hosnwt_ctx* h, int grid, int dir, int csx, 
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  for (int w = 0; w < 3; ++w) launch_transforms(rq.data(), batch, c.tb, c.d.xtmp, c.st);
+  // the first warm-up records the FFT batches for the layout tuner, as the
+  // step graph's first capture does
+  fft_tune_record(fft_tune_enabled());
+  launch_transforms(rq.data(), batch, c.tb, c.d.xtmp, c.st);
+  fft_tune_record(false);
+  if (fft_tune_run(c.st) < 0) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (double* q : bufs) cudaFree(q);
+    return fail(c, HOSNWT_ERR_CUDA, "time_transform: FFT layout tuning failed");
+  }
+  for (int w = 0; w < 2; ++w) launch_transforms(rq.data(), batch, c.tb, c.d.xtmp, c.st);
   cudaGraph_t g = nullptr;
   cudaGraphExec_t ge = nullptr;
   float ms = 0.f;
