@@ -420,6 +420,25 @@ __device__ __forceinline__ void dft(T* v) {
   else dft8(v);
 }
 
+// Division by a divisor fixed for a whole stage, by multiply-high (the
+// round-up method of Granlund and Montgomery, 1994): with s = ceil(log2 d)
+// and m = floor(2^32 (2^s - d) / d) + 1, x / d = (mulhi(x, m) + x) >> s for
+// every 32-bit x.  The stage loops divide their work index on every
+// iteration; a plain division by a run-time divisor takes about twenty
+// instructions.
+struct FastDiv {
+  unsigned d, m, s;
+};
+__device__ __forceinline__ FastDiv fastdiv(int d) {
+  const unsigned ud = (unsigned)d;
+  const unsigned s = 32u - (unsigned)__clz(ud - 1u);
+  const unsigned long long m = ((1ULL << 32) * ((1ULL << s) - ud)) / ud + 1ULL;
+  return FastDiv{ud, (unsigned)m, s};
+}
+__device__ __forceinline__ int operator/(int x, FastDiv f) {
+  return (int)(((unsigned long long)__umulhi((unsigned)x, f.m) + (unsigned)x) >> f.s);
+}
+
 // One Stockham stage of radix R (R in {2, 3, 4, 5, 7, 8}) on P sequences of
 // length L, src -> dst; Ns is the product of the radices of earlier stages.
 // Butterfly j takes src[j + t L/R], twiddled by exp(-2 pi i t k / (Ns R))
@@ -429,10 +448,11 @@ __device__ void st_small(const T* __restrict__ src, T* __restrict__ dst, int L, 
                          const T* __restrict__ stw) {
   const int nb = L / R;
   const int W = P * nb;
+  const FastDiv fnb = fastdiv(nb), fns = fastdiv(Ns);
   for (int w = threadIdx.x; w < W; w += blockDim.x) {
-    const int p = w / nb, j = w - p * nb;
+    const int p = w / fnb, j = w - p * nb;
     const int off = p * L;
-    const int k = j % Ns;
+    const int k = j - (j / fns) * Ns;
     T v[R];
 #pragma unroll
     for (int t = 0; t < R; ++t) v[t] = src[pz(off + j + t * nb)];
@@ -459,14 +479,15 @@ __device__ void st_generic(T* __restrict__ src, T* __restrict__ dst, int L, int 
   const int nb = L / R, h = (R + 1) / 2;
   const int rs = L / R;
   const int W1 = P * nb * (h - 1);
+  const FastDiv fnb = fastdiv(nb), fh1 = fastdiv(h - 1), fh = fastdiv(h), fns = fastdiv(Ns);
   for (int w = threadIdx.x; w < W1; w += blockDim.x) {
-    const int j = w % nb;
-    const int r = w / nb;
-    const int t = 1 + r % (h - 1);
-    const int p = r / (h - 1);
+    const int r = w / fnb;
+    const int j = w - r * nb;
+    const int p = r / fh1;
+    const int t = 1 + r - p * (h - 1);
     const int off = p * L;
     T va = src[pz(off + j + t * nb)], vb = src[pz(off + j + (R - t) * nb)];
-    const int k = j % Ns;
+    const int k = j - (j / fns) * Ns;
     if (k != 0) {
       va = cmul(va, ldt(stw + (t - 1) * Ns + k));
       vb = cmul(vb, ldt(stw + (R - t - 1) * Ns + k));
@@ -477,12 +498,12 @@ __device__ void st_generic(T* __restrict__ src, T* __restrict__ dst, int L, int 
   __syncthreads();
   const int W2 = P * nb * h;
   for (int w = threadIdx.x; w < W2; w += blockDim.x) {
-    const int j = w % nb;
-    const int r = w / nb;
-    const int o = r % h;
-    const int p = r / h;
+    const int r = w / fnb;
+    const int j = w - r * nb;
+    const int p = r / fh;
+    const int o = r - p * h;
     const int off = p * L;
-    const int k = j % Ns;
+    const int k = j - (j / fns) * Ns;
     const int base = off + (j - k) * R + k;
     const T v0 = src[pz(off + j)];
     if (o == 0) {
@@ -515,9 +536,10 @@ template <int R, bool DIF, typename T>
 __device__ void ip_stage(T* __restrict__ x, int L, int ld, int S, int P, const T* __restrict__ tw) {
   const int m = S / R;
   const int nb = L / R;
+  const FastDiv fnb = fastdiv(nb), fm = fastdiv(m);
   for (int w = threadIdx.x; w < P * nb; w += blockDim.x) {
-    const int p = w / nb, bj = w - p * nb;
-    const int blk = bj / m, j = bj - blk * m;
+    const int p = w / fnb, bj = w - p * nb;
+    const int blk = bj / fm, j = bj - blk * m;
     const int base = p * ld + blk * S + j;
     T v[R];
 #pragma unroll
@@ -536,9 +558,12 @@ __device__ void ip_stage(T* __restrict__ x, int L, int ld, int S, int P, const T
   }
 }
 
+// Stages i0 .. i1-1 of the in-place FFT, in the order of its form (DIF:
+// stage i, DIT: stage nst-1-i); all of them by default.
 template <bool DIF, typename T>
-__device__ void ip_fft(const FftInplace& F, T* x, int ld, int P) {
-  for (int i = 0; i < F.nst; ++i) {
+__device__ void ip_fft(const FftInplace& F, T* x, int ld, int P, int i0 = 0, int i1 = -1) {
+  const int n = i1 < 0 ? F.nst : i1;
+  for (int i = i0; i < n; ++i) {
     const int s = DIF ? i : F.nst - 1 - i;
     int S = F.L;
     for (int q = 0; q < s; ++q) S /= F.rad[q];
@@ -553,6 +578,42 @@ __device__ void ip_fft(const FftInplace& F, T* x, int ld, int P) {
     }
     __syncthreads();
   }
+}
+
+// The turn of Bluestein's convolution in one pass: the last DIF stage, the
+// product with the conjugated kernel spectrum h (conj(x) h, in the DIF
+// output order) and the first DIT stage.  Both stages have span R and no
+// twiddles, so each butterfly keeps its R elements in registers throughout.
+template <int R, typename T>
+__device__ void ip_turn_r(T* __restrict__ x, int L, int ld, int P, const T* __restrict__ h) {
+  const int nb = L / R;
+  const FastDiv fnb = fastdiv(nb);
+  for (int w = threadIdx.x; w < P * nb; w += blockDim.x) {
+    const int p = w / fnb, blk = w - p * nb;
+    const int base = p * ld + blk * R;
+    T v[R];
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = x[pz(base + t)];
+    dft<R>(v);
+#pragma unroll
+    for (int t = 0; t < R; ++t) v[t] = cmulconj(v[t], ldt(h + blk * R + t));
+    dft<R>(v);
+#pragma unroll
+    for (int t = 0; t < R; ++t) x[pz(base + t)] = v[t];
+  }
+}
+
+template <typename T>
+__device__ void ip_turn(const FftInplace& F, T* x, int ld, int P, const T* h) {
+  switch (F.rad[F.nst - 1]) {
+    case 2: ip_turn_r<2>(x, F.L, ld, P, h); break;
+    case 3: ip_turn_r<3>(x, F.L, ld, P, h); break;
+    case 4: ip_turn_r<4>(x, F.L, ld, P, h); break;
+    case 5: ip_turn_r<5>(x, F.L, ld, P, h); break;
+    case 7: ip_turn_r<7>(x, F.L, ld, P, h); break;
+    default: ip_turn_r<8>(x, F.L, ld, P, h); break;
+  }
+  __syncthreads();
 }
 
 // Complex FFT of P sequences of length F.L held in a (a <-> b ping-pong);
@@ -711,7 +772,16 @@ __global__ void __launch_bounds__(NT, NT == kFT ? HOSNWT_FFT_MIN_BLOCKS : 1)
         const dff a = is_sin ? sj : rj, c = is_sin ? rj : sj;
         v = mkc(dfma(dim(cs), a, dscale(2.f, c)), dscale(2.f, dmul(dre(cs), a)));
       }
+      if (blue) v = cmul(v, ldt(tab<dfc>(F.chirp) + j));  // Bluestein's premultiply
       A[pz(l * zld + j)] = v;
+    }
+    if (blue) {
+      // the convolution's zero padding
+      const int pad = zld - D;
+      for (int w = tid; w < P * pad; w += blockDim.x) {
+        const int p = w / pad;
+        A[pz(p * zld + D + (w - p * pad))] = czero<dfc>();
+      }
     }
   } else {
   for (int w = tid; w < NL * D; w += blockDim.x) {
@@ -746,6 +816,15 @@ __global__ void __launch_bounds__(NT, NT == kFT ? HOSNWT_FFT_MIN_BLOCKS : 1)
   if (F.mode == FFT_STOCKHAM) {
     Z = run_fft(F.fft, A, B, P);
     O = reinterpret_cast<double*>(Z == A ? B : A);
+  } else if (blue && DF) {
+    // as below, with the premultiply done by the load loop, the turn in one
+    // pass (ip_turn) and the postmultiply by the unpack
+    const int M = zld;
+    ip_fft<true>(F.ip, A, M, P, 0, F.ip.nst - 1);
+    ip_turn(F.ip, A, M, P, tab<T>(F.hrev));
+    ip_fft<false>(F.ip, A, M, P, 1, F.ip.nst);
+    Z = A;
+    O = nullptr;  // rows in each sequence's free tail, see orow
   } else if (blue) {
     // X_k = conj-chirp_k sum_j (z_j conj-chirp_j) chirp_{k-j}: a cyclic
     // convolution of length M >= 2 D + 2, in place in A
@@ -808,7 +887,8 @@ __global__ void __launch_bounds__(NT, NT == kFT ? HOSNWT_FFT_MIN_BLOCKS : 1)
     const dff s0 = d2df(J.f0), sm = d2df(J.fm), sl = d2df(J.fl);
     for (int w = tid; w < P * (ne + 1); w += blockDim.x) {
       const int p = w / (ne + 1), m = w - p * (ne + 1);
-      const dfc W = Z[pz(p * zld + m)];
+      dfc W = Z[pz(p * zld + m)];
+      if (blue) W = cmul(ldt(tab<dfc>(F.chirp) + m), cconj(W));  // Bluestein's postmultiply
       double* o = orow(p);
       const int k = 2 * m;
       o[k] = df2d(dmul(k == 0 ? s0 : (k == D ? sl : sm), is_sin ? dneg(dim(W)) : dre(W)));
