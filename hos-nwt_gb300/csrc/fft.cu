@@ -1663,7 +1663,9 @@ struct FftTuneRecord {
 
 std::mutex g_tune_mu;
 std::map<std::string, FftLayout> g_tune_done;  // guarded by g_tune_mu
-std::vector<FftTuneRecord> g_tune_pending;     // guarded by g_tune_mu
+// batches recorded by this thread's capture, tuned on its own stream (the
+// records point into that context's device memory)
+thread_local std::vector<FftTuneRecord> g_tune_pending;
 thread_local bool g_tune_recording = false;
 
 std::string fft_signature(const AxisBatch& in, const FftPlanInfo* const* plan) {
@@ -1693,10 +1695,7 @@ void fft_tune_record(bool on) { g_tune_recording = on; }
 
 int fft_tune_run(cudaStream_t st) {
   std::vector<FftTuneRecord> todo;
-  {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    todo.swap(g_tune_pending);
-  }
+  todo.swap(g_tune_pending);
   if (todo.empty()) return 0;
   // one scratch buffer takes the outputs of every candidate launch
   long long ext = 1;
@@ -1706,7 +1705,10 @@ int fft_tune_run(cudaStream_t st) {
       ext = std::max(ext, (J.nlines - 1) * J.out_sl + (J.nout - 1) * J.out_sk + 1);
     }
   double* scratch = nullptr;
-  if (cudaMalloc(&scratch, sizeof(double) * ext) != cudaSuccess) return -1;
+  if (cudaMalloc(&scratch, sizeof(double) * ext) != cudaSuccess) {
+    cudaGetLastError();  // no room for the scratch outputs: keep the default layouts
+    return 0;
+  }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);

@@ -87,3 +87,47 @@ def test_fft_transforms_match_oracle(lib, mode):
     out = json.loads(r.stdout.strip().splitlines()[-1])
     print(mode, out)
     assert out["worst_fraction_of_tol"] < 1.0
+
+
+NAN_SCRIPT = r"""
+import json, sys
+import numpy as np
+sys.path[:0] = [ROOT, ROOT + "/hos-nwt_gb300"]
+import hosnwt
+from oracle.hos_oracle import Fourier, default_input
+n1, n2, p1, p2 = 513, 257, 4, 4
+inp = default_input(T_stop=5.0, amp_mono=0.02, nu_mono=0.7, theta_mono=10.0, ylen=20.0, toler=1e-7)
+g = hosnwt.Tank(inp, n1, n2, 9, 4, p1, p2)
+nd1, nd2 = ((p1 + 1) * n1) // 2, ((p2 + 1) * n2) // 2
+F = Fourier(n1, n2, nd1, nd2, 16)
+rng = np.random.default_rng(5)
+out = {}
+for bad in (np.nan, np.inf):
+    a = rng.standard_normal((nd1, nd2))
+    a[7, 11] = bad
+    got = g.transform("big", 1, "cos", "cos", a)
+    clean = a.copy()
+    clean[7, 11] = 0.0
+    ref = F.S2F_big(clean, "cos", "cos")
+    # the x pass spreads the bad entry over column 11, the y pass over every
+    # row: the whole output becomes non-finite; a clean transform after it
+    # is exact again (no state is left behind)
+    out[str(bad)] = bool(np.all(~np.isfinite(got)))
+    again = g.transform("big", 1, "cos", "cos", clean)
+    out[str(bad) + "_after"] = float(np.max(np.abs(again - ref)) / np.max(np.abs(ref)))
+g.close()
+print(json.dumps(out))
+"""
+
+
+def test_fft_passes_propagate_nan_and_inf(lib):
+    env = dict(os.environ)
+    env["HOSNWT_FFT"] = "1"
+    env.pop("HOSNWT_FFT_DF", None)
+    r = subprocess.run([sys.executable, "-c", f"ROOT = {ROOT!r}\n" + NAN_SCRIPT], cwd=ROOT, env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, (r.stdout[-2000:], r.stderr[-3000:])
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    for bad in ("nan", "inf"):
+        assert out[bad], (bad, out)
+        assert out[bad + "_after"] < 1e-13 * 23, (bad, out)
