@@ -1560,7 +1560,7 @@ static int diagnostics(Ctx& c, double out[5]) {
 // check_slope (initial_condition.f90:687-716): filter eta and phis when the
 // slope of the last right-hand side exceeds 8
 static int check_slope(Ctx& c, int* filtered) {
-  double dg[5];
+  double dg[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   int rc = diagnostics(c, dg);
   if (rc) return rc;
   int f = 0;

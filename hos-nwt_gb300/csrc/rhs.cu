@@ -130,13 +130,6 @@ __global__ void k_gtof(const double* __restrict__ G1, const double* __restrict__
   }
 }
 
-__global__ void k_pow(const double* __restrict__ prev, const double* __restrict__ e1, double jp1,
-                      double* out, long long n) {
-  pdl_wait();
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < n) out[i] = prev[i] / jp1 * e1[i];
-}
-
 // eta^j / j! for a run of orders without dealiasing in between:
 // e_{j+1} = e_j / (j+1) * e_1 for j = j0 .. j1-1 (resol_HOS.f90:979-987)
 struct PowArgs {
@@ -229,12 +222,6 @@ __global__ void k_mul(const double* __restrict__ x, const double* __restrict__ y
   pdl_wait();
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n) out[i] = (s * x[i]) * y[i];
-}
-
-__global__ void k_add(double* out, const double* __restrict__ x, long long n) {
-  pdl_wait();
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < n) out[i] += x[i];
 }
 
 __global__ void k_sq2(const double* __restrict__ a, const double* __restrict__ b, double* out,
@@ -565,12 +552,6 @@ __global__ void k_sweet_rhs(const double* __restrict__ eta1st, const double* __r
   const double pz = phiz1st_spec[i] + phiz1[i];
   rhs[i] = -eta1st[i] - phit1[i] - iabsnb * nu[i] * pz;
   keta1[i] = pz;
-}
-
-__global__ void k_sum3(const double* a, const double* b, const double* c, double* out, long long n) {
-  pdl_wait();
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < n) out[i] = a[i] + b[i] + c[i];
 }
 
 // ---------------------------------------------------------------------------
