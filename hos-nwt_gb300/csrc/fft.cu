@@ -428,22 +428,10 @@ __device__ __forceinline__ void dft(T* v) {
   else dft8(v);
 }
 
-// Division by a divisor fixed for a whole stage, by multiply-high (the
-// round-up method of Granlund and Montgomery, 1994): with s = ceil(log2 d)
-// and m = floor(2^32 (2^s - d) / d) + 1, x / d = (mulhi(x, m) + x) >> s for
-// every 32-bit x.  The stage loops divide their work index on every
-// iteration; a plain division by a run-time divisor takes about twenty
-// instructions.
-struct FastDiv {
-  unsigned d, m, s;
-};
-__device__ __forceinline__ FastDiv fastdiv(int d) {
-  const unsigned ud = (unsigned)d;
-  const unsigned s = 32u - (unsigned)__clz(ud - 1u);
-  const unsigned long long m = ((1ULL << 32) * ((1ULL << s) - ud)) / ud + 1ULL;
-  return FastDiv{ud, (unsigned)m, s};
-}
-__device__ __forceinline__ int operator/(int x, FastDiv f) {
+// x / d with the stage's constant (make_fastdiv): the stage loops divide
+// their work index on every iteration, and a plain division by a run-time
+// divisor takes about twenty instructions.
+__device__ __forceinline__ int operator/(int x, FastDivC f) {
   return (int)(((unsigned long long)__umulhi((unsigned)x, f.m) + (unsigned)x) >> f.s);
 }
 
@@ -453,10 +441,9 @@ __device__ __forceinline__ int operator/(int x, FastDiv f) {
 // with k = j mod Ns, and writes dst[(j - k) R + k + t Ns].
 template <int R, typename T>
 __device__ void st_small(const T* __restrict__ src, T* __restrict__ dst, int L, int Ns, int P,
-                         const T* __restrict__ stw) {
+                         const T* __restrict__ stw, FastDivC fnb, FastDivC fns) {
   const int nb = L / R;
   const int W = P * nb;
-  const FastDiv fnb = fastdiv(nb), fns = fastdiv(Ns);
   for (int w = threadIdx.x; w < W; w += blockDim.x) {
     const int p = w / fnb, j = w - p * nb;
     const int off = p * L;
@@ -483,11 +470,11 @@ __device__ void st_small(const T* __restrict__ src, T* __restrict__ dst, int L, 
 //   A = v_0 + sum_t s_t cos(2 pi t o / R),  B = sum_t d_t sin(2 pi t o / R).
 template <typename T>
 __device__ void st_generic(T* __restrict__ src, T* __restrict__ dst, int L, int Ns, int R, int P,
-                           const T* __restrict__ tw, const T* __restrict__ stw) {
+                           const T* __restrict__ tw, const T* __restrict__ stw, FastDivC fnb,
+                           FastDivC fh1, FastDivC fh, FastDivC fns) {
   const int nb = L / R, h = (R + 1) / 2;
   const int rs = L / R;
   const int W1 = P * nb * (h - 1);
-  const FastDiv fnb = fastdiv(nb), fh1 = fastdiv(h - 1), fh = fastdiv(h), fns = fastdiv(Ns);
   for (int w = threadIdx.x; w < W1; w += blockDim.x) {
     const int r = w / fnb;
     const int j = w - r * nb;
@@ -541,10 +528,10 @@ __device__ void st_generic(T* __restrict__ src, T* __restrict__ dst, int L, int 
 // the inputs, then DFT.  Each butterfly reads and writes only its own
 // elements, so a stage needs no barrier inside it.
 template <int R, bool DIF, typename T>
-__device__ void ip_stage(T* __restrict__ x, int L, int ld, int S, int P, const T* __restrict__ tw) {
+__device__ void ip_stage(T* __restrict__ x, int L, int ld, int S, int P, const T* __restrict__ tw,
+                         FastDivC fnb, FastDivC fm) {
   const int m = S / R;
   const int nb = L / R;
-  const FastDiv fnb = fastdiv(nb), fm = fastdiv(m);
   for (int w = threadIdx.x; w < P * nb; w += blockDim.x) {
     const int p = w / fnb, bj = w - p * nb;
     const int blk = bj / fm, j = bj - blk * m;
@@ -576,13 +563,15 @@ __device__ void ip_fft(const FftInplace& F, T* x, int ld, int P, int i0 = 0, int
     int S = F.L;
     for (int q = 0; q < s; ++q) S /= F.rad[q];
     const T* tw = tab<T>(F.tw) + F.off[s];
+    const FastDivC& a = F.dnb[s];
+    const FastDivC& b = F.dm[s];
     switch (F.rad[s]) {
-      case 2: ip_stage<2, DIF>(x, F.L, ld, S, P, tw); break;
-      case 3: ip_stage<3, DIF>(x, F.L, ld, S, P, tw); break;
-      case 4: ip_stage<4, DIF>(x, F.L, ld, S, P, tw); break;
-      case 5: ip_stage<5, DIF>(x, F.L, ld, S, P, tw); break;
-      case 7: ip_stage<7, DIF>(x, F.L, ld, S, P, tw); break;
-      default: ip_stage<8, DIF>(x, F.L, ld, S, P, tw); break;
+      case 2: ip_stage<2, DIF>(x, F.L, ld, S, P, tw, a, b); break;
+      case 3: ip_stage<3, DIF>(x, F.L, ld, S, P, tw, a, b); break;
+      case 4: ip_stage<4, DIF>(x, F.L, ld, S, P, tw, a, b); break;
+      case 5: ip_stage<5, DIF>(x, F.L, ld, S, P, tw, a, b); break;
+      case 7: ip_stage<7, DIF>(x, F.L, ld, S, P, tw, a, b); break;
+      default: ip_stage<8, DIF>(x, F.L, ld, S, P, tw, a, b); break;
     }
     __syncthreads();
   }
@@ -593,9 +582,8 @@ __device__ void ip_fft(const FftInplace& F, T* x, int ld, int P, int i0 = 0, int
 // output order) and the first DIT stage.  Both stages have span R and no
 // twiddles, so each butterfly keeps its R elements in registers throughout.
 template <int R, typename T>
-__device__ void ip_turn_r(T* __restrict__ x, int L, int ld, int P, const T* __restrict__ h) {
+__device__ void ip_turn_r(T* __restrict__ x, int L, int ld, int P, const T* __restrict__ h, FastDivC fnb) {
   const int nb = L / R;
-  const FastDiv fnb = fastdiv(nb);
   for (int w = threadIdx.x; w < P * nb; w += blockDim.x) {
     const int p = w / fnb, blk = w - p * nb;
     const int base = p * ld + blk * R;
@@ -613,13 +601,14 @@ __device__ void ip_turn_r(T* __restrict__ x, int L, int ld, int P, const T* __re
 
 template <typename T>
 __device__ void ip_turn(const FftInplace& F, T* x, int ld, int P, const T* h) {
+  const FastDivC& a = F.dnb[F.nst - 1];
   switch (F.rad[F.nst - 1]) {
-    case 2: ip_turn_r<2>(x, F.L, ld, P, h); break;
-    case 3: ip_turn_r<3>(x, F.L, ld, P, h); break;
-    case 4: ip_turn_r<4>(x, F.L, ld, P, h); break;
-    case 5: ip_turn_r<5>(x, F.L, ld, P, h); break;
-    case 7: ip_turn_r<7>(x, F.L, ld, P, h); break;
-    default: ip_turn_r<8>(x, F.L, ld, P, h); break;
+    case 2: ip_turn_r<2>(x, F.L, ld, P, h, a); break;
+    case 3: ip_turn_r<3>(x, F.L, ld, P, h, a); break;
+    case 4: ip_turn_r<4>(x, F.L, ld, P, h, a); break;
+    case 5: ip_turn_r<5>(x, F.L, ld, P, h, a); break;
+    case 7: ip_turn_r<7>(x, F.L, ld, P, h, a); break;
+    default: ip_turn_r<8>(x, F.L, ld, P, h, a); break;
   }
   __syncthreads();
 }
@@ -632,14 +621,15 @@ __device__ T* run_fft(const FftStages& F, T* a, T* b, int P) {
   for (int s = 0; s < F.nst; ++s) {
     const int R = F.rad[s];
     const T* stw = tab<T>(F.stw) + F.twoff[s];
+    const FastDivC &dnb = F.dnb[s], &dns = F.dns[s];
     switch (R) {
-      case 2: st_small<2>(a, b, F.L, Ns, P, stw); break;
-      case 3: st_small<3>(a, b, F.L, Ns, P, stw); break;
-      case 4: st_small<4>(a, b, F.L, Ns, P, stw); break;
-      case 5: st_small<5>(a, b, F.L, Ns, P, stw); break;
-      case 7: st_small<7>(a, b, F.L, Ns, P, stw); break;
-      case 8: st_small<8>(a, b, F.L, Ns, P, stw); break;
-      default: st_generic(a, b, F.L, Ns, R, P, tab<T>(F.tw), stw); break;
+      case 2: st_small<2>(a, b, F.L, Ns, P, stw, dnb, dns); break;
+      case 3: st_small<3>(a, b, F.L, Ns, P, stw, dnb, dns); break;
+      case 4: st_small<4>(a, b, F.L, Ns, P, stw, dnb, dns); break;
+      case 5: st_small<5>(a, b, F.L, Ns, P, stw, dnb, dns); break;
+      case 7: st_small<7>(a, b, F.L, Ns, P, stw, dnb, dns); break;
+      case 8: st_small<8>(a, b, F.L, Ns, P, stw, dnb, dns); break;
+      default: st_generic(a, b, F.L, Ns, R, P, tab<T>(F.tw), stw, dnb, F.dh1[s], F.dh[s], dns); break;
     }
     __syncthreads();
     Ns *= R;
@@ -1230,6 +1220,20 @@ std::vector<cld> fft_ld(const std::vector<cld>& a) {
 // 7s, 5s and 3s; false if L has a prime factor above 7.
 bool factor_smooth(int L, std::vector<int>& rad) { return factor_stages(L, rad, 7); }
 
+// FP32 instructions per complex point of a double-float stage of radix R
+// (butterfly and twiddle products, lazy renormalisation), from the counts
+// of the arithmetic above
+double df_stage_cost(int R) {
+  switch (R) {
+    case 2: return 38.0;
+    case 3: return 59.0;
+    case 4: return 62.0;
+    case 5: return 96.0;
+    case 7: return 123.0;
+    default: return 88.0;
+  }
+}
+
 double inplace_cost(const std::vector<int>& rad, int L) {
   double c = 0.0;
   for (size_t s = 0; s < rad.size(); ++s) c += stage_cost(rad[s], s + 1 == rad.size());
@@ -1265,7 +1269,16 @@ const double2* upload_tab(const std::vector<double2>& v, bool df, std::vector<vo
 bool upload_stages(const std::vector<int>& rad, int L, bool df, std::vector<void*>& allocs, FftStages* f) {
   f->L = L;
   f->nst = (int)rad.size();
-  for (int s = 0; s < f->nst; ++s) f->rad[s] = rad[s];
+  long long ns = 1;
+  for (int s = 0; s < f->nst; ++s) {
+    const int R = rad[s], h = (R + 1) / 2;
+    f->rad[s] = R;
+    f->dnb[s] = make_fastdiv((unsigned)(L / R));
+    f->dns[s] = make_fastdiv((unsigned)ns);
+    f->dh1[s] = make_fastdiv((unsigned)std::max(h - 1, 1));
+    f->dh[s] = make_fastdiv((unsigned)h);
+    ns *= R;
+  }
   f->tw = upload_tab(twiddles(L), df, allocs);
   // stage twiddles exp(-2 pi i t k / (Ns R)) at (t - 1) Ns + k
   std::vector<double2> stw;
@@ -1295,6 +1308,8 @@ bool upload_inplace(const std::vector<int>& rad, int L, bool df, std::vector<voi
     const int R = rad[s], m = S / R;
     f->rad[s] = R;
     f->off[s] = (int)tw.size();
+    f->dnb[s] = make_fastdiv((unsigned)(L / R));
+    f->dm[s] = make_fastdiv((unsigned)m);
     for (int q = 1; q < R; ++q)
       for (int j = 0; j < m; ++j) {
         const cld w = unit_root((long long)q * j, S);
@@ -1325,7 +1340,10 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
   double cost_s = 1e300, cost_r = 1e300, cost_b = 1e300;
   if (factor_stages(D, rad_s)) cost_s = stages_cost(rad_s, D);
   if (is_prime(D) && factor_stages(D - 1, rad_r)) cost_r = 2.0 * stages_cost(rad_r, D - 1) + 8.0 * (D - 1);
-  int M = 0;
+  // Bluestein's length: the cheapest 7-smooth M >= 2 D + 2, by the FP64
+  // model for the FP64 tables and by the double-float one for theirs
+  int M = 0, M_df = 0;
+  double cost_df = 1e300;
   for (long long c = 2LL * D + 2; c <= std::min<long long>(3LL * D, kBlueMaxM); ++c) {
     std::vector<int> r;
     if (!factor_smooth((int)c, r)) continue;
@@ -1334,6 +1352,13 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
       cost_b = cb;
       M = (int)c;
       rad_b = r;
+    }
+    double cd = 0.0;
+    for (int R : r) cd += df_stage_cost(R);
+    cd *= 2.0 * (double)c;
+    if (cd < cost_df) {
+      cost_df = cd;
+      M_df = (int)c;
     }
   }
   double fcost;
@@ -1353,7 +1378,6 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
   // host tables shared by both arithmetics
   std::vector<int> gp, gs;
   std::vector<double2> bc, chirp;
-  std::vector<cld> H;
   if (mode == FFT_RADER) {
     const int p = D, g = primitive_root(p);
     if (g == 0) return false;
@@ -1373,18 +1397,12 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
       bc[k] = make_double2((double)v.real(), (double)v.imag());
     }
   } else if (mode == FFT_BLUESTEIN) {
-    // chirp exp(-i pi j^2 / D) (exact phase index j^2 mod 2D), the kernel
-    // h_n = conj chirp_|n| on |n| < D of the cyclic length M, and its
-    // spectrum (stored conjugated over M in each plan's DIF output order)
+    // chirp exp(-i pi j^2 / D) (exact phase index j^2 mod 2D)
     chirp.resize(D);
-    std::vector<cld> hk(M, cld(0, 0));
     for (int j = 0; j < D; ++j) {
       const cld w = unit_root((long long)j * j % (2LL * D), 2LL * D);
       chirp[j] = make_double2((double)w.real(), (double)w.imag());
-      hk[j] = std::conj(w);
-      if (j > 0) hk[M - j] = std::conj(w);
     }
-    H = fft_ld(hk);
   }
   // (cos, 2 sin)(pi j / D), j = 0..D
   std::vector<double2> trig(D + 1);
@@ -1411,11 +1429,21 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
       d.bconj = upload_tab(bc, df, allocs);
       if (!d.bconj) return false;
     } else {
-      if (!factor_smooth(M, r) || !upload_inplace(r, M, df, allocs, &d.ip)) return false;
-      const std::vector<int> pos = dif_positions(M, r);
-      std::vector<double2> hrev(M);
-      for (int k = 0; k < M; ++k) {
-        const cld v = std::conj(H[k]) / (long double)M;
+      // the kernel h_n = conj chirp_|n| on |n| < D of the cyclic length Ml,
+      // and its spectrum, stored conjugated over Ml in the DIF output order
+      const int Ml = df ? M_df : M;
+      if (!factor_smooth(Ml, r) || !upload_inplace(r, Ml, df, allocs, &d.ip)) return false;
+      std::vector<cld> hk(Ml, cld(0, 0));
+      for (int j = 0; j < D; ++j) {
+        const cld w(chirp[j].x, -chirp[j].y);
+        hk[j] = w;
+        if (j > 0) hk[Ml - j] = w;
+      }
+      const std::vector<cld> H = fft_ld(hk);
+      const std::vector<int> pos = dif_positions(Ml, r);
+      std::vector<double2> hrev(Ml);
+      for (int k = 0; k < Ml; ++k) {
+        const cld v = std::conj(H[k]) / (long double)Ml;
         hrev[pos[k]] = make_double2((double)v.real(), (double)v.imag());
       }
       d.chirp = upload_tab(chirp, df, allocs);
@@ -1432,6 +1460,7 @@ bool build_fft_plan(int D, std::vector<void*>& allocs, FftPlanInfo* out) {
   out->D = D;
   out->mode = h.mode;
   out->M = (h.mode == FFT_BLUESTEIN) ? M : 0;
+  out->M_df = (h.mode == FFT_BLUESTEIN) ? M_df : 0;
   out->dev = dev;
   out->dev_df = dev + 1;
   // two lines share one complex FFT; pre/post processing about 7 per point
@@ -1462,7 +1491,8 @@ const FftPlanInfo* fft_choice(const AxisJob& J, const Tables& tb, double cost_ot
 namespace {
 
 size_t fft_smem(const FftPlanInfo& f, int P) {
-  if (f.mode == FFT_BLUESTEIN) return (size_t)padded((long long)P * f.M) * sizeof(double2);
+  if (f.mode == FFT_BLUESTEIN)
+    return (size_t)padded((long long)P * (fft_df_enabled() ? f.M_df : f.M)) * sizeof(double2);
   return (size_t)2 * padded((long long)P * (f.D + 1)) * sizeof(double2);
 }
 

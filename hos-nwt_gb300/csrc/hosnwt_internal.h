@@ -235,11 +235,28 @@ void launch_y_f2s(const Tables& tb, const double* in, int nlines, long long y_st
 constexpr int kFftMaxSt = 16;      // stages of one complex FFT
 constexpr int kFftMaxRadix = 127;  // largest odd prime factor of a stage
 
+// Division by a constant d as multiply-high (Granlund and Montgomery, 1994):
+// with s = ceil(log2 d) and m = floor(2^32 (2^s - d) / d) + 1,
+// x / d = (mulhi(x, m) + x) >> s for every 32-bit x.  The constants of
+// the FFT stage loops are set on the host with the plans.
+struct FastDivC {
+  unsigned d, m, s;
+};
+inline FastDivC make_fastdiv(unsigned d) {
+  unsigned s = 0;
+  while ((1ULL << s) < d) ++s;
+  const unsigned long long m = ((1ULL << 32) * ((1ULL << s) - d)) / d + 1ULL;
+  return FastDivC{d, (unsigned)m, s};
+}
+
 struct FftStages {
   int L;                     // complex length
   int nst;                   // number of Stockham stages
   int rad[kFftMaxSt];        // radix of each stage, in order
   int twoff[kFftMaxSt];      // offset of each stage's twiddles in stw
+  // division constants of stage s: L / R, Ns, and for an odd radix given at
+  // run time (R + 1) / 2 - 1 and (R + 1) / 2
+  FastDivC dnb[kFftMaxSt], dns[kFftMaxSt], dh1[kFftMaxSt], dh[kFftMaxSt];
   const double2* tw;         // exp(-2 pi i q / L), q = 0..L-1
   const double2* stw;        // stage twiddles: stage s (radix R, Ns the product of the
                              //   earlier radices) holds exp(-2 pi i t k / (Ns R)) at
@@ -256,6 +273,7 @@ struct FftInplace {
   int nst;
   int rad[kFftMaxSt];
   int off[kFftMaxSt];
+  FastDivC dnb[kFftMaxSt], dm[kFftMaxSt];  // division constants: L / R and m of stage s
   const double2* tw;
 };
 
@@ -278,7 +296,8 @@ struct FftDesc {
 struct FftPlanInfo {
   int D = 0;
   int mode = 0;
-  int M = 0;                 // bluestein convolution length
+  int M = 0;                 // bluestein convolution length (FP64 tables)
+  int M_df = 0;              // the same for the double-float tables
   const FftDesc* dev = nullptr;     // FP64 tables
   const FftDesc* dev_df = nullptr;  // double-float tables of the same plan
   double cost_line = 0.0;    // FP64 instructions per line (two lines share one complex FFT)
