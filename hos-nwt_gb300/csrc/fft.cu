@@ -577,6 +577,69 @@ __device__ void ip_fft(const FftInplace& F, T* x, int ld, int P, int i0 = 0, int
   }
 }
 
+// Bluestein's first DIF stage when its radix is 8: a sequence's inputs
+// j >= D are zero and D < M / 2, so butterfly j (elements j + t m, t < 8,
+// m = M / 8) has t >= 4 zero and t = 3 zero for j + 3 m >= D; the
+// radix-8 DFT of (a0, a1, a2, a3, 0, 0, 0, 0) takes half the adds of the
+// first level.  The padding is never read, so it needs no zero fill.
+template <typename T>
+__device__ void ip_first_dif8(T* __restrict__ x, int ld, int P, const T* __restrict__ tw, FastDivC fm, int m, int D) {
+  constexpr auto r = Ar<T>::k(0.70710678118654752440);
+  for (int w = threadIdx.x; w < P * m; w += blockDim.x) {
+    const int p = w / fm, j = w - p * m;
+    const int base = p * ld + j;
+    T a[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) a[t] = (j + t * m < D) ? x[pz(base + t * m)] : czero<T>();
+    // dft4 of (x0, x1, 0, 0): x0 + x1, x0 - i x1, x0 - x1, x0 + i x1
+    T e[4] = {cadd(a[0], a[2]), cadd(a[0], cmi(a[2])), csub(a[0], a[2]), csub(a[0], cmi(a[2]))};
+    T o[4] = {cadd(a[1], a[3]), cadd(a[1], cmi(a[3])), csub(a[1], a[3]), csub(a[1], cmi(a[3]))};
+    o[1] = crot1(r, o[1]);
+    o[2] = cmi(o[2]);
+    o[3] = crot3(r, o[3]);
+    T v[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      v[k] = cadd(e[k], o[k]);
+      v[k + 4] = csub(e[k], o[k]);
+    }
+    if (j != 0) {
+#pragma unroll
+      for (int t = 1; t < 8; ++t) v[t] = cmul(v[t], ldt(tw + (t - 1) * m + j));
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) x[pz(base + t * m)] = cnorm(v[t]);
+  }
+}
+
+// Bluestein's last DIT stage when its radix is 8, for outputs k <= kneed <
+// 2 m only: butterfly j yields k = j and k = j + m, the first two outputs
+// of its radix-8 DFT, and no butterfly with j > kneed is needed.
+template <typename T>
+__device__ void ip_last_dit8(T* __restrict__ x, int ld, int P, const T* __restrict__ tw, FastDivC fm, int m,
+                             int kneed) {
+  constexpr auto r = Ar<T>::k(0.70710678118654752440);
+  for (int w = threadIdx.x; w < P * m; w += blockDim.x) {
+    const int p = w / fm, j = w - p * m;
+    if (j > kneed) continue;
+    const int base = p * ld + j;
+    T v[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) v[t] = x[pz(base + t * m)];
+    if (j != 0) {
+#pragma unroll
+      for (int t = 1; t < 8; ++t) v[t] = cmul(v[t], ldt(tw + (t - 1) * m + j));
+    }
+    // outputs 0 and 1 of the radix-8 DFT, as dft8 forms them
+    const T e0 = cadd(cadd(v[0], v[4]), cadd(v[2], v[6]));
+    const T e1 = cadd(csub(v[0], v[4]), cmi(csub(v[2], v[6])));
+    const T o0 = cadd(cadd(v[1], v[5]), cadd(v[3], v[7]));
+    const T o1 = crot1(r, cadd(csub(v[1], v[5]), cmi(csub(v[3], v[7]))));
+    x[pz(base)] = cnorm(cadd(e0, o0));
+    if (j + m <= kneed) x[pz(base + m)] = cnorm(cadd(e1, o1));
+  }
+}
+
 // The turn of Bluestein's convolution in one pass: the last DIF stage, the
 // product with the conjugated kernel spectrum h (conj(x) h, in the DIF
 // output order) and the first DIT stage.  Both stages have span R and no
@@ -773,8 +836,8 @@ __global__ void __launch_bounds__(NT, NT == kFT ? HOSNWT_FFT_MIN_BLOCKS : 1)
       if (blue) v = cmul(cnorm(v), ldt(tab<dfc>(F.chirp) + j));  // Bluestein's premultiply
       A[pz(l * zld + j)] = cnorm(v);
     }
-    if (blue) {
-      // the convolution's zero padding
+    if (blue && F.ip.rad[0] != 8) {
+      // the convolution's zero padding (a radix-8 first stage never reads it)
       const int pad = zld - D;
       for (int w = tid; w < P * pad; w += blockDim.x) {
         const int p = w / pad;
@@ -818,9 +881,23 @@ __global__ void __launch_bounds__(NT, NT == kFT ? HOSNWT_FFT_MIN_BLOCKS : 1)
     // as below, with the premultiply done by the load loop, the turn in one
     // pass (ip_turn) and the postmultiply by the unpack
     const int M = zld;
-    ip_fft<true>(F.ip, A, M, P, 0, F.ip.nst - 1);
-    ip_turn(F.ip, A, M, P, tab<T>(F.hrev));
-    ip_fft<false>(F.ip, A, M, P, 1, F.ip.nst);
+    const FftInplace& I = F.ip;
+    if (I.rad[0] == 8) {
+      ip_first_dif8(A, M, P, tab<T>(I.tw) + I.off[0], I.dm[0], M / 8, D);
+      __syncthreads();
+      ip_fft<true>(I, A, M, P, 1, I.nst - 1);
+    } else {
+      ip_fft<true>(I, A, M, P, 0, I.nst - 1);
+    }
+    ip_turn(I, A, M, P, tab<T>(F.hrev));
+    if (I.rad[0] == 8) {
+      // the unpack reads outputs k <= D / 2 < M / 4
+      ip_fft<false>(I, A, M, P, 1, I.nst - 1);
+      ip_last_dit8(A, M, P, tab<T>(I.tw) + I.off[0], I.dm[0], M / 8, D / 2);
+      __syncthreads();
+    } else {
+      ip_fft<false>(I, A, M, P, 1, I.nst);
+    }
     Z = A;
     O = nullptr;  // rows in each sequence's free tail, see orow
   } else if (blue) {
