@@ -845,24 +845,24 @@ __global__ void __launch_bounds__(NT, NT == kFT ? HOSNWT_FFT_MIN_BLOCKS : 1)
       }
     }
   } else {
-  for (int w = tid; w < NL * D; w += blockDim.x) {
-    const int j = w / NL;
-    double ua = U(j), ub = U(D - j);
-    const double2 cs = __ldg(F.trig + j);  // (cos, 2 sin)(theta_j)
-    double t;
-    if (j == 0) {
-      ua *= J.e0;
-      ub *= J.eD;
-      t = is_sin ? 0.0 : 2.0 * (ua + ub);
-      c1 += ua - ub;
-    } else if (!is_sin) {
-      t = fma(-cs.y, ua - ub, ua + ub);
-      c1 = fma(ua, cs.x, c1);
-    } else {
-      t = fma(cs.y, ua + ub, ua - ub);
+    for (int w = tid; w < NL * D; w += blockDim.x) {
+      const int j = w / NL;
+      double ua = U(j), ub = U(D - j);
+      const double2 cs = __ldg(F.trig + j);  // (cos, 2 sin)(theta_j)
+      double t;
+      if (j == 0) {
+        ua *= J.e0;
+        ub *= J.eD;
+        t = is_sin ? 0.0 : 2.0 * (ua + ub);
+        c1 += ua - ub;
+      } else if (!is_sin) {
+        t = fma(-cs.y, ua - ub, ua + ub);
+        c1 = fma(ua, cs.x, c1);
+      } else {
+        t = fma(cs.y, ua + ub, ua - ub);
+      }
+      put_part(A + pz((l >> 1) * zld + j), l & 1, t);
     }
-    put_part(A + pz((l >> 1) * zld + j), l & 1, t);
-  }
   }
   if (!DF && !is_sin) {
     // lanes with the same line: lane = l (mod NL)
@@ -971,61 +971,61 @@ __global__ void __launch_bounds__(NT, NT == kFT ? HOSNWT_FFT_MIN_BLOCKS : 1)
     }
     __syncthreads();
   } else {
-  for (int w = tid; w < P * (ne + 1); w += blockDim.x) {
-    const int p = w / (ne + 1), m = w - p * (ne + 1);
-    const double2 z1 = Z[pz(p * zld + m)];
-    const double2 z2 = Z[pz(p * zld + (m == 0 ? 0 : D - m))];
-    // 2 T_a = z1 + conj z2, 2 T_b = (z1 - conj z2) / i: real parts tr,
-    // imaginary parts with the sign flipped nti
-    const double tr[2] = {z1.x + z2.x, z1.y + z2.y};
-    const double nti[2] = {z2.y - z1.y, z1.x - z2.x};
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      double* o = orow(2 * p + h);
-      if (!is_sin) {
-        o[2 * m] = tr[h];
-        if (m >= 1 && m <= no) o[2 * m + 1] = nti[h];
-      } else {
-        o[2 * m] = nti[h];
-        if (m == 0) {
-          o[1] = 0.5 * tr[h];
-        } else if (m <= no) {
-          o[2 * m + 1] = tr[h];
+    for (int w = tid; w < P * (ne + 1); w += blockDim.x) {
+      const int p = w / (ne + 1), m = w - p * (ne + 1);
+      const double2 z1 = Z[pz(p * zld + m)];
+      const double2 z2 = Z[pz(p * zld + (m == 0 ? 0 : D - m))];
+      // 2 T_a = z1 + conj z2, 2 T_b = (z1 - conj z2) / i: real parts tr,
+      // imaginary parts with the sign flipped nti
+      const double tr[2] = {z1.x + z2.x, z1.y + z2.y};
+      const double nti[2] = {z2.y - z1.y, z1.x - z2.x};
+  #pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        double* o = orow(2 * p + h);
+        if (!is_sin) {
+          o[2 * m] = tr[h];
+          if (m >= 1 && m <= no) o[2 * m + 1] = nti[h];
+        } else {
+          o[2 * m] = nti[h];
+          if (m == 0) {
+            o[1] = 0.5 * tr[h];
+          } else if (m <= no) {
+            o[2 * m + 1] = tr[h];
+          }
         }
       }
     }
-  }
-  if (!is_sin && tid < NL) {
-    double s = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][tid];
-    orow(tid)[1] = 4.0 * s;
-  }
-  __syncthreads();
-
-  // ---- odd outputs: inclusive prefix sums over O[1], O[3], ..., O[2 no + 1]
-  {
-    const int n = no + 1;
-    const int c = (n + 31) / 32;
-    for (int ll = warp; ll < NL; ll += (int)(blockDim.x >> 5)) {
-      double* o = orow(ll) + 1;
-      const int i0 = min(lane * c, n), i1 = min(i0 + c, n);
+    if (!is_sin && tid < NL) {
       double s = 0.0;
-      for (int i = i0; i < i1; ++i) s += o[2 * i];
-      double incl = s;
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const double v = __shfl_up_sync(0xffffffffu, incl, off);
-        if (lane >= off) incl += v;
-      }
-      double run = __shfl_up_sync(0xffffffffu, incl, 1);
-      if (lane == 0) run = 0.0;
-      for (int i = i0; i < i1; ++i) {
-        run += o[2 * i];
-        o[2 * i] = run;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w][tid];
+      orow(tid)[1] = 4.0 * s;
+    }
+    __syncthreads();
+
+    // ---- odd outputs: inclusive prefix sums over O[1], O[3], ..., O[2 no + 1]
+    {
+      const int n = no + 1;
+      const int c = (n + 31) / 32;
+      for (int ll = warp; ll < NL; ll += (int)(blockDim.x >> 5)) {
+        double* o = orow(ll) + 1;
+        const int i0 = min(lane * c, n), i1 = min(i0 + c, n);
+        double s = 0.0;
+        for (int i = i0; i < i1; ++i) s += o[2 * i];
+        double incl = s;
+  #pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const double v = __shfl_up_sync(0xffffffffu, incl, off);
+          if (lane >= off) incl += v;
+        }
+        double run = __shfl_up_sync(0xffffffffu, incl, 1);
+        if (lane == 0) run = 0.0;
+        for (int i = i0; i < i1; ++i) {
+          run += o[2 * i];
+          o[2 * i] = run;
+        }
       }
     }
-  }
-  __syncthreads();
+    __syncthreads();
   }
 
   // ---- scale and store (line fastest, like the loads)
