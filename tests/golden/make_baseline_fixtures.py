@@ -2,13 +2,16 @@
 (tests/golden/baseline_{c1,c2,c3,c5}.npz; cases in tests/baseline_cases.py):
 
   python tests/golden/make_baseline_fixtures.py [--threads N] [c1 c2 c3 c5]
+  python tests/golden/make_baseline_fixtures.py [--threads N] --loop-only c3
 
 Per case: one solveHOS2 on a seeded modal state, one runge4_adapt2 on a
 seeded physical state (after one right-hand side at the step's start time,
 which sets the wavemaker state the step's first volume correction reads),
-and, for c1 and c2, the time loop from the initial condition with the probe
-records.  The oracle's transforms use N threads (default 1); c5 takes
-several minutes.
+and, for c1, c2 and c3, the time loop from the initial condition with the
+probe records (c3: its first simulated second, the final eta as a sampled
+record).  --loop-only adds the loop records to an existing fixture.  The
+oracle's transforms use N threads (default 1); c5 and the c3 loop take
+tens of minutes.
 """
 import os
 import sys
@@ -24,7 +27,7 @@ import numpy as np  # noqa: E402
 
 import baseline_cases as bc  # noqa: E402
 
-LOOP_T = {"c1": None, "c2": 10.0}   # simulated seconds of the time loop (None: the whole run)
+LOOP_T = {"c1": None, "c2": 10.0, "c3": 1.0}   # simulated seconds of the time loop (None: the whole run)
 
 
 def rhs_case(name, w, out, full):
@@ -56,7 +59,7 @@ def step_case(name, w, out, full):
             out.update(bc.summarize("step_" + key, res[key], 200 + i))
 
 
-def loop_case(w, out, T):
+def loop_case(name, w, out, T):
     inp = dict(w["inp"])
     if T is not None:
         inp["T_stop"] = T
@@ -65,7 +68,10 @@ def loop_case(w, out, T):
     recs = o.run()
     out["loop_t"] = np.array([r[0] for r in recs])
     out["loop_probes"] = np.array([r[1] for r in recs])
-    out["loop_eta"] = o.eta
+    if name in bc.SAMPLED:
+        out.update(bc.summarize("loop_eta", o.eta, 300))
+    else:
+        out["loop_eta"] = o.eta
     out["loop_T_stop"] = np.array([inp["T_stop"]])
     out["h"] = np.array([o.h])
     out["Hs"] = np.array([w["Hs"]])
@@ -80,9 +86,20 @@ def make(name):
         rhs_case(name, w, out, full)
         step_case(name, w, out, full)
         if name in LOOP_T:
-            loop_case(w, out, LOOP_T[name])
+            loop_case(name, w, out, LOOP_T[name])
     np.savez_compressed(os.path.join(HERE, f"baseline_{name}.npz"), **out)
     print(name, f"{time.perf_counter() - t0:.1f} s", flush=True)
+
+
+def add_loop(name):
+    """Add the time-loop records to an existing fixture, keeping its others."""
+    t0 = time.perf_counter()
+    path = os.path.join(HERE, f"baseline_{name}.npz")
+    out = dict(np.load(path))
+    with tempfile.TemporaryDirectory() as tmp:
+        loop_case(name, bc.spec(name, tmp), out, LOOP_T[name])
+    np.savez_compressed(path, **out)
+    print(name, f"loop {time.perf_counter() - t0:.1f} s", flush=True)
 
 
 if __name__ == "__main__":
@@ -91,5 +108,9 @@ if __name__ == "__main__":
         import oracle.hos_oracle as ho
         ho.set_workers(int(args[1]))
         args = args[2:]
-    for n in (args or ["c1", "c2", "c3", "c5"]):
-        make(n)
+    if args[:1] == ["--loop-only"]:
+        for n in args[1:]:
+            add_loop(n)
+    else:
+        for n in (args or ["c1", "c2", "c3", "c5"]):
+            make(n)

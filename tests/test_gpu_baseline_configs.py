@@ -5,7 +5,8 @@ ABI, against the oracle's fixtures (tests/golden/baseline_*.npz):
   c2  irregular_2d    (n1 = 1025, M = 5, p1 = 5, 512 components): RHS, step,
                       the first 10 s of the time loop
   c3  directional_3d  (513 x 257, M = 5, p = 4): RHS, step (sampled entries,
-                      max |.|, sum of squares and random projections)
+                      max |.|, sum of squares and random projections), the
+                      first simulated second of the time loop
   c5  steep_3d        (1025 x 513, M = 7, p = 7): RHS, step (sampled)
 
 Tolerances (FP64, different summation orders):
@@ -86,7 +87,7 @@ def test_step(lib, name):
           f"{abs(err - ref_err) / max(ref_err, 1e-12):.2e}")
 
 
-@pytest.mark.parametrize("name", ["c1", "c2"])
+@pytest.mark.parametrize("name", ["c1", "c2", "c3"])
 def test_time_loop(lib, name):
     fx = bc.load(name)
     with tempfile.TemporaryDirectory() as tmp:
@@ -102,6 +103,17 @@ def test_time_loop(lib, name):
     p = np.array([r[1] for r in recs])
     assert np.max(np.abs(t - t_ref)) < 1e-12
     h, Hs = float(fx["h"][0]), float(fx["Hs"][0])
-    assert np.max(np.abs(p - p_ref)) * h / Hs <= 1e-9
-    assert np.max(np.abs(p - p_ref)) / np.max(np.abs(p_ref)) <= 1e-8
-    assert np.max(np.abs(eta - fx["loop_eta"])) * h / Hs <= 1e-9
+    dp = np.max(np.abs(p - p_ref))
+    assert dp * h / Hs <= 1e-9
+    assert dp / np.max(np.abs(p_ref)) <= 1e-8
+    if name in bc.SAMPLED:
+        # the final eta as a sampled record: max |d eta| / Hs <= 1e-9 is a
+        # deviation of 1e-9 Hs / (h max |eta_ref|) relative to max |eta_ref|
+        ref_max = float(fx["loop_eta_max"][0])
+        de = bc.compare_summary(fx, "loop_eta", eta, 300, 1e-9 * Hs / (h * ref_max))
+        de_hs = de * ref_max * h / Hs
+    else:
+        de_hs = np.max(np.abs(eta - fx["loop_eta"])) * h / Hs
+        assert de_hs <= 1e-9
+    print(f"loop {name}: {len(recs)} records, max |d probe| h/Hs {dp * h / Hs:.2e}, "
+          f"relative {dp / np.max(np.abs(p_ref)):.2e}; eta {de_hs:.2e} of Hs")
